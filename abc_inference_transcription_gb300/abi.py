@@ -1,0 +1,163 @@
+"""ctypes mirror of include/abcgpu.h and the loader of libabcgpu.so.
+
+The structures here are byte-for-byte the C structs of the ABI; the oracle's
+test wrapper reuses them.  Loading the library never falls back to anything:
+if libabcgpu.so is missing the import of the product path fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+MAX_AGES = 8
+MAX_CONDS = 16
+MAX_STEPS = 8
+MAX_PARAMS = 32
+
+OK = 0
+ERR_INVALID = -1
+ERR_CUDA = -2
+ERR_NOMEM = -3
+ERR_EVENT_CAP = -4
+ERR_NONFINITE = -5
+ERR_CAPACITY = -6
+ERR_STATE = -7
+
+STATUS_NAMES = {
+    OK: "ABC_OK", ERR_INVALID: "ABC_ERR_INVALID", ERR_CUDA: "ABC_ERR_CUDA",
+    ERR_NOMEM: "ABC_ERR_NOMEM", ERR_EVENT_CAP: "ABC_ERR_EVENT_CAP",
+    ERR_NONFINITE: "ABC_ERR_NONFINITE", ERR_CAPACITY: "ABC_ERR_CAPACITY",
+    ERR_STATE: "ABC_ERR_STATE",
+}
+
+# model index m of wrapper.jl:47-51
+MODEL_NAMES = ["const", "const_const", "kon", "alpha", "gamma"]
+FP64 = 0
+FP32 = 1
+
+
+class AbcConfig(C.Structure):
+    _fields_ = [
+        ("cycle", C.c_double),
+        ("n_burn_cycles", C.c_int32),
+        ("n_steps", C.c_int32),
+        ("n_ages", C.c_int32),
+        ("n_conds", C.c_int32),
+        ("ages", C.c_double * MAX_AGES),
+        ("pulse", C.c_double * MAX_CONDS),
+        ("chase", C.c_double * MAX_CONDS),
+        ("pulse_stat_cond", C.c_int32),
+        ("chase_stat_cond", C.c_int32),
+        ("splicing", C.c_int32),
+        ("scaling_column", C.c_int32),
+        ("precision", C.c_int32),
+        ("reserved0", C.c_int32),
+        ("event_cap", C.c_int64),
+    ]
+
+
+class AbcPrior(C.Structure):
+    _fields_ = [
+        ("kon", C.c_double * 2), ("koff", C.c_double * 2), ("alpha", C.c_double * 2),
+        ("gamma", C.c_double * 2), ("lambda_", C.c_double * 2), ("beta", C.c_double * 2),
+        ("scaling", C.c_double * 2), ("vary_mode", C.c_int32), ("reserved0", C.c_int32),
+        ("factor", C.c_double * 2),
+    ]
+
+
+def nstats(n_ages: int, n_conds: int) -> int:
+    """4A + 3J, scripts/compute_errors.jl:148."""
+    return 4 * n_ages + 3 * n_conds
+
+
+def num_params(cfg: AbcConfig, model: int) -> int:
+    """theta columns: get_vary_map (scripts/model.jl:30-43) + lambda + extensions."""
+    if model not in (1, 2, 3, 4, 5):
+        raise ValueError(f"model must be 1..5, got {model}")
+    return 5 + (cfg.n_steps - 1 if model >= 3 else 0) + int(bool(cfg.splicing)) + int(bool(cfg.scaling_column))
+
+
+def ptr(a: np.ndarray | None, ctype=C.c_double):
+    if a is None:
+        return None
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG_DIR, "_build", "libabcgpu.so")
+
+
+class AbcError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+_lib = None
+
+
+def load_library(path: str | None = None) -> C.CDLL:
+    """Load libabcgpu.so (built by abc_inference_transcription_gb300.build)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ImportError(
+            f"{p} not found: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+            "(there is no CPU fallback)")
+    lib = C.CDLL(p)
+    _declare(lib)
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _declare(lib: C.CDLL) -> None:
+    vp = C.c_void_p
+    dp = C.POINTER(C.c_double)
+    i32p = C.POINTER(C.c_int32)
+    i64p = C.POINTER(C.c_int64)
+    u64p = C.POINTER(C.c_uint64)
+    i64 = C.c_int64
+    u64 = C.c_uint64
+    sig = {
+        "abc_create": (C.c_int, [C.POINTER(vp), C.POINTER(AbcConfig)]),
+        "abc_destroy": (C.c_int, [vp]),
+        "abc_last_error": (C.c_char_p, [vp]),
+        "abc_num_params": (C.c_int, [vp, C.c_int]),
+        "abc_num_stats": (C.c_int, [vp]),
+        "abc_stream": (vp, [vp]),
+        "abc_set_cells": (C.c_int, [vp, i64, i32p, i32p, dp, dp]),
+        "abc_sample_prior": (C.c_int, [vp, C.c_int, i64, u64, i64, C.POINTER(AbcPrior), dp]),
+        "abc_simulate": (C.c_int, [vp, C.c_int, dp, i64, u64, i64, dp]),
+        "abc_simulate_device": (C.c_int, [vp, C.c_int, vp, i64, u64, i64, vp]),
+        "abc_synchronize": (C.c_int, [vp]),
+        "abc_simulate_batch": (C.c_int, [vp, i32p, dp, i64, i64, u64, i64, dp]),
+        "abc_simulate_batch_device": (C.c_int, [vp, vp, vp, i64, i64, u64, i64, vp]),
+        "abc_simulate_cells": (C.c_int, [vp, C.c_int, dp, i64, u64, i64, i32p, i32p, i64p, u64p, dp]),
+        "abc_last_counters": (C.c_int, [vp, i64p, i64p]),
+        "abc_profile": (C.c_int, [vp, C.c_int]),
+        "abc_profile_read": (C.c_int, [vp, dp]),
+        "abc_errors": (C.c_int, [vp, dp, dp, i64, C.c_int, C.c_int, i32p, dp, i64, dp]),
+        "abc_errors_select": (C.c_int, [vp, dp, dp, i64, C.c_int, C.c_int, i32p, dp, i64, C.c_int,
+                                        C.c_double, i64p]),
+        "abc_accept_fetch": (C.c_int, [vp, i64p, i64p, dp]),
+        "abc_select_counters": (C.c_int, [vp, i64p, i64p]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+# Every symbol include/abcgpu.h declares (checked by the CPU test suite).
+ABI_SYMBOLS = [
+    "abc_create", "abc_destroy", "abc_last_error", "abc_num_params", "abc_num_stats",
+    "abc_stream", "abc_set_cells", "abc_sample_prior", "abc_simulate", "abc_simulate_device",
+    "abc_synchronize", "abc_simulate_batch", "abc_simulate_batch_device", "abc_simulate_cells", "abc_last_counters",
+    "abc_profile", "abc_profile_read", "abc_errors",
+    "abc_errors_select", "abc_accept_fetch", "abc_select_counters",
+]

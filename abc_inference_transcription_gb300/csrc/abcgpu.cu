@@ -1,0 +1,768 @@
+// abcgpu.cu — the C ABI (include/abcgpu.h): context, device memory, stream,
+// and the host-side orchestration of the kernels.  No compute happens on the
+// host; without a CUDA device every call fails with ABC_ERR_CUDA.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/abcgpu.h"
+#include "distance.cuh"
+#include "kernels.h"
+
+using namespace abc;
+
+namespace {
+
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t cap = 0;  // elements
+  cudaError_t ensure(size_t n) {
+    if (n <= cap && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = std::max<size_t>(n, 1);
+    cudaError_t e = cudaMalloc((void**)&p, want * sizeof(T));
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+constexpr size_t kChunkBytes = size_t(2) << 30;  // counts buffer budget per simulate chunk
+
+}  // namespace
+
+struct abc_ctx {
+  abc_config cfg;
+  DevCfg dcfg;
+  int device = 0;
+  int sms = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // cells, internal order = sorted by group (cond*A + age)
+  bool cells_set = false;
+  int64_t C = 0;
+  std::vector<int64_t> perm;  // internal -> caller index
+  DBuf<int32_t> d_cond, d_age, d_gstart;
+  DBuf<uint32_t> d_id;
+  DBuf<double> d_beta, d_age_dist;
+  // simulation workspace
+  DBuf<double> d_theta, d_stats;
+  DBuf<int32_t> d_models;
+  DBuf<PRec> d_rec;
+  DBuf<PRecF> d_recf;
+  DBuf<int2> d_counts, d_captured;
+  DBuf<int64_t> d_events;
+  DBuf<uint64_t> d_hash;
+  DBuf<unsigned long long> d_misc;  // [0] work counter, [1] events, [2] rejections
+  DBuf<int> d_status;
+  int64_t last_events = 0, last_rej = 0;
+  // per-phase device timing (abc_profile): 4 events per chunk
+  bool prof = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  double phase_ms[3] = {0, 0, 0};
+  // selection workspace and results
+  DBuf<double> d_data, d_se, d_sel_stats, d_e64, d_se64, d_out_err;
+  DBuf<float> d_sw, d_dw, d_s32, d_X, d_esub;
+  DBuf<Cand> d_cand;
+  DBuf<int32_t> d_sp;
+  DBuf<int64_t> d_gcount, d_goff, d_alen, d_aoff, d_out_idx;
+  DBuf<unsigned long long> d_gcursor, d_ncand;
+  DBuf<int> d_fail;
+  int64_t cand_cap = int64_t(1) << 22;
+  int64_t sel_G = 0, sel_total = 0, sel_cands = 0, sel_rechecked = 0;
+  bool sel_ready = false;
+};
+
+static int fail(abc_ctx* c, int status, const std::string& msg) {
+  if (c) c->err = msg;
+  return status;
+}
+
+static int cuda_fail(abc_ctx* c, cudaError_t e, const char* where) {
+  return fail(c, e == cudaErrorMemoryAllocation ? ABC_ERR_NOMEM : ABC_ERR_CUDA,
+              std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                   \
+  do {                                             \
+    cudaError_t e_ = (call);                       \
+    if (e_ != cudaSuccess) return cuda_fail(c, e_, #call); \
+  } while (0)
+
+static int validate_config(const abc_config* cfg, std::string& msg) {
+  if (!(cfg->cycle > 0.0) || !std::isfinite(cfg->cycle)) return msg = "cycle must be > 0", ABC_ERR_INVALID;
+  if (cfg->n_steps < 1 || cfg->n_steps > ABC_MAX_STEPS) return msg = "n_steps out of range", ABC_ERR_INVALID;
+  if (cfg->n_ages < 1 || cfg->n_ages > ABC_MAX_AGES) return msg = "n_ages out of range", ABC_ERR_INVALID;
+  if (cfg->n_conds < 1 || cfg->n_conds > ABC_MAX_CONDS) return msg = "n_conds out of range", ABC_ERR_INVALID;
+  if (cfg->n_burn_cycles < 1) return msg = "n_burn_cycles must be >= 1", ABC_ERR_INVALID;
+  if (cfg->pulse_stat_cond < 0 || cfg->pulse_stat_cond >= cfg->n_conds || cfg->chase_stat_cond < 0 ||
+      cfg->chase_stat_cond >= cfg->n_conds)
+    return msg = "pulse/chase statistic condition out of range", ABC_ERR_INVALID;
+  if (cfg->precision != ABC_FP64 && cfg->precision != ABC_FP32) return msg = "bad precision", ABC_ERR_INVALID;
+  const double t0 = -(double)cfg->n_burn_cycles * cfg->cycle;
+  for (int a = 0; a < cfg->n_ages; ++a)
+    if (!(cfg->ages[a] > 0.0 && cfg->ages[a] < cfg->cycle)) return msg = "ages must lie in (0, cycle)", ABC_ERR_INVALID;
+  for (int j = 0; j < cfg->n_conds; ++j) {
+    if (!(cfg->pulse[j] > 0.0) || !(cfg->chase[j] >= 0.0)) return msg = "pulse must be > 0, chase >= 0", ABC_ERR_INVALID;
+    for (int a = 0; a < cfg->n_ages; ++a) {
+      double texp = (cfg->ages[a] - cfg->pulse[j]) - cfg->chase[j];
+      if (!(texp > t0)) return msg = "labelling starts before the simulated horizon", ABC_ERR_INVALID;
+    }
+  }
+  return ABC_OK;
+}
+
+static DevCfg make_dcfg(const abc_config* cfg) {
+  DevCfg d;
+  memset(&d, 0, sizeof(d));
+  d.cycle = cfg->cycle;
+  d.step_len = cfg->cycle / (double)cfg->n_steps;
+  d.t0 = -(double)cfg->n_burn_cycles * cfg->cycle;
+  for (int a = 0; a < ABC_MAX_AGES; ++a) d.ages[a] = cfg->ages[a];
+  for (int j = 0; j < ABC_MAX_CONDS; ++j) {
+    d.pulse[j] = cfg->pulse[j];
+    d.chase[j] = cfg->chase[j];
+  }
+  d.event_cap = cfg->event_cap;
+  d.n_steps = cfg->n_steps;
+  d.n_ages = cfg->n_ages;
+  d.n_conds = cfg->n_conds;
+  d.splicing = cfg->splicing ? 1 : 0;
+  d.scaling_column = cfg->scaling_column ? 1 : 0;
+  d.pulse_stat = cfg->pulse_stat_cond;
+  d.chase_stat = cfg->chase_stat_cond;
+  d.npar = 0;
+  return d;
+}
+
+static int npar_of(const abc_config* cfg, int model) {
+  if (model < 1 || model > 5) return ABC_ERR_INVALID;
+  return 5 + (model >= 3 ? cfg->n_steps - 1 : 0) + (cfg->splicing ? 1 : 0) + (cfg->scaling_column ? 1 : 0);
+}
+
+extern "C" {
+
+int abc_create(abc_ctx** out, const abc_config* cfg) {
+  if (!out || !cfg) return ABC_ERR_INVALID;
+  *out = nullptr;
+  std::string msg;
+  int st = validate_config(cfg, msg);
+  if (st) {
+    fprintf(stderr, "abc_create: %s\n", msg.c_str());
+    return st;
+  }
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return ABC_ERR_CUDA;
+  abc_ctx* c = new (std::nothrow) abc_ctx();
+  if (!c) return ABC_ERR_NOMEM;
+  c->cfg = *cfg;
+  c->dcfg = make_dcfg(cfg);
+  c->device = dev;
+  if (cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return ABC_ERR_CUDA;
+  }
+  if (c->d_misc.ensure(4) || c->d_status.ensure(1)) {
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return ABC_ERR_NOMEM;
+  }
+  *out = c;
+  return ABC_OK;
+}
+
+int abc_destroy(abc_ctx* c) {
+  if (!c) return ABC_OK;
+  cudaStreamSynchronize(c->stream);
+  c->d_cond.release(); c->d_age.release(); c->d_gstart.release(); c->d_id.release();
+  c->d_beta.release(); c->d_age_dist.release(); c->d_theta.release(); c->d_stats.release();
+  c->d_models.release(); c->d_rec.release(); c->d_recf.release(); c->d_counts.release(); c->d_captured.release();
+  c->d_events.release(); c->d_hash.release(); c->d_misc.release(); c->d_status.release();
+  c->d_data.release(); c->d_se.release(); c->d_sel_stats.release(); c->d_e64.release(); c->d_se64.release();
+  c->d_out_err.release(); c->d_sw.release(); c->d_dw.release(); c->d_s32.release(); c->d_X.release();
+  c->d_esub.release(); c->d_cand.release(); c->d_sp.release(); c->d_gcount.release(); c->d_goff.release();
+  c->d_alen.release(); c->d_aoff.release(); c->d_out_idx.release(); c->d_gcursor.release();
+  c->d_ncand.release(); c->d_fail.release();
+  for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return ABC_OK;
+}
+
+const char* abc_last_error(const abc_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int abc_num_params(const abc_ctx* c, int model) {
+  if (!c) return ABC_ERR_INVALID;
+  return npar_of(&c->cfg, model);
+}
+
+int abc_num_stats(const abc_ctx* c) {
+  if (!c) return ABC_ERR_INVALID;
+  return ABC_NSTATS(c->cfg.n_ages, c->cfg.n_conds);
+}
+
+void* abc_stream(abc_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int abc_set_cells(abc_ctx* c, int64_t n_cells, const int32_t* cell_cond, const int32_t* cell_age,
+                  const double* cell_beta, const double* age_dist) {
+  if (!c) return ABC_ERR_INVALID;
+  if (n_cells < 2 || n_cells > (int64_t(1) << 31) || !cell_cond || !cell_age || !cell_beta || !age_dist)
+    return fail(c, ABC_ERR_INVALID, "abc_set_cells: bad arguments");
+  const int A = c->cfg.n_ages, J = c->cfg.n_conds, NG = A * J;
+  std::vector<int64_t> count(NG, 0);
+  for (int64_t i = 0; i < n_cells; ++i) {
+    if (cell_cond[i] < 0 || cell_cond[i] >= J || cell_age[i] < 0 || cell_age[i] >= A)
+      return fail(c, ABC_ERR_INVALID, "abc_set_cells: condition or age group out of range");
+    if (!(cell_beta[i] >= 0.0 && cell_beta[i] <= 1.0))
+      return fail(c, ABC_ERR_INVALID, "abc_set_cells: capture efficiency outside [0, 1]");
+    count[cell_cond[i] * A + cell_age[i]]++;
+  }
+  for (int g = 0; g < NG; ++g)
+    if (count[g] < 2) return fail(c, ABC_ERR_INVALID, "abc_set_cells: every (condition, age) group needs >= 2 cells");
+  for (int i = 0; i < NG; ++i)
+    if (!std::isfinite(age_dist[i])) return fail(c, ABC_ERR_INVALID, "abc_set_cells: non-finite weight");
+  std::vector<int64_t> perm(n_cells);
+  for (int64_t i = 0; i < n_cells; ++i) perm[i] = i;
+  std::stable_sort(perm.begin(), perm.end(), [&](int64_t x, int64_t y) {
+    return cell_cond[x] * A + cell_age[x] < cell_cond[y] * A + cell_age[y];
+  });
+  std::vector<int32_t> hc(n_cells), ha(n_cells), gs(NG + 1, 0);
+  std::vector<uint32_t> hid(n_cells);
+  std::vector<double> hb(n_cells);
+  for (int64_t i = 0; i < n_cells; ++i) {
+    int64_t s = perm[i];
+    hc[i] = cell_cond[s];
+    ha[i] = cell_age[s];
+    hid[i] = (uint32_t)s;
+    hb[i] = cell_beta[s];
+  }
+  for (int g = 0; g < NG; ++g) gs[g + 1] = gs[g] + (int32_t)count[g];
+  CK(cudaStreamSynchronize(c->stream));
+  CK(c->d_cond.ensure(n_cells));
+  CK(c->d_age.ensure(n_cells));
+  CK(c->d_id.ensure(n_cells));
+  CK(c->d_beta.ensure(n_cells));
+  CK(c->d_gstart.ensure(NG + 1));
+  CK(c->d_age_dist.ensure(NG));
+  CK(cudaMemcpy(c->d_cond.p, hc.data(), sizeof(int32_t) * n_cells, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->d_age.p, ha.data(), sizeof(int32_t) * n_cells, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->d_id.p, hid.data(), sizeof(uint32_t) * n_cells, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->d_beta.p, hb.data(), sizeof(double) * n_cells, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->d_gstart.p, gs.data(), sizeof(int32_t) * (NG + 1), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->d_age_dist.p, age_dist, sizeof(double) * NG, cudaMemcpyHostToDevice));
+  c->perm = perm;
+  c->C = n_cells;
+  c->cells_set = true;
+  return ABC_OK;
+}
+
+int abc_sample_prior(abc_ctx* c, int model, int64_t P, uint64_t seed, int64_t particle_offset,
+                     const abc_prior* prior, double* theta_out) {
+  if (!c) return ABC_ERR_INVALID;
+  const int npar = npar_of(&c->cfg, model);
+  if (npar < 0 || P < 0 || !prior || (!theta_out && P > 0)) return fail(c, ABC_ERR_INVALID, "abc_sample_prior: bad arguments");
+  if (particle_offset < 0 || particle_offset + P > (int64_t(1) << 32))
+    return fail(c, ABC_ERR_INVALID, "abc_sample_prior: particle index beyond 2^32");
+  if (P == 0) return ABC_OK;
+  if (prior->vary_mode == 1 && !(prior->factor[0] > 0.0 && prior->factor[1] > 0.0))
+    return fail(c, ABC_ERR_INVALID, "abc_sample_prior: factor bounds must be > 0");
+  if (c->cfg.scaling_column && !(prior->scaling[0] > 0.0 && prior->scaling[1] > 0.0))
+    return fail(c, ABC_ERR_INVALID, "abc_sample_prior: scaling bounds must be > 0");
+  PriorArgs a;
+  a.cfg = c->dcfg;
+  a.cfg.npar = npar;
+  a.model = model;
+  a.n_particles = P;
+  a.p_offset = particle_offset;
+  a.seed = seed;
+  const double* src[6] = {prior->kon, prior->koff, prior->alpha, prior->gamma, prior->lambda, prior->beta};
+  for (int i = 0; i < 6; ++i) {
+    a.lo[i] = src[i][0];
+    a.hi[i] = src[i][1];
+  }
+  a.lo[6] = c->cfg.scaling_column ? xlog(prior->scaling[0]) / ABC_LN10 : 0.0;
+  a.hi[6] = c->cfg.scaling_column ? xlog(prior->scaling[1]) / ABC_LN10 : 0.0;
+  a.vary_mode = prior->vary_mode;
+  a.lf0 = prior->vary_mode == 1 ? xlog(prior->factor[0]) / ABC_LN10 : 0.0;
+  a.lf1 = prior->vary_mode == 1 ? xlog(prior->factor[1]) / ABC_LN10 : 0.0;
+  CK(c->d_theta.ensure((size_t)P * npar));
+  a.theta = c->d_theta.p;
+  CK(launch_prior(a, c->stream));
+  CK(cudaMemcpyAsync(theta_out, c->d_theta.p, sizeof(double) * P * npar, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return ABC_OK;
+}
+
+// Enqueue setup -> SSA -> capture/statistics for particles [0, P) of
+// d_theta (device), writing d_stats (device).  Chunked so that the per-cell
+// counts stay within kChunkBytes.
+static int npar_max(const abc_config* cfg) { return npar_of(cfg, 3); }
+
+static cudaError_t prof_mark(abc_ctx* c) {
+  if (!c->prof) return cudaSuccess;
+  if (c->ev_used == c->ev_pool.size()) {
+    cudaEvent_t e;
+    cudaError_t r = cudaEventCreate(&e);
+    if (r != cudaSuccess) return r;
+    c->ev_pool.push_back(e);
+  }
+  return cudaEventRecord(c->ev_pool[c->ev_used++], c->stream);
+}
+
+static int enqueue_simulate(abc_ctx* c, int model, const int32_t* d_models, const double* d_theta, int64_t ld,
+                            int64_t P, uint64_t seed, int64_t p_offset, double* d_stats, bool want_cells) {
+  const int npar = d_models ? npar_max(&c->cfg) : npar_of(&c->cfg, model);
+  const int K = ABC_NSTATS(c->cfg.n_ages, c->cfg.n_conds);
+  const int64_t C = c->C;
+  int64_t chunk = std::max<int64_t>(1, (int64_t)(kChunkBytes / (sizeof(int2) * (size_t)C)));
+  if (want_cells) chunk = P;  // per-cell outputs are requested for small P only
+  chunk = std::min<int64_t>(chunk, std::max<int64_t>(P, 1));
+  CK(c->d_rec.ensure(chunk));
+  CK(c->d_recf.ensure(chunk));
+  CK(c->d_counts.ensure((size_t)chunk * C));
+  if (want_cells) {
+    CK(c->d_captured.ensure((size_t)chunk * C));
+    CK(c->d_events.ensure((size_t)chunk * C));
+    CK(c->d_hash.ensure((size_t)chunk * C));
+  }
+  CK(cudaMemsetAsync(c->d_misc.p, 0, sizeof(unsigned long long) * 4, c->stream));
+  CK(cudaMemsetAsync(c->d_status.p, 0, sizeof(int), c->stream));
+  c->ev_used = 0;
+  const bool fp64 = c->cfg.precision == ABC_FP64;
+  const int bps = fp64 ? ssa_blocks_per_sm_fp64() : ssa_blocks_per_sm_fp32();
+  for (int64_t p0 = 0; p0 < P; p0 += chunk) {
+    const int64_t n = std::min(chunk, P - p0);
+    SetupArgs sa;
+    sa.cfg = c->dcfg;
+    sa.cfg.npar = npar;
+    sa.model = model;
+    sa.models = d_models ? d_models + p0 : nullptr;
+    sa.ld_theta = ld;
+    sa.theta = d_theta + p0 * ld;
+    sa.n_particles = n;
+    sa.rec = c->d_rec.p;
+    sa.recf = c->d_recf.p;
+    sa.status = c->d_status.p;
+    CK(prof_mark(c));
+    CK(launch_setup(sa, c->stream));
+    CK(prof_mark(c));
+    CK(cudaMemsetAsync(c->d_misc.p, 0, sizeof(unsigned long long), c->stream));
+    SsaArgs ss;
+    ss.cfg = sa.cfg;
+    ss.rec = c->d_rec.p;
+    ss.recf = c->d_recf.p;
+    ss.cell_cond = c->d_cond.p;
+    ss.cell_age = c->d_age.p;
+    ss.cell_id = c->d_id.p;
+    ss.order = nullptr;
+    ss.n_cells = C;
+    ss.n_items = n * C;
+    ss.p_offset = p_offset + p0;
+    ss.seed = seed;
+    ss.counts = c->d_counts.p;
+    ss.events = want_cells ? c->d_events.p : nullptr;
+    ss.hash = want_cells ? c->d_hash.p : nullptr;
+    ss.counter = c->d_misc.p;
+    ss.totals = c->d_misc.p + 1;
+    ss.status = c->d_status.p;
+    ss.want_hash = want_cells ? 1 : 0;
+    const int64_t warps_needed = (ss.n_items + 31) / 32;
+    int64_t grid = (int64_t)std::max(1, bps) * c->sms;
+    grid = std::min<int64_t>(grid, (warps_needed + 3) / 4);
+    grid = std::max<int64_t>(grid, 1);
+    CK(fp64 ? launch_ssa_fp64(ss, (int)grid, c->stream) : launch_ssa_fp32(ss, (int)grid, c->stream));
+    CK(prof_mark(c));
+    StatsArgs st;
+    st.cfg = sa.cfg;
+    st.counts = c->d_counts.p;
+    st.beta = c->d_beta.p;
+    st.cell_id = c->d_id.p;
+    st.gstart = c->d_gstart.p;
+    st.age_dist = c->d_age_dist.p;
+    st.n_cells = C;
+    st.n_particles = n;
+    st.p_offset = p_offset + p0;
+    st.seed = seed;
+    st.stats = d_stats + p0 * K;
+    st.captured = want_cells ? c->d_captured.p : nullptr;
+    CK(launch_stats(st, c->stream));
+    CK(prof_mark(c));
+  }
+  return ABC_OK;
+}
+
+static int check_sim_args(abc_ctx* c, int model, int64_t P, int64_t particle_offset) {
+  if (!c->cells_set) return fail(c, ABC_ERR_STATE, "abc_set_cells must be called before simulating");
+  if (npar_of(&c->cfg, model) < 0) return fail(c, ABC_ERR_INVALID, "model must be 1..5");
+  if (P < 0) return fail(c, ABC_ERR_INVALID, "negative particle count");
+  if (particle_offset < 0 || particle_offset + P > (int64_t(1) << 32))
+    return fail(c, ABC_ERR_INVALID, "particle index beyond 2^32");
+  return ABC_OK;
+}
+
+static int finish_status(abc_ctx* c) {
+  int hs = 0;
+  unsigned long long tot[3] = {0, 0, 0};
+  CK(cudaMemcpyAsync(&hs, c->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpyAsync(tot, c->d_misc.p, sizeof(tot), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->last_events = (int64_t)tot[1];
+  c->last_rej = (int64_t)tot[2];
+  if (c->prof) {
+    c->phase_ms[0] = c->phase_ms[1] = c->phase_ms[2] = 0.0;
+    for (size_t i = 0; i + 3 < c->ev_used; i += 4) {
+      for (int ph = 0; ph < 3; ++ph) {
+        float ms = 0.0f;
+        CK(cudaEventElapsedTime(&ms, c->ev_pool[i + ph], c->ev_pool[i + ph + 1]));
+        c->phase_ms[ph] += ms;
+      }
+    }
+  }
+  c->ev_used = 0;
+  if (hs & STF_EVENT_CAP) return fail(c, ABC_ERR_EVENT_CAP, "a trajectory exceeded the event cap");
+  if (hs & (STF_OVERFLOW | STF_NONFINITE))
+    return fail(c, ABC_ERR_NONFINITE, "non-finite rate or molecule count overflow");
+  return ABC_OK;
+}
+
+int abc_simulate_device(abc_ctx* c, int model, const double* d_theta, int64_t P, uint64_t seed,
+                        int64_t particle_offset, double* d_stats) {
+  if (!c) return ABC_ERR_INVALID;
+  int st = check_sim_args(c, model, P, particle_offset);
+  if (st) return st;
+  if (P == 0) return ABC_OK;
+  if (!d_theta || !d_stats) return fail(c, ABC_ERR_INVALID, "null device pointer");
+  return enqueue_simulate(c, model, nullptr, d_theta, npar_of(&c->cfg, model), P, seed, particle_offset, d_stats,
+                          false);
+}
+
+int abc_simulate_batch_device(abc_ctx* c, const int32_t* d_models, const double* d_theta, int64_t ld_theta,
+                              int64_t P, uint64_t seed, int64_t particle_offset, double* d_stats) {
+  if (!c) return ABC_ERR_INVALID;
+  int st = check_sim_args(c, 1, P, particle_offset);
+  if (st) return st;
+  if (P == 0) return ABC_OK;
+  if (!d_models || !d_theta || !d_stats) return fail(c, ABC_ERR_INVALID, "null device pointer");
+  if (ld_theta < npar_max(&c->cfg)) return fail(c, ABC_ERR_INVALID, "ld_theta below the largest npar");
+  return enqueue_simulate(c, 0, d_models, d_theta, ld_theta, P, seed, particle_offset, d_stats, false);
+}
+
+int abc_simulate_batch(abc_ctx* c, const int32_t* models, const double* theta, int64_t ld_theta, int64_t P,
+                       uint64_t seed, int64_t particle_offset, double* stats_out) {
+  if (!c) return ABC_ERR_INVALID;
+  int st = check_sim_args(c, 1, P, particle_offset);
+  if (st) return st;
+  if (P == 0) return ABC_OK;
+  if (!models || !theta || !stats_out) return fail(c, ABC_ERR_INVALID, "null host pointer");
+  if (ld_theta < npar_max(&c->cfg)) return fail(c, ABC_ERR_INVALID, "ld_theta below the largest npar");
+  for (int64_t p = 0; p < P; ++p)
+    if (models[p] < 1 || models[p] > 5) return fail(c, ABC_ERR_INVALID, "model ids must be 1..5");
+  const int K = ABC_NSTATS(c->cfg.n_ages, c->cfg.n_conds);
+  CK(c->d_models.ensure((size_t)P));
+  CK(c->d_theta.ensure((size_t)P * ld_theta));
+  CK(c->d_stats.ensure((size_t)P * K));
+  CK(cudaMemcpyAsync(c->d_models.p, models, sizeof(int32_t) * P, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->d_theta.p, theta, sizeof(double) * P * ld_theta, cudaMemcpyHostToDevice, c->stream));
+  st = enqueue_simulate(c, 0, c->d_models.p, c->d_theta.p, ld_theta, P, seed, particle_offset, c->d_stats.p, false);
+  if (st) return st;
+  CK(cudaMemcpyAsync(stats_out, c->d_stats.p, sizeof(double) * P * K, cudaMemcpyDeviceToHost, c->stream));
+  return finish_status(c);
+}
+
+int abc_synchronize(abc_ctx* c) {
+  if (!c) return ABC_ERR_INVALID;
+  return finish_status(c);
+}
+
+int abc_simulate(abc_ctx* c, int model, const double* theta, int64_t P, uint64_t seed, int64_t particle_offset,
+                 double* stats_out) {
+  if (!c) return ABC_ERR_INVALID;
+  int st = check_sim_args(c, model, P, particle_offset);
+  if (st) return st;
+  if (P == 0) return ABC_OK;
+  if (!theta || !stats_out) return fail(c, ABC_ERR_INVALID, "null host pointer");
+  const int npar = npar_of(&c->cfg, model);
+  const int K = ABC_NSTATS(c->cfg.n_ages, c->cfg.n_conds);
+  CK(c->d_theta.ensure((size_t)P * npar));
+  CK(c->d_stats.ensure((size_t)P * K));
+  CK(cudaMemcpyAsync(c->d_theta.p, theta, sizeof(double) * P * npar, cudaMemcpyHostToDevice, c->stream));
+  st = enqueue_simulate(c, model, nullptr, c->d_theta.p, npar, P, seed, particle_offset, c->d_stats.p, false);
+  if (st) return st;
+  CK(cudaMemcpyAsync(stats_out, c->d_stats.p, sizeof(double) * P * K, cudaMemcpyDeviceToHost, c->stream));
+  return finish_status(c);
+}
+
+int abc_simulate_cells(abc_ctx* c, int model, const double* theta, int64_t P, uint64_t seed,
+                       int64_t particle_offset, int32_t* counts_out, int32_t* captured_out, int64_t* events_out,
+                       uint64_t* hash_out, double* stats_out) {
+  if (!c) return ABC_ERR_INVALID;
+  int st = check_sim_args(c, model, P, particle_offset);
+  if (st) return st;
+  if (P == 0) return ABC_OK;
+  if (!theta) return fail(c, ABC_ERR_INVALID, "null theta");
+  const int64_t C = c->C;
+  if ((double)P * (double)C * 24.0 > (double)(size_t(8) << 30))
+    return fail(c, ABC_ERR_INVALID, "abc_simulate_cells: P x C too large for per-cell output");
+  const int npar = npar_of(&c->cfg, model);
+  const int K = ABC_NSTATS(c->cfg.n_ages, c->cfg.n_conds);
+  CK(c->d_theta.ensure((size_t)P * npar));
+  CK(c->d_stats.ensure((size_t)P * K));
+  CK(cudaMemcpyAsync(c->d_theta.p, theta, sizeof(double) * P * npar, cudaMemcpyHostToDevice, c->stream));
+  st = enqueue_simulate(c, model, nullptr, c->d_theta.p, npar, P, seed, particle_offset, c->d_stats.p, true);
+  if (st) return st;
+  std::vector<int2> cnt((size_t)P * C), cap((size_t)P * C);
+  std::vector<int64_t> ev((size_t)P * C);
+  std::vector<uint64_t> hs((size_t)P * C);
+  CK(cudaMemcpyAsync(cnt.data(), c->d_counts.p, sizeof(int2) * P * C, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpyAsync(cap.data(), c->d_captured.p, sizeof(int2) * P * C, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpyAsync(ev.data(), c->d_events.p, sizeof(int64_t) * P * C, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpyAsync(hs.data(), c->d_hash.p, sizeof(uint64_t) * P * C, cudaMemcpyDeviceToHost, c->stream));
+  if (stats_out)
+    CK(cudaMemcpyAsync(stats_out, c->d_stats.p, sizeof(double) * P * K, cudaMemcpyDeviceToHost, c->stream));
+  st = finish_status(c);
+  // internal (group-sorted) order -> caller's cell order
+  for (int64_t p = 0; p < P; ++p)
+    for (int64_t i = 0; i < C; ++i) {
+      const int64_t src = p * C + i, dst = p * C + c->perm[i];
+      if (counts_out) { counts_out[2 * dst] = cnt[src].x; counts_out[2 * dst + 1] = cnt[src].y; }
+      if (captured_out) { captured_out[2 * dst] = cap[src].x; captured_out[2 * dst + 1] = cap[src].y; }
+      if (events_out) events_out[dst] = ev[src];
+      if (hash_out) hash_out[dst] = hs[src];
+    }
+  return st;
+}
+
+int abc_profile(abc_ctx* c, int enable) {
+  if (!c) return ABC_ERR_INVALID;
+  c->prof = enable != 0;
+  c->ev_used = 0;
+  return ABC_OK;
+}
+
+int abc_profile_read(const abc_ctx* c, double* ms_out) {
+  if (!c || !ms_out) return ABC_ERR_INVALID;
+  for (int i = 0; i < 3; ++i) ms_out[i] = c->phase_ms[i];
+  return ABC_OK;
+}
+
+int abc_last_counters(const abc_ctx* c, int64_t* events, int64_t* rejections) {
+  if (!c) return ABC_ERR_INVALID;
+  if (events) *events = c->last_events;
+  if (rejections) *rejections = c->last_rej;
+  return ABC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// distance + acceptance
+// ---------------------------------------------------------------------------
+static int load_dist_inputs(abc_ctx* c, const double* data, const double* se, int64_t G, int K, int n_fam,
+                            const int32_t* fam, const double* stats, int64_t P, DistInputs& in) {
+  if (!data || !se || !stats || G <= 0 || P <= 0 || K <= 0)
+    return fail(c, ABC_ERR_INVALID, "distance: bad arguments");
+  if (P > (int64_t(1) << 31) - 1 || G > (int64_t(1) << 31) - 1)
+    return fail(c, ABC_ERR_INVALID, "distance: P and G must be < 2^31");
+  in.G = G;
+  in.P = P;
+  in.K = K;
+  if (n_fam <= 0 || !fam) {
+    in.n_fam = 1;
+    in.fam[0] = K;
+  } else {
+    if (n_fam > 16) return fail(c, ABC_ERR_INVALID, "distance: at most 16 families");
+    int sum = 0;
+    for (int f = 0; f < n_fam; ++f) {
+      if (fam[f] < 0) return fail(c, ABC_ERR_INVALID, "distance: negative family size");
+      in.fam[f] = fam[f];
+      sum += fam[f];
+    }
+    if (sum != K) return fail(c, ABC_ERR_INVALID, "distance: family sizes must sum to K");
+    in.n_fam = n_fam;
+  }
+  CK(c->d_data.ensure((size_t)G * K));
+  CK(c->d_se.ensure((size_t)G * K));
+  CK(c->d_sel_stats.ensure((size_t)P * K));
+  CK(cudaMemcpyAsync(c->d_data.p, data, sizeof(double) * G * K, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->d_se.p, se, sizeof(double) * G * K, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->d_sel_stats.p, stats, sizeof(double) * P * K, cudaMemcpyHostToDevice, c->stream));
+  in.data = c->d_data.p;
+  in.se = c->d_se.p;
+  in.stats = c->d_sel_stats.p;
+  return ABC_OK;
+}
+
+int abc_errors(abc_ctx* c, const double* data, const double* se, int64_t G, int K, int n_fam,
+               const int32_t* fam, const double* stats, int64_t P, double* err_out) {
+  if (!c) return ABC_ERR_INVALID;
+  if (!err_out) return fail(c, ABC_ERR_INVALID, "abc_errors: null output");
+  DistInputs in;
+  int st = load_dist_inputs(c, data, se, G, K, n_fam, fam, stats, P, in);
+  if (st) return st;
+  DBuf<double> out;
+  CK(out.ensure((size_t)P * G));
+  cudaError_t e = launch_dist_full(in, out.p, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(err_out, out.p, sizeof(double) * P * G, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  out.release();
+  if (e != cudaSuccess) return cuda_fail(c, e, "abc_errors");
+  return ABC_OK;
+}
+
+// candidate pass with capacity handling; returns candidate count in *n
+static int candidate_pass(abc_ctx* c, const DistInputs& in, int64_t* n) {
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    CK(c->d_cand.ensure((size_t)c->cand_cap));
+    CK(cudaMemsetAsync(c->d_ncand.p, 0, sizeof(unsigned long long), c->stream));
+    CK(launch_dist_fast(c->d_s32.p, c->d_sw.p, c->d_dw.p, in.P, in.G, in.K, c->d_X.p, c->d_cand.p, c->d_ncand.p,
+                        c->cand_cap, nullptr, 0, 0, c->stream));
+    unsigned long long h = 0;
+    CK(cudaMemcpyAsync(&h, c->d_ncand.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if ((int64_t)h <= c->cand_cap) {
+      *n = (int64_t)h;
+      return ABC_OK;
+    }
+    c->cand_cap = (int64_t)h + (int64_t)h / 8 + 1024;
+  }
+  return fail(c, ABC_ERR_CAPACITY, "candidate buffer overflow");
+}
+
+int abc_errors_select(abc_ctx* c, const double* data, const double* se, int64_t G, int K, int n_fam,
+                      const int32_t* fam, const double* stats, int64_t P, int mode, double eps_or_q,
+                      int64_t* n_accepted_total) {
+  if (!c) return ABC_ERR_INVALID;
+  c->sel_ready = false;
+  if (mode != 0 && mode != 1) return fail(c, ABC_ERR_INVALID, "mode must be 0 (eps) or 1 (top-q)");
+  if (mode == 1 && !(eps_or_q > 0.0 && eps_or_q <= 1.0)) return fail(c, ABC_ERR_INVALID, "q must be in (0, 1]");
+  if (mode == 0 && eps_or_q != eps_or_q) return fail(c, ABC_ERR_INVALID, "eps is NaN");
+  DistInputs in;
+  int st = load_dist_inputs(c, data, se, G, K, n_fam, fam, stats, P, in);
+  if (st) return st;
+  CK(c->d_sw.ensure((size_t)G * K));
+  CK(c->d_dw.ensure((size_t)G * K));
+  CK(c->d_s32.ensure((size_t)P * K));
+  CK(c->d_X.ensure((size_t)G));
+  CK(c->d_ncand.ensure(1));
+  CK(c->d_gcount.ensure((size_t)G));
+  CK(c->d_goff.ensure((size_t)G + 1));
+  CK(c->d_gcursor.ensure((size_t)G));
+  CK(c->d_alen.ensure((size_t)G));
+  CK(c->d_aoff.ensure((size_t)G + 1));
+  CK(c->d_fail.ensure((size_t)G));
+  CK(launch_dist_prep(in, c->d_sw.p, c->d_dw.p, c->d_s32.p, c->stream));
+  const int64_t kq = mode == 1 ? (int64_t)std::ceil(eps_or_q * (double)P) : 0;
+  std::vector<float> hX((size_t)G);
+  if (mode == 0) {
+    float x;
+    if (eps_or_q >= 10.0) {
+      x = INFINITY;
+    } else if (eps_or_q < 0.0) {
+      x = -1.0f;
+    } else {
+      const float e = (float)eps_or_q;
+      x = e + 2.0f * dist_bound(e, K);
+      x = std::nextafter(x, INFINITY);
+    }
+    std::fill(hX.begin(), hX.end(), x);
+    CK(cudaMemcpyAsync(c->d_X.p, hX.data(), sizeof(float) * G, cudaMemcpyHostToDevice, c->stream));
+  } else {
+    // thresholds from a strided subsample
+    const int64_t n_sub = std::min<int64_t>(P, 32768);
+    const int64_t stride = std::max<int64_t>(1, P / n_sub);
+    const int64_t k_sub = (int64_t)std::ceil(2.0 * eps_or_q * (double)n_sub) + 16;
+    if (k_sub >= n_sub) {
+      std::fill(hX.begin(), hX.end(), INFINITY);
+      CK(cudaMemcpyAsync(c->d_X.p, hX.data(), sizeof(float) * G, cudaMemcpyHostToDevice, c->stream));
+    } else {
+      CK(c->d_esub.ensure((size_t)n_sub * G));
+      CK(launch_dist_fast(c->d_s32.p, c->d_sw.p, c->d_dw.p, P, G, K, nullptr, nullptr, nullptr, 0, c->d_esub.p,
+                          stride, n_sub, c->stream));
+      CK(launch_dist_threshold(c->d_esub.p, n_sub, G, k_sub, K, c->d_X.p, c->stream));
+      CK(cudaMemcpyAsync(hX.data(), c->d_X.p, sizeof(float) * G, cudaMemcpyDeviceToHost, c->stream));
+    }
+  }
+  int64_t ncand = 0;
+  c->sel_rechecked = 0;
+  for (int round = 0; round < 4; ++round) {
+    st = candidate_pass(c, in, &ncand);
+    if (st) return st;
+    CK(c->d_e64.ensure((size_t)ncand));
+    CK(c->d_se64.ensure((size_t)ncand));
+    CK(c->d_sp.ensure((size_t)ncand));
+    CK(launch_dist_recheck(in, c->d_cand.p, ncand, c->d_e64.p, c->stream));
+    CK(launch_dist_group_sort(c->d_cand.p, c->d_e64.p, ncand, G, c->d_gcount.p, c->d_goff.p, c->d_sp.p,
+                              c->d_se64.p, c->d_gcursor.p, c->stream));
+    CK(cudaMemsetAsync(c->d_fail.p, 0, sizeof(int) * G, c->stream));
+    CK(launch_dist_accept_len(c->d_goff.p, c->d_se64.p, G, mode, eps_or_q, kq, c->d_X.p, K, c->d_alen.p,
+                              c->d_fail.p, c->stream));
+    c->sel_rechecked += ncand;
+    if (mode == 0) break;
+    std::vector<int> hf((size_t)G);
+    CK(cudaMemcpyAsync(hf.data(), c->d_fail.p, sizeof(int) * G, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    bool any = false;
+    for (int64_t g = 0; g < G; ++g) {
+      if (hf[g]) {
+        any = true;
+        hX[g] = (round >= 1 || !(hX[g] < INFINITY)) ? INFINITY : 4.0f * hX[g] + 0.1f;
+      }
+    }
+    if (!any) break;
+    if (round == 3) return fail(c, ABC_ERR_CAPACITY, "top-q selection did not converge");
+    CK(cudaMemcpyAsync(c->d_X.p, hX.data(), sizeof(float) * G, cudaMemcpyHostToDevice, c->stream));
+  }
+  CK(launch_scan(c->d_alen.p, G, c->d_aoff.p, c->stream));
+  int64_t total = 0;
+  CK(cudaMemcpyAsync(&total, c->d_aoff.p + G, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  CK(c->d_out_idx.ensure((size_t)std::max<int64_t>(total, 1)));
+  CK(c->d_out_err.ensure((size_t)std::max<int64_t>(total, 1)));
+  CK(launch_dist_compact(c->d_goff.p, c->d_sp.p, c->d_se64.p, c->d_aoff.p, G, 0, c->d_out_idx.p, c->d_out_err.p,
+                         c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->sel_G = G;
+  c->sel_total = total;
+  c->sel_cands = ncand;
+  c->sel_ready = true;
+  if (n_accepted_total) *n_accepted_total = total;
+  return ABC_OK;
+}
+
+int abc_accept_fetch(abc_ctx* c, int64_t* gene_offsets, int64_t* particle_idx, double* err) {
+  if (!c) return ABC_ERR_INVALID;
+  if (!c->sel_ready) return fail(c, ABC_ERR_STATE, "no selection result: call abc_errors_select first");
+  if (!gene_offsets || (!particle_idx && c->sel_total > 0)) return fail(c, ABC_ERR_INVALID, "null output");
+  CK(cudaMemcpyAsync(gene_offsets, c->d_aoff.p, sizeof(int64_t) * (c->sel_G + 1), cudaMemcpyDeviceToHost, c->stream));
+  if (c->sel_total > 0) {
+    CK(cudaMemcpyAsync(particle_idx, c->d_out_idx.p, sizeof(int64_t) * c->sel_total, cudaMemcpyDeviceToHost,
+                       c->stream));
+    if (err)
+      CK(cudaMemcpyAsync(err, c->d_out_err.p, sizeof(double) * c->sel_total, cudaMemcpyDeviceToHost, c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return ABC_OK;
+}
+
+int abc_select_counters(const abc_ctx* c, int64_t* candidates, int64_t* rechecked) {
+  if (!c) return ABC_ERR_INVALID;
+  if (candidates) *candidates = c->sel_cands;
+  if (rechecked) *rechecked = c->sel_rechecked;
+  return ABC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,46 @@
+// distance.cuh — shared pieces of the particle x gene distance kernels.
+//
+// err_pg = min(10, sum_f sum_{k in f} (d_gk - s_pk)^2 / (se_gk^2 + 0.01 d_gk^2 + eps_gk) / K)
+// with eps_gk = 1e-4 iff se_gk + d_gk == 0 (scripts/compute_errors.jl:30-43,
+// clipped at 10 by :159-161).
+//
+// Fast path (FP32 CUDA cores): with a = sqrt(w_gk) the term is
+// (a d - a s)^2; a and a*d are formed in FP64 and rounded once, so
+// t = fma(-a, s, a d) and acc = fma(t, t, acc): two FMAs per (p, g, k).
+// Because w d^2 <= 1/0.01 = 100 for every gene, |a d| <= 10, and a forward
+// error analysis of the FP32 evaluation gives
+//   |err32 - err64| <= B(err) = 1.5 u (64 sqrt(err) + (K + 8) err),  u = 2^-24,
+// B increasing in err.  Pairs whose FP32 error lies within B of the threshold
+// are rechecked in FP64 in the reference's operation order.
+#pragma once
+#include <math.h>
+
+namespace abc {
+
+#if defined(__CUDACC__)
+#define ABC_HDF __host__ __device__ __forceinline__
+#else
+#define ABC_HDF inline
+#endif
+
+ABC_HDF float dist_bound_f(float e, int K) {
+  if (!(e >= 0.0f)) e = 0.0f;
+  const float u = 5.9604644775390625e-08f;
+  return 1.5f * u * (64.0f * sqrtf(e) + (float)(K + 8) * e) + 1e-30f;
+}
+
+constexpr int kDistTile = 128;  // particles and genes per CTA tile
+constexpr int kDistKc = 16;     // statistics per shared-memory stage
+constexpr int kHistBins = 4096; // threshold histogram bins (sqrt scale on [0, 10])
+
+ABC_HDF int hist_bin(float e) {
+  float x = sqrtf(e * 0.1f) * (float)kHistBins;
+  int b = (int)x;
+  return b < 0 ? 0 : (b >= kHistBins ? kHistBins - 1 : b);
+}
+ABC_HDF float hist_upper(int b) {
+  float q = (float)(b + 1) / (float)kHistBins;
+  return 10.0f * q * q * 1.0000005f;
+}
+
+}  // namespace abc

@@ -1,0 +1,104 @@
+// kernels.h — internal launchers shared by the C-ABI translation unit.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ssa.cuh"
+
+namespace abc {
+
+struct StatsArgs {
+  DevCfg cfg;
+  const int2* counts;        // [P][C] internal cell order
+  const double* beta;        // [C] internal order
+  const uint32_t* cell_id;   // [C] caller's cell index
+  const int32_t* gstart;     // [A*J + 1] group starts, group = cond*A + age
+  const double* age_dist;    // [A*J] row-major (a*J + j)
+  int64_t n_cells;
+  int64_t n_particles;
+  int64_t p_offset;
+  uint64_t seed;
+  double* stats;             // [P][K]
+  int2* captured;            // optional [P][C]
+};
+
+struct SetupArgs {
+  DevCfg cfg;
+  int model;
+  const int32_t* models;     // optional per-particle model (overrides model)
+  int64_t ld_theta;          // theta row stride (>= npar of the particle's model)
+  const double* theta;       // [P][ld_theta]
+  int64_t n_particles;
+  PRec* rec;
+  PRecF* recf;
+  int* status;
+};
+
+struct PriorArgs {
+  DevCfg cfg;
+  int model;
+  int64_t n_particles;
+  int64_t p_offset;
+  uint64_t seed;
+  double lo[7], hi[7];       // kon, koff, alpha, gamma, lambda, beta, log10 scaling
+  double lf0, lf1;           // log10 factor bounds
+  int vary_mode;
+  double* theta;             // [P][npar]
+};
+
+// ---------------------------------------------------------------------------
+// distance + acceptance (scripts/compute_errors.jl:30-70, accepted_particles.jl)
+// ---------------------------------------------------------------------------
+struct DistInputs {
+  const double* data;   // [G][K]
+  const double* se;     // [G][K]
+  const double* stats;  // [P][K]
+  int64_t G, P;
+  int K;
+  int n_fam;
+  int fam[16];          // family sizes (sum K)
+};
+
+struct Cand {
+  int32_t p, g;
+};
+
+// per (g,k): sw = sqrt(w), dw = sqrt(w) d in FP32, w = 1/((se^2 + 0.01 d^2) + eps)
+cudaError_t launch_dist_prep(const DistInputs& in, float* sw, float* dw, float* s32, cudaStream_t s);
+// FP32 direct distance: emit (p, g) with min(10, err32) <= X[g] (mode emit), or
+// write err32 of the particles p = row*stride into esub[row][g] (mode sample).
+cudaError_t launch_dist_fast(const float* s32, const float* sw, const float* dw, int64_t P, int64_t G, int K,
+                             const float* X, Cand* cand, unsigned long long* n_cand, int64_t cap,
+                             float* esub, int64_t stride, int64_t n_sub, cudaStream_t s);
+// per gene: X[g] = upper edge of the histogram bin where the count of esub
+// reaches k_sub, plus the bound (+inf when fewer than k_sub finite values).
+cudaError_t launch_dist_threshold(const float* esub, int64_t n_sub, int64_t G, int64_t k_sub, int K,
+                                  float* X, cudaStream_t s);
+// FP64 error of each candidate, in the reference's operation order.
+cudaError_t launch_dist_recheck(const DistInputs& in, const Cand* cand, int64_t n, double* e64, cudaStream_t s);
+// group candidates by gene and sort each gene's list by (err, p).
+cudaError_t launch_dist_group_sort(const Cand* cand, const double* e64, int64_t n, int64_t G,
+                                   int64_t* gcount, int64_t* goff, int32_t* sp, double* se64,
+                                   unsigned long long* gcursor, cudaStream_t s);
+// accepted prefix length per gene (mode 0: err <= eps; mode 1: the k smallest
+// finite errors) and, in mode 1, a failure flag when the candidate threshold
+// X[g] could have excluded a member of the top k.
+cudaError_t launch_dist_accept_len(const int64_t* goff, const double* se64, int64_t G, int mode, double eps,
+                                   int64_t k, const float* X, int K, int64_t* alen, int* fail, cudaStream_t s);
+// compact the accepted prefixes: idx (1-based particle index + p_base) and err.
+cudaError_t launch_dist_compact(const int64_t* goff, const int32_t* sp, const double* se64, const int64_t* aoff,
+                                int64_t G, int64_t p_base, int64_t* idx, double* err, cudaStream_t s);
+cudaError_t launch_scan(const int64_t* cnt, int64_t G, int64_t* off, cudaStream_t s);
+// full FP64 error matrix [P][G]
+cudaError_t launch_dist_full(const DistInputs& in, double* err, cudaStream_t s);
+float dist_bound(float e, int K);
+
+cudaError_t launch_prior(const PriorArgs& a, cudaStream_t s);
+cudaError_t launch_setup(const SetupArgs& a, cudaStream_t s);
+cudaError_t launch_ssa_fp64(const SsaArgs& a, int grid, cudaStream_t s);
+cudaError_t launch_ssa_fp32(const SsaArgs& a, int grid, cudaStream_t s);
+cudaError_t launch_stats(const StatsArgs& a, cudaStream_t s);
+int ssa_blocks_per_sm_fp64();
+int ssa_blocks_per_sm_fp32();
+
+}  // namespace abc

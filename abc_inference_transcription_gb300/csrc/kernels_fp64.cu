@@ -1,0 +1,194 @@
+// kernels_fp64.cu — prior draw, particle setup, FP64 (oracle-mode) SSA and the
+// fused capture + statistics kernel.  Built with -fmad=false: every FP64
+// result here is bit-identical to the FP64 CPU oracle.
+#include "kernels.h"
+
+namespace abc {
+
+// ---------------------------------------------------------------------------
+// Prior draw (fix_params, scripts/abc_simulation.jl:3-11): one thread per
+// particle, Philox stream ST_PRIOR, cell 0.  Column order of theta:
+// kon(1|S), koff, alpha(1|S), gamma(1|S), lambda, [beta], [scaling].
+// ---------------------------------------------------------------------------
+__global__ void prior_kernel(PriorArgs A) {
+  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= A.n_particles) return;
+  Rng r;
+  rng_init(r, A.seed, ST_PRIOR, 0u, (uint32_t)(A.p_offset + p));
+  double* th = A.theta + p * A.cfg.npar;
+  const int S = A.cfg.n_steps;
+  int i = 0;
+  uint32_t a, b;
+  for (int rate = 0; rate < 4; ++rate) {
+    const double lo = A.lo[rate], hi = A.hi[rate];
+    bool varies = (A.model == 3 && rate == 0) || (A.model == 4 && rate == 2) || (A.model == 5 && rate == 3);
+    rng_pair(r, a, b);
+    double base = lo + (hi - lo) * u52(a, b);
+    if (!varies) {
+      th[i++] = base;
+    } else if (A.vary_mode == 0) {
+      th[i++] = base;
+      for (int k = 1; k < S; ++k) {
+        rng_pair(r, a, b);
+        th[i++] = lo + (hi - lo) * u52(a, b);
+      }
+    } else {
+      for (int k = 0; k < S; ++k) {
+        rng_pair(r, a, b);
+        th[i++] = base + (A.lf0 + (A.lf1 - A.lf0) * u52(a, b));
+      }
+    }
+  }
+  rng_pair(r, a, b);
+  th[i++] = A.lo[4] + (A.hi[4] - A.lo[4]) * u52(a, b);
+  if (A.cfg.splicing) {
+    rng_pair(r, a, b);
+    th[i++] = A.lo[5] + (A.hi[5] - A.lo[5]) * u52(a, b);
+  }
+  if (A.cfg.scaling_column) {
+    rng_pair(r, a, b);
+    th[i++] = xexp10(A.lo[6] + (A.hi[6] - A.lo[6]) * u52(a, b));
+  }
+}
+
+cudaError_t launch_prior(const PriorArgs& a, cudaStream_t s) {
+  if (a.n_particles <= 0) return cudaSuccess;
+  int blocks = (int)((a.n_particles + 127) / 128);
+  prior_kernel<<<blocks, 128, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// theta -> rates, thinning bounds and initial state; one thread per particle.
+// ---------------------------------------------------------------------------
+__global__ void setup_kernel(SetupArgs A) {
+  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= A.n_particles) return;
+  PRec R;
+  const int model = A.models ? A.models[p] : A.model;
+  int st = (model >= 1 && model <= 5) ? parse_theta(A.cfg, model, A.theta + p * A.ld_theta, R) : -1;
+  if (st) {
+    atomicOr(A.status, STF_NONFINITE);
+    // a harmless record: the trajectory sees no reactions
+    for (int k = 0; k < kMaxSteps; ++k) R.kon[k] = R.alp[k] = R.gam[k] = R.amax[k] = 0.0;
+    R.koff = R.lam = R.beta = R.scal = R.g0 = R.u0 = R.s0 = 0.0;
+    R.cost = 1.0;
+  }
+  A.rec[p] = R;
+  PRecF F;
+  for (int k = 0; k < kMaxSteps; ++k) {
+    F.kon[k] = (float)R.kon[k];
+    F.alp[k] = (float)R.alp[k];
+    F.gam[k] = (float)R.gam[k];
+    F.amax[k] = (float)R.amax[k];
+  }
+  F.koff = (float)R.koff;
+  F.lam = (float)R.lam;
+  F.beta = (float)R.beta;
+  F.scal = (float)R.scal;
+  A.recf[p] = F;
+}
+
+cudaError_t launch_setup(const SetupArgs& a, cudaStream_t s) {
+  if (a.n_particles <= 0) return cudaSuccess;
+  int blocks = (int)((a.n_particles + 63) / 64);
+  setup_kernel<<<blocks, 64, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// SSA, FP64 oracle mode.
+// ---------------------------------------------------------------------------
+cudaError_t launch_ssa_fp64(const SsaArgs& a, int grid, cudaStream_t s) {
+  ssa_kernel<true><<<grid, 128, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Capture + statistics: one CTA (8 warps) per particle.  Warp w handles the
+// (condition, age) groups w, w+8, ...: each lane thins its cells' counts
+// binomially with the cell's capture efficiency (downsample,
+// scripts/model.jl:221-239, realised per cell), accumulates exact integer
+// moment sums, and the warp reduces them with shuffles.  One thread then
+// forms the 4A + 3J statistics (abc_simulation.jl:23-46).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ long long shfl_xor_ll(long long v, int o) {
+  return __shfl_xor_sync(0xffffffffu, v, o);
+}
+__device__ __forceinline__ __int128 shfl_xor_i128(__int128 v, int o) {
+  unsigned long long lo = (unsigned long long)(unsigned __int128)v;
+  long long hi = (long long)(v >> 64);
+  lo = __shfl_xor_sync(0xffffffffu, lo, o);
+  hi = __shfl_xor_sync(0xffffffffu, hi, o);
+  return (__int128)(((unsigned __int128)(unsigned long long)hi << 64) | (unsigned __int128)lo);
+}
+
+__global__ void __launch_bounds__(256) stats_kernel(StatsArgs A) {
+  __shared__ double mom[kMaxAges * kMaxConds * 5];
+  __shared__ double wts[kMaxAges * kMaxConds];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ng = A.cfg.n_ages * A.cfg.n_conds;
+  const int K = 4 * A.cfg.n_ages + 3 * A.cfg.n_conds;
+  for (int i = threadIdx.x; i < ng; i += blockDim.x) wts[i] = A.age_dist[i];
+  for (int64_t p = blockIdx.x; p < A.n_particles; p += gridDim.x) {
+    const int2* cnt = A.counts + p * A.n_cells;
+    const uint32_t pg = (uint32_t)(A.p_offset + p);
+    for (int g = warp; g < ng; g += (blockDim.x >> 5)) {
+      const int g0 = A.gstart[g], g1 = A.gstart[g + 1];
+      long long su = 0, sl = 0;
+      __int128 suu = 0, sll = 0, sul = 0;
+      for (int i = g0 + lane; i < g1; i += 32) {
+        int2 c = cnt[i];
+        Rng r;
+        rng_init(r, A.seed, ST_CAPTURE, A.cell_id[i], pg);
+        long long cu = binomial(r, c.x, A.beta[i]);
+        long long cl = binomial(r, c.y, A.beta[i]);
+        if (A.captured) A.captured[p * A.n_cells + i] = make_int2((int)cu, (int)cl);
+        su += cu;
+        sl += cl;
+        suu += (__int128)(cu * cu);
+        sll += (__int128)(cl * cl);
+        sul += (__int128)(cu * cl);
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        su += shfl_xor_ll(su, o);
+        sl += shfl_xor_ll(sl, o);
+        suu += shfl_xor_i128(suu, o);
+        sll += shfl_xor_i128(sll, o);
+        sul += shfl_xor_i128(sul, o);
+      }
+      if (lane == 0) {
+        long long n = g1 - g0;
+        double nd = (double)n;
+        double dn = nd * (double)(n - 1);
+        __int128 nvu = (__int128)n * suu - (__int128)su * su;
+        __int128 ncv = (__int128)n * sul - (__int128)su * sl;
+        __int128 nvl = (__int128)n * sll - (__int128)sl * sl;
+        double* m = mom + g * 5;
+        m[0] = (double)su / nd;
+        m[1] = (double)sl / nd;
+        m[2] = i128_to_double(nvu) / dn;
+        m[3] = i128_to_double(ncv) / dn;
+        m[4] = i128_to_double(nvl) / dn;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) stats_from_moments(A.cfg, mom, wts, A.stats + p * K);
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_stats(const StatsArgs& a, cudaStream_t s) {
+  if (a.n_particles <= 0) return cudaSuccess;
+  int blocks = (int)(a.n_particles < 1048576 ? a.n_particles : 1048576);
+  stats_kernel<<<blocks, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+int ssa_blocks_per_sm_fp64() {
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssa_kernel<true>, 128, 0);
+  return n;
+}
+
+}  // namespace abc

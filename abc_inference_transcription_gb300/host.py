@@ -1,0 +1,232 @@
+"""Host-side mirror of the reference's hot-path interface over libabcgpu.so.
+
+Reference functions and the calls that replace them (paths inside
+pthomaslab/abc_inference_transcription):
+
+  fix_params(vary_map, N)           scripts/abc_simulation.jl:3-11   -> fix_params / Context.sample_prior
+  abc_sim(theta, ...)               scripts/abc_simulation.jl:13-62  -> abc_sim / Context.simulate
+  the particle loop                 scripts/abc_simulation.jl:88-97  -> Context.simulate over a theta batch
+  compute_trunc_errors(...)         scripts/compute_errors.jl:45-70  -> compute_trunc_errors / Context.errors
+  acceptance loop                   scripts/accepted_particles.jl:12-32 -> accepted_particles / Context.select
+
+Every call goes to the CUDA library; there is no CPU fallback (a missing
+library raises ImportError, a failing call raises AbcError).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .abi import AbcConfig, AbcError, AbcPrior, nstats, num_params, ptr
+from .config import CellTable, REF_FAMILIES
+
+
+class Context:
+    """One CUDA stream and its device buffers (abc_create / abc_destroy)."""
+
+    def __init__(self, cfg: AbcConfig, cells: CellTable | None = None):
+        self.lib = abi.load_library()
+        self.cfg = cfg
+        h = C.c_void_p()
+        st = self.lib.abc_create(C.byref(h), C.byref(cfg))
+        if st != 0:
+            raise AbcError(st, "abc_create failed (is a CUDA device visible?)")
+        self.h = h
+        self.K = nstats(cfg.n_ages, cfg.n_conds)
+        self.cells = None
+        if cells is not None:
+            self.set_cells(cells)
+
+    # -- lifecycle ---------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.abc_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int) -> None:
+        if st != 0:
+            msg = self.lib.abc_last_error(self.h)
+            raise AbcError(st, msg.decode() if msg else "")
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.abc_stream(self.h) or 0)
+
+    def num_params(self, model: int) -> int:
+        return num_params(self.cfg, model)
+
+    # -- cells -------------------------------------------------------------
+    def set_cells(self, cells: CellTable) -> None:
+        cond = np.ascontiguousarray(cells.cond, np.int32)
+        age = np.ascontiguousarray(cells.age, np.int32)
+        beta = np.ascontiguousarray(cells.beta, np.float64)
+        w = np.ascontiguousarray(cells.age_dist, np.float64)
+        if w.shape != (self.cfg.n_ages, self.cfg.n_conds):
+            raise ValueError(f"age_dist must be {self.cfg.n_ages} x {self.cfg.n_conds}")
+        self._check(self.lib.abc_set_cells(self.h, cond.shape[0], ptr(cond, C.c_int32), ptr(age, C.c_int32),
+                                           ptr(beta), ptr(w)))
+        self.cells = cells
+
+    # -- prior ---------------------------------------------------------------
+    def sample_prior(self, model: int, n: int, seed: int, prior: AbcPrior, offset: int = 0) -> np.ndarray:
+        th = np.zeros((n, self.num_params(model)))
+        self._check(self.lib.abc_sample_prior(self.h, model, n, seed, offset, C.byref(prior), ptr(th)))
+        return th
+
+    # -- simulation -------------------------------------------------------
+    def simulate(self, model: int, theta: np.ndarray, seed: int, offset: int = 0) -> np.ndarray:
+        th = np.ascontiguousarray(theta, np.float64)
+        if th.ndim != 2 or th.shape[1] != self.num_params(model):
+            raise ValueError(f"theta must be P x {self.num_params(model)}")
+        out = np.zeros((th.shape[0], self.K))
+        self._check(self.lib.abc_simulate(self.h, model, ptr(th), th.shape[0], seed, offset, ptr(out)))
+        return out
+
+    def simulate_device(self, model: int, d_theta: int, n: int, seed: int, d_stats: int, offset: int = 0) -> None:
+        """Device pointers (e.g. torch tensors' data_ptr()); stream-ordered on self.stream."""
+        self._check(self.lib.abc_simulate_device(self.h, model, C.c_void_p(d_theta), n, seed, offset,
+                                                 C.c_void_p(d_stats)))
+
+    def simulate_batch(self, models: np.ndarray, theta: np.ndarray, seed: int, offset: int = 0) -> np.ndarray:
+        """Mixed-model batch: theta rows padded to the largest npar."""
+        m = np.ascontiguousarray(models, np.int32)
+        th = np.ascontiguousarray(theta, np.float64)
+        out = np.zeros((th.shape[0], self.K))
+        self._check(self.lib.abc_simulate_batch(self.h, ptr(m, C.c_int32), ptr(th), th.shape[1], th.shape[0], seed,
+                                                offset, ptr(out)))
+        return out
+
+    def simulate_batch_device(self, d_models: int, d_theta: int, ld: int, n: int, seed: int, d_stats: int,
+                              offset: int = 0) -> None:
+        self._check(self.lib.abc_simulate_batch_device(self.h, C.c_void_p(d_models), C.c_void_p(d_theta), ld, n,
+                                                       seed, offset, C.c_void_p(d_stats)))
+
+    def synchronize(self) -> None:
+        self._check(self.lib.abc_synchronize(self.h))
+
+    def simulate_cells(self, model: int, theta: np.ndarray, seed: int, offset: int = 0) -> dict:
+        th = np.ascontiguousarray(theta, np.float64)
+        P, Cn = th.shape[0], self.cells.n
+        out = {"counts": np.zeros((P, Cn, 2), np.int32), "captured": np.zeros((P, Cn, 2), np.int32),
+               "events": np.zeros((P, Cn), np.int64), "hash": np.zeros((P, Cn), np.uint64),
+               "stats": np.zeros((P, self.K))}
+        self._check(self.lib.abc_simulate_cells(
+            self.h, model, ptr(th), P, seed, offset, ptr(out["counts"], C.c_int32), ptr(out["captured"], C.c_int32),
+            ptr(out["events"], C.c_int64), ptr(out["hash"], C.c_uint64), ptr(out["stats"])))
+        return out
+
+    def profile(self, enable: bool = True) -> None:
+        self._check(self.lib.abc_profile(self.h, int(enable)))
+
+    def phase_ms(self) -> tuple[float, float, float]:
+        """[setup, SSA, capture+statistics] kernel milliseconds of the last synchronized call."""
+        out = np.zeros(3)
+        self._check(self.lib.abc_profile_read(self.h, ptr(out)))
+        return float(out[0]), float(out[1]), float(out[2])
+
+    def last_counters(self) -> tuple[int, int]:
+        ev, rej = C.c_int64(), C.c_int64()
+        self._check(self.lib.abc_last_counters(self.h, C.byref(ev), C.byref(rej)))
+        return ev.value, rej.value
+
+    # -- distance + acceptance --------------------------------------------
+    @staticmethod
+    def _fam(families, K):
+        if families is None:
+            return 0, None
+        f = np.ascontiguousarray(families, np.int32)
+        if int(f.sum()) != K:
+            raise ValueError("family sizes must sum to K")
+        return f.shape[0], f
+
+    def errors(self, data: np.ndarray, se: np.ndarray, stats: np.ndarray, families=None) -> np.ndarray:
+        d = np.ascontiguousarray(data, np.float64)
+        e = np.ascontiguousarray(se, np.float64)
+        s = np.ascontiguousarray(stats, np.float64)
+        G, K = d.shape
+        nf, f = self._fam(families, K)
+        out = np.zeros((s.shape[0], G))
+        self._check(self.lib.abc_errors(self.h, ptr(d), ptr(e), G, K, nf, ptr(f, C.c_int32), ptr(s), s.shape[0],
+                                        ptr(out)))
+        return out
+
+    def select(self, data: np.ndarray, se: np.ndarray, stats: np.ndarray, mode: int, eps_or_q: float,
+               families=None) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """Accepted particles per gene: (offsets[G+1], 1-based indices, errors)."""
+        d = np.ascontiguousarray(data, np.float64)
+        e = np.ascontiguousarray(se, np.float64)
+        s = np.ascontiguousarray(stats, np.float64)
+        G, K = d.shape
+        nf, f = self._fam(families, K)
+        tot = C.c_int64()
+        self._check(self.lib.abc_errors_select(self.h, ptr(d), ptr(e), G, K, nf, ptr(f, C.c_int32), ptr(s),
+                                               s.shape[0], mode, float(eps_or_q), C.byref(tot)))
+        off = np.zeros(G + 1, np.int64)
+        idx = np.zeros(max(tot.value, 1), np.int64)
+        err = np.zeros(max(tot.value, 1))
+        self._check(self.lib.abc_accept_fetch(self.h, ptr(off, C.c_int64), ptr(idx, C.c_int64), ptr(err)))
+        return off, idx[:tot.value], err[:tot.value]
+
+    def select_counters(self) -> tuple[int, int]:
+        a, b = C.c_int64(), C.c_int64()
+        self._check(self.lib.abc_select_counters(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+
+# ---------------------------------------------------------------------------
+# Reference-named entry points (same argument meaning; batched over particles)
+# ---------------------------------------------------------------------------
+def fix_params(ctx: Context, model: int, n: int, seed: int, prior: AbcPrior, offset: int = 0) -> np.ndarray:
+    """Prior draw of n particles, column order hcat(kon, koff, alpha, gamma, lambda)
+    with the varying rate expanded (scripts/abc_simulation.jl:3-11)."""
+    return ctx.sample_prior(model, n, seed, prior, offset)
+
+
+def abc_sim(ctx: Context, model: int, theta: np.ndarray, seed: int, offset: int = 0) -> dict:
+    """Statistics of each particle in the reference's five outputs
+    (scripts/abc_simulation.jl:47-61): s_pulse and s_chase (2 x A each: mean
+    row then Fano-factor row), s_ratios, s_mean_corr, s_corr_mean (J each)."""
+    st = ctx.simulate(model, theta, seed, offset)
+    return split_stats(st, ctx.cfg.n_ages, ctx.cfg.n_conds)
+
+
+def split_stats(st: np.ndarray, A: int, J: int) -> dict:
+    return {
+        "s_pulse": np.stack([st[:, 0:A], st[:, A:2 * A]], axis=1),
+        "s_chase": np.stack([st[:, 2 * A:3 * A], st[:, 3 * A:4 * A]], axis=1),
+        "s_ratios": st[:, 4 * A:4 * A + J],
+        "s_mean_corr": st[:, 4 * A + J:4 * A + 2 * J],
+        "s_corr_mean": st[:, 4 * A + 2 * J:4 * A + 3 * J],
+    }
+
+
+def compute_trunc_errors(ctx: Context, data: np.ndarray, se: np.ndarray, stats: np.ndarray,
+                         families=tuple(REF_FAMILIES)) -> np.ndarray:
+    """P x G clipped normalised errors (scripts/compute_errors.jl:45-70)."""
+    return ctx.errors(data, se, stats, families)
+
+
+def accepted_particles(ctx: Context, data: np.ndarray, se: np.ndarray, stats: np.ndarray, eps: float = 4.8,
+                       families=tuple(REF_FAMILIES)) -> list[list[int]]:
+    """Per gene: 1-based particle indices with err <= eps sorted by error, or [0]
+    when none (scripts/accepted_particles.jl:20-29)."""
+    off, idx, _ = ctx.select(data, se, stats, 0, eps, families)
+    out = []
+    for g in range(off.shape[0] - 1):
+        lst = idx[off[g]:off[g + 1]].tolist()
+        out.append(lst if lst else [0])
+    return out

@@ -1,0 +1,354 @@
+#!/usr/bin/env python3
+"""Benchmark of the ABC simulation hot path on GB300.
+
+Workload (one step): the five-model ABC batch -- all 5 gene models mixed in
+one persistent FP32 SSA launch (FP64 clock), PER_MODEL particles per model x
+2,000 synthetic cells (1,200 pulse, 800 chase, Beta(4,16) capture), the
+reference time grid (cycle 20 h, 5 age groups, 11 labelling conditions),
+followed by binomial capture and the 53 summary statistics per particle.
+Metric: fired SSA events per second.  A fresh random stream (seed) per step.
+
+  value       device-timed (CUDA events on the library's stream), inputs
+              resident in HBM; the per-cell count buffer (> 129 MB L2) is
+              rewritten every step, so no L2 flush is needed.
+  e2e         the same step through the public host API (abc_simulate_batch
+              with host theta / host statistics, copies inside the timed region).
+  roofline    SSA kernel against the instruction-issue roofline (algorithmic
+              ops per event x events / SSA kernel time vs 152 SMs x 128 lanes x
+              max SM clock); capture+statistics kernel against HBM bandwidth.
+  cpu_baseline  the FP64 CPU SSA (oracle port, OpenMP over host cores) on a
+              bounded sample of the same particles.
+
+--impl reference: the CPU implementation alone (rank 0), same metric/config.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_CELLS = 2000
+OPS_PER_EVENT = 60          # algorithmic instruction count per fired event
+LANES_PER_SM = 128
+SMS = 152
+PER_MODEL_DEFAULT = 4000
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--per-model", type=int, default=PER_MODEL_DEFAULT)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+        return pk, "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def workload(per_model: int, seed0: int, offset: int):
+    """theta of the five-model batch (prior draws on the GPU), padded to 9 columns."""
+    import numpy as np
+    from abc_inference_transcription_gb300 import FP32, factor_prior, make_config, synthetic_cells
+    from abc_inference_transcription_gb300.host import Context
+    cfg = make_config("hour", precision=FP32)
+    cells = synthetic_cells(seed=1)
+    ctx = Context(cfg, cells)
+    pr = factor_prior()
+    thetas, models = [], []
+    for m in range(1, 6):
+        th = ctx.sample_prior(m, per_model, seed0 + m, pr, offset=offset + (m - 1) * per_model)
+        pad = np.zeros((per_model, 9))
+        pad[:, :th.shape[1]] = th
+        thetas.append(pad)
+        models.append(np.full(per_model, m, np.int32))
+    return cfg, cells, ctx, np.vstack(thetas), np.concatenate(models)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_ssa_rate(cfg, cells, theta, models, seconds: float, threads: int):
+    """FP64 CPU SSA (the oracle port) on a growing sample of the same particles,
+    interleaved over the five models, until one run takes >= seconds/3."""
+    import numpy as np
+    from abc_inference_transcription_gb300 import FP64
+    from oracle import oracle as orc
+    orc.build()
+    import copy
+    cfg64 = copy.copy(cfg)
+    cfg64.precision = FP64
+    P = theta.shape[0]
+    per_model = P // 5
+    order = np.concatenate([[m * per_model + i for m in range(5)] for i in range(per_model)])
+    n = 5
+    while True:
+        sel = order[:n]
+        ev = 0
+        t0 = time.perf_counter()
+        for m in range(1, 6):
+            rows = sel[models[sel] == m]
+            if rows.size == 0:
+                continue
+            npar = 5 if m <= 2 else 9
+            out = orc.simulate(cfg64, cells, m, theta[rows, :npar], seed=77, n_threads=threads, want_cells=True)
+            ev += int(out["events"].sum())
+        dt = time.perf_counter() - t0
+        if dt >= seconds / 3 or n >= P:
+            return ev / dt, n, dt, ev
+        n = min(P, max(n + 5, int(n * max(2.0, seconds / 3 / max(dt, 1e-3)))))
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import numpy as np
+    from abc_inference_transcription_gb300 import FP64, factor_prior, make_config, synthetic_cells
+    from oracle import oracle as orc
+    orc.build()
+    cfg = make_config("hour", precision=FP64)
+    cells = synthetic_cells(seed=1)
+    per_model = args.per_model
+    thetas, models = [], []
+    for m in range(1, 6):
+        th = orc.sample_prior(cfg, m, per_model, 11 + m, factor_prior(), offset=(m - 1) * per_model)
+        pad = np.zeros((per_model, 9))
+        pad[:, :th.shape[1]] = th
+        thetas.append(pad)
+        models.append(np.full(per_model, m, np.int32))
+    theta, mods = np.vstack(thetas), np.concatenate(models)
+    threads = os.cpu_count() or 1
+    rates = []
+    n_sample = None
+    for k in range(args.warmup + args.steps):
+        budget = max(2.0, min(args.cpu_seconds, 150.0 / max(1, args.warmup + args.steps)))
+        rate, n, dt, ev = cpu_ssa_rate(cfg, cells, theta, mods, budget, threads)
+        n_sample = n
+        if k >= args.warmup:
+            rates.append(rate)
+    value = statistics.median(rates)
+    sample = f"first {n_sample} particles of the five-model batch (interleaved models) x {N_CELLS} cells per step"
+    line = {
+        "impl": "reference", "metric": "SSA events/s", "value": value, "unit": "events/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded prior draws, synthetic cells)",
+        "config": {"workload": f"five-model SSA batch, {args.per_model} particles/model x {N_CELLS} cells, "
+                               "reference time grid (h)", "cells": N_CELLS},
+        "cpu_baseline": {"value": value, "unit": "events/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference is Julia (not installed); this is the FP64 C restatement of its simulation, "
+                "the exact SSA of the same reaction network",
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import numpy as np
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    if rank == 0:
+        import __graft_entry__
+        __graft_entry__.build()
+    if dist:
+        dist.barrier()
+
+    P_rank = 5 * args.per_model
+    cfg, cells, ctx, theta, models = workload(args.per_model, 11, rank * P_rank)
+    ld = theta.shape[1]
+    K = ctx.K
+    d_theta = torch.from_numpy(theta).cuda()
+    d_models = torch.from_numpy(models).cuda()
+    d_stats = torch.empty((P_rank, K), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    ctx.profile(True)
+
+    def step(seed):
+        ctx.simulate_batch_device(d_models.data_ptr(), d_theta.data_ptr(), ld, P_rank, seed, d_stats.data_ptr(),
+                                  offset=rank * P_rank)
+        ctx.synchronize()
+        ev, rej = ctx.last_counters()
+        return ev, rej, ctx.phase_ms()
+
+    for w in range(args.warmup):
+        step(500 + w)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sampler = ClockSampler(local)
+    sampler.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    tot_ev = tot_rej = 0
+    phase = np.zeros(3)
+    for k in range(args.steps):
+        ev, rej, ph = step(1000 + k)
+        tot_ev += ev
+        tot_rej += rej
+        phase += np.array(ph)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    t_ms = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([t_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_ms = float(t.item())
+        e = torch.tensor([tot_ev], device="cuda", dtype=torch.float64)
+        dist.all_reduce(e, op=dist.ReduceOp.SUM)
+        tot_ev_all = float(e.item())
+    else:
+        tot_ev_all = float(tot_ev)
+    value = tot_ev_all / (t_ms / 1e3)
+
+    # e2e through the host API
+    e2e = None
+    if not args.no_e2e:
+        st_host = np.zeros((P_rank, K))
+        ctx.simulate_batch(models, theta, 900, offset=rank * P_rank)  # warm host path
+        t0 = time.perf_counter()
+        ev_e2e = 0
+        for k in range(args.steps):
+            st_host = ctx.simulate_batch(models, theta, 1000 + k, offset=rank * P_rank)
+            ev_e2e += ctx.last_counters()[0]
+        dt = time.perf_counter() - t0
+        if dist:
+            t = torch.tensor([dt], device="cuda", dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt = float(t.item())
+            e = torch.tensor([ev_e2e], device="cuda", dtype=torch.float64)
+            dist.all_reduce(e, op=dist.ReduceOp.SUM)
+            ev_e2e = float(e.item())
+        e2e = {"value": ev_e2e / dt, "unit": "events/s", "h2d_bytes_per_step": int(theta.nbytes + models.nbytes),
+               "d2h_bytes_per_step": int(st_host.nbytes)}
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    peaks, peak_src = load_peaks()
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    ssa_s = phase[1] / 1e3
+    achieved_ev = tot_ev / ssa_s
+    peak_ev = SMS * LANES_PER_SM * sm_max * 1e6 / OPS_PER_EVENT
+    stats_bytes = args.steps * (P_rank * N_CELLS * 8 + P_rank * K * 8)
+    stats_gbs = stats_bytes / (phase[2] / 1e3) / 1e9
+    cpu = None
+    try:
+        rate, n, dt, ev = cpu_ssa_rate(cfg, cells, theta, models, args.cpu_seconds, os.cpu_count() or 1)
+        cpu = {"value": rate, "unit": "events/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"first {n} particles of the same batch (interleaved models) x {N_CELLS} cells, "
+                         f"{ev} events in {dt:.1f} s, FP64 oracle SSA"}
+    except Exception as exc:  # the oracle is a reported baseline only
+        cpu = {"value": None, "unit": "events/s", "cores": os.cpu_count(), "kind": "port", "sample": repr(exc)}
+    line = {
+        "metric": "SSA events/s", "value": value, "unit": "events/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (FP64 clock)", "data": "synthetic (seeded prior draws, synthetic cells)",
+        "config": {"workload": f"five-model SSA batch: 5 x {args.per_model} particles x {N_CELLS} cells, "
+                               "reference time grid (h), factor prior, capture + 53 statistics",
+                   "particles_per_step": P_rank * world, "cells": N_CELLS, "parallelism": f"particle shards x{world}",
+                   "l2": "per-cell count buffer (P x C x 8 B) exceeds L2 and is rewritten every step"},
+        "events_per_step": tot_ev_all / args.steps, "thinning_rejections": tot_rej,
+        "particles_per_s": P_rank * world * args.steps / (t_ms / 1e3),
+        "phase_ms_per_step": {"setup": phase[0] / args.steps, "ssa": phase[1] / args.steps,
+                              "capture_stats": phase[2] / args.steps},
+        "roofline": {"bound": "issue", "achieved": achieved_ev / 1e9, "peak": peak_ev / 1e9, "unit": "Gevents/s",
+                     "frac": achieved_ev / peak_ev, "traffic": None,
+                     "basis": f"{OPS_PER_EVENT} algorithmic ops/event, {SMS} SMs x {LANES_PER_SM} lanes x "
+                              f"{sm_max:.0f} MHz ({peak_src} sm_max)"},
+        "roofline_stats": {"bound": "hbm", "achieved": stats_gbs, "peak": float(peaks.get("hbm_gbs", 6800.0)),
+                           "unit": "GB/s", "frac": stats_gbs / float(peaks.get("hbm_gbs", 6800.0)),
+                           "traffic": None, "peak_source": peak_src},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": 3 * args.steps,
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,186 @@
+/*
+ * abcgpu.h — C ABI of libabcgpu.so, the GB300 (sm_103a) implementation of the
+ * ABC simulation + rejection hot path of pthomaslab/abc_inference_transcription.
+ *
+ * The reference has no FFI layer: its "API" is a set of Julia functions that
+ * are `include`d by wrapper.jl.  Every entry point below names the reference
+ * function (file:line, paths inside the reference project) whose role it takes.
+ *
+ * Conventions
+ *   - Status: 0 on success, a negative abc_status on failure.  Nothing aborts
+ *     or traps; abc_last_error() returns a message for the last failure.
+ *   - Matrices are ROW-MAJOR with the row index first ("P x npar" means row p
+ *     holds particle p).  A Julia caller passes the transpose of its
+ *     column-major matrix (identical memory), see INTEGRATION.md.
+ *   - Particle indices returned by the acceptance step are 1-based (reference
+ *     convention, scripts/accepted_particles.jl:20-26).
+ *   - Host pointers unless the function name ends in _device.
+ *   - One context = one CUDA stream = one host thread.  Independent contexts
+ *     are safe to use from different threads.
+ *   - No CPU fallback: without a usable CUDA device abc_create fails.
+ */
+#ifndef ABCGPU_H
+#define ABCGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ABC_MAX_AGES   8
+#define ABC_MAX_CONDS 16
+#define ABC_MAX_STEPS  8
+#define ABC_MAX_PARAMS 32
+#define ABC_MAX_FAMILIES 16
+
+/* Statistics per particle in the reference layout (scripts/compute_errors.jl:148,152-154):
+ * pulse_mean[A], pulse_ff[A], chase_mean[A], chase_ff[A], ratio[J], mean_corr[J], corr_mean[J]. */
+#define ABC_NSTATS(A, J) (4 * (A) + 3 * (J))
+
+typedef enum abc_status {
+  ABC_OK = 0,
+  ABC_ERR_INVALID = -1,   /* bad argument or configuration */
+  ABC_ERR_CUDA = -2,      /* a CUDA runtime call failed */
+  ABC_ERR_NOMEM = -3,     /* device allocation failed */
+  ABC_ERR_EVENT_CAP = -4, /* a trajectory exceeded abc_config.event_cap fired events */
+  ABC_ERR_NONFINITE = -5, /* non-finite rate or count overflow inside a kernel */
+  ABC_ERR_CAPACITY = -6,  /* candidate buffer could not be grown or top-q did not converge */
+  ABC_ERR_STATE = -7      /* call order violated (e.g. simulate before set_cells) */
+} abc_status;
+
+/* Model index m, as in wrapper.jl:47-51 and scripts/abc_simulation.jl:82-85. */
+typedef enum abc_model {
+  ABC_MODEL_CONST = 1,       /* constant rates, transcription scales with size */
+  ABC_MODEL_CONST_CONST = 2, /* constant rates, no size scaling */
+  ABC_MODEL_KON = 3,         /* burst frequency k_on varies over the age steps */
+  ABC_MODEL_ALPHA = 4,       /* burst size (synthesis rate) varies */
+  ABC_MODEL_GAMMA = 5        /* decay rate varies */
+} abc_model;
+
+typedef enum abc_precision {
+  ABC_FP64 = 0, /* oracle mode: bit-exact with the FP64 CPU oracle */
+  ABC_FP32 = 1  /* production mode: FP32 propensities, FP64 clock */
+} abc_precision;
+
+/* Time grid, labelling conditions and model options (all times in the unit of
+ * the rates; the reference uses hours with cycle = 20, scripts/abc_simulation.jl:65-79). */
+typedef struct abc_config {
+  double  cycle;                  /* cell-cycle length T */
+  int32_t n_burn_cycles;          /* trajectories start at t0 = -n_burn_cycles*T (reference 3, abc_simulation.jl:73) */
+  int32_t n_steps;                /* age steps of a varying rate (reference 5, model.jl:181) */
+  int32_t n_ages;                 /* A: observation ages (reference 5, abc_simulation.jl:74) */
+  int32_t n_conds;                /* J: labelling conditions (reference 11, abc_simulation.jl:65) */
+  double  ages[ABC_MAX_AGES];     /* observation ages, each in (0, T) */
+  double  pulse[ABC_MAX_CONDS];   /* pulse length per condition */
+  double  chase[ABC_MAX_CONDS];   /* chase length per condition */
+  int32_t pulse_stat_cond;        /* 0-based condition giving pulse mean/FF (reference j==6 -> 5) */
+  int32_t chase_stat_cond;        /* 0-based condition giving chase mean/FF (reference j==7 -> 6) */
+  int32_t splicing;               /* 0: reference model (G,u,l); 1: unspliced->spliced, extra theta column */
+  int32_t scaling_column;         /* 0: size-scaling exponent fixed by the model; 1: last theta column */
+  int32_t precision;              /* abc_precision */
+  int32_t reserved0;
+  int64_t event_cap;              /* fired events allowed per trajectory (<= 0: 2^28) */
+} abc_config;
+
+/* Prior of the log10 rates (scripts/abc_simulation.jl:3-11).  Ranges are log10
+ * bounds except scaling, whose bounds are linear (drawn log-uniformly). */
+typedef struct abc_prior {
+  double kon[2], koff[2], alpha[2], gamma[2], lambda[2], beta[2], scaling[2];
+  int32_t vary_mode;   /* 0: the varying rate gets n_steps independent draws (reference);
+                          1: base draw times a log-uniform factor per step */
+  int32_t reserved0;
+  double factor[2];    /* linear factor bounds for vary_mode 1, e.g. {0.2, 5} */
+} abc_prior;
+
+typedef struct abc_ctx abc_ctx;
+
+/* Create a context on the current CUDA device.  Replaces the global model
+ * configuration of scripts/abc_simulation.jl:64-85. */
+int abc_create(abc_ctx** out, const abc_config* cfg);
+int abc_destroy(abc_ctx* ctx);
+const char* abc_last_error(const abc_ctx* ctx);
+/* Number of theta columns for a model under this context's configuration
+ * (get_vary_map, scripts/model.jl:30-43, plus the optional extensions). */
+int abc_num_params(const abc_ctx* ctx, int model);
+/* Number of statistics per particle, 4A + 3J (scripts/compute_errors.jl:148). */
+int abc_num_stats(const abc_ctx* ctx);
+/* cudaStream_t used by the context, as void*. */
+void* abc_stream(abc_ctx* ctx);
+
+/* Synthetic cell table: labelling condition (0-based), age group (0-based) and
+ * capture efficiency of each cell, and the A x J age/condition weights
+ * (row-major, weights[a*J + j]).  Replaces betas / age / pulse_idx / chase_idx /
+ * age_id_distribution (scripts/abc_simulation.jl:14, scripts/load_process_data.jl:68-81).
+ * Every (condition, age) group must hold at least 2 cells. */
+int abc_set_cells(abc_ctx* ctx, int64_t n_cells, const int32_t* cell_cond,
+                  const int32_t* cell_age, const double* cell_beta,
+                  const double* age_dist);
+
+/* Prior draw, fix_params (scripts/abc_simulation.jl:3-11).  theta_out: P x npar. */
+int abc_sample_prior(abc_ctx* ctx, int model, int64_t n_particles, uint64_t seed,
+                     int64_t particle_offset, const abc_prior* prior, double* theta_out);
+
+/* Simulate particles and return their statistics, abc_sim
+ * (scripts/abc_simulation.jl:13-62; the per-particle loop at :88-97).
+ * theta: P x npar (log10 rates), stats_out: P x nstats.  Particle p uses the
+ * random streams of global particle index particle_offset + p. */
+int abc_simulate(abc_ctx* ctx, int model, const double* theta, int64_t n_particles,
+                 uint64_t seed, int64_t particle_offset, double* stats_out);
+/* Same with device pointers, stream-ordered on abc_stream(ctx); returns after
+ * enqueueing.  abc_synchronize() reports kernel status words. */
+int abc_simulate_device(abc_ctx* ctx, int model, const double* d_theta, int64_t n_particles,
+                        uint64_t seed, int64_t particle_offset, double* d_stats);
+int abc_synchronize(abc_ctx* ctx);
+
+/* Several models in one launch (the five-model ABC batch): particle p is
+ * simulated with model models[p] (1..5) from theta row p; the row stride
+ * ld_theta must be at least the largest npar of any model (9 for the reference
+ * configuration).  Same output as abc_simulate. */
+int abc_simulate_batch(abc_ctx* ctx, const int32_t* models, const double* theta, int64_t ld_theta,
+                       int64_t n_particles, uint64_t seed, int64_t particle_offset, double* stats_out);
+int abc_simulate_batch_device(abc_ctx* ctx, const int32_t* d_models, const double* d_theta, int64_t ld_theta,
+                              int64_t n_particles, uint64_t seed, int64_t particle_offset, double* d_stats);
+
+/* Per-cell view of abc_simulate for parity tests: raw counts (u, l) at the
+ * observation time, captured counts, fired-event counts and event-sequence
+ * hashes, each P x C in the caller's cell order (any pointer may be NULL). */
+int abc_simulate_cells(abc_ctx* ctx, int model, const double* theta, int64_t n_particles,
+                       uint64_t seed, int64_t particle_offset, int32_t* counts_out,
+                       int32_t* captured_out, int64_t* events_out, uint64_t* hash_out,
+                       double* stats_out);
+
+/* Counters of the last simulate call: fired events and thinning rejections. */
+int abc_last_counters(const abc_ctx* ctx, int64_t* events, int64_t* rejections);
+/* Per-kernel device timing (CUDA events on the context stream), the tracing
+ * counterpart of the reference's @time (scripts/abc_simulation.jl:88).
+ * abc_profile_read returns, for the last synchronized simulate call, the
+ * milliseconds spent in [setup, SSA, capture+statistics] kernels. */
+int abc_profile(abc_ctx* ctx, int enable);
+int abc_profile_read(const abc_ctx* ctx, double* ms_out);
+
+/* Error matrix, compute_trunc_errors / nlsqerror_part (scripts/compute_errors.jl:30-70):
+ * err[p*G+g] = min(10, sum_f sum_{k in f} (d-s)^2/(se^2+0.01 d^2+eps)/K).
+ * data, se: G x K; stats: P x K; family sizes sum to K (NULL: one family). */
+int abc_errors(abc_ctx* ctx, const double* data, const double* se, int64_t n_genes, int K,
+               int n_families, const int32_t* family_sizes, const double* stats,
+               int64_t n_particles, double* err_out);
+
+/* Acceptance, scripts/accepted_particles.jl:12-32.  mode 0: accept err <= eps
+ * (reference eps = 4.8); mode 1: accept the ceil(q*P) smallest errors per gene.
+ * Accepted sets equal the FP64 oracle's; lists are sorted by (err, index).
+ * Results stay in the context; fetch them with abc_accept_fetch. */
+int abc_errors_select(abc_ctx* ctx, const double* data, const double* se, int64_t n_genes,
+                      int K, int n_families, const int32_t* family_sizes,
+                      const double* stats, int64_t n_particles, int mode, double eps_or_q,
+                      int64_t* n_accepted_total);
+/* gene_offsets: G+1 entries; particle_idx: 1-based, n_accepted_total entries;
+ * err: FP64 errors of the accepted pairs (may be NULL). */
+int abc_accept_fetch(abc_ctx* ctx, int64_t* gene_offsets, int64_t* particle_idx, double* err);
+/* Counters of the last selection: FP32 candidates rechecked in FP64. */
+int abc_select_counters(const abc_ctx* ctx, int64_t* candidates, int64_t* rechecked);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ABCGPU_H */

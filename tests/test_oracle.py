@@ -1,0 +1,220 @@
+"""CPU tests of the FP64 oracle: pinned against the known-answer vectors and
+the reference's golden outputs before it is trusted as the GPU checker."""
+import math
+
+import numpy as np
+import pytest
+
+from abc_inference_transcription_gb300.config import (N_PULSE_CONDS, REF_FAMILIES, beta_moments, make_config,
+                                                       reference_prior, minute_prior, synthetic_cells)
+from conftest import GOLDEN
+
+MODELS = ["const", "const_const", "kon", "alpha", "gamma"]
+
+
+# --- Philox4x32-10 known-answer vectors (Random123 kat_vectors, philox4x32 10 rounds)
+KAT = [
+    ([0, 0, 0, 0], [0, 0], [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]),
+    ([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2, [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]),
+    ([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0],
+     [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]),
+]
+
+
+@pytest.mark.parametrize("ctr,key,want", KAT)
+def test_philox_kat(orc, ctr, key, want):
+    assert [int(x) for x in orc.philox(ctr, key)] == want
+
+
+def test_xlog_xexp_accuracy(orc):
+    rng = np.random.default_rng(0)
+    xs = np.exp(rng.uniform(-700, 700, 4000))
+    rel = max(abs(orc.xlog(x) - math.log(x)) / abs(math.log(x)) for x in xs if abs(math.log(x)) > 1e-3)
+    assert rel < 4.5e-16
+    us = rng.uniform(2.0 ** -33, 1.0, 4000)
+    assert max(abs(orc.xlog(u) - math.log(u)) for u in us) < 2e-15
+    ys = rng.uniform(-700, 700, 4000)
+    assert max(abs(orc.xexp(y) - math.exp(y)) / math.exp(y) for y in ys) < 4.5e-16
+    assert orc.xexp(-800.0) == 0.0 and math.isinf(orc.xexp(800.0))
+    assert orc.xexp(0.0) == 1.0 and orc.xlog(1.0) == 0.0
+
+
+@pytest.mark.parametrize("n,p", [(7, 0.3), (40, 0.1), (1000, 0.004), (60, 0.5), (5000, 0.14), (123456, 0.2),
+                                 (200, 0.93), (10 ** 6, 0.5)])
+def test_binomial_moments(orc, n, p):
+    draws = orc.binomial(n, p, 20000, seed=3, stream=1)
+    assert draws.min() >= 0 and draws.max() <= n
+    mean, var = n * p, n * p * (1 - p)
+    se_mean = math.sqrt(var / draws.size)
+    assert abs(draws.mean() - mean) < 5 * se_mean
+    # variance within 5 standard errors (kurtosis of a binomial ~ 3)
+    assert abs(draws.var() - var) < 5 * var * math.sqrt(2.0 / draws.size) + 1e-9
+
+
+def test_binomial_small_exact_distribution(orc):
+    n, p = 12, 0.35
+    draws = orc.binomial(n, p, 60000, seed=9, stream=1)
+    obs = np.bincount(draws, minlength=n + 1)
+    expect = np.array([math.comb(n, k) * p ** k * (1 - p) ** (n - k) for k in range(n + 1)]) * draws.size
+    mask = expect > 5
+    chi2 = (((obs - expect) ** 2) / expect)[mask].sum()
+    assert chi2 < 45  # ~ chi2 with <= 12 dof, p ~ 1e-5
+
+
+def test_prior_ranges(orc):
+    cfg = make_config("hour")
+    pr = reference_prior()
+    for model in range(1, 6):
+        th = orc.sample_prior(cfg, model, 2000, 5, pr)
+        npar = 5 if model <= 2 else 9
+        assert th.shape == (2000, npar)
+        lo = {1: -3, 2: -3, 3: -3, 4: -3, 5: -3}
+        assert th.min() >= -3.0 and th.max() <= 3.0
+        assert th[:, -1].min() >= -0.7 and th[:, -1].max() <= 0.0
+    cfgm = make_config("min", splicing=True, scaling_column=True)
+    th = orc.sample_prior(cfgm, 1, 3000, 6, minute_prior())
+    assert th.shape == (3000, 7)
+    assert 0.5 <= th[:, -1].min() and th[:, -1].max() <= 2.0
+
+
+def _load_golden():
+    z = np.load(f"{GOLDEN}/recovered_statistics.npz")
+    return z
+
+
+@pytest.mark.parametrize("mi", range(5))
+def test_moment_ode_matches_reference_golden(orc, mi):
+    """The moment-ODE restatement reproduces data/recovered_statistics (written
+    by scripts/recover_statistics.jl with iv[1] = 1/2, no capture).  The golden
+    values come from CVODE_BDF at default tolerances with the 1 % steady-state
+    stopping rule (scripts/model.jl:114-142), so agreement is ~1e-2."""
+    z = _load_golden()
+    name = MODELS[mi]
+    theta, gold = z[f"{name}_theta"], z[f"{name}_moments"]
+    cfg = make_config("hour")
+    iv = np.zeros(9)
+    iv[0] = 0.5
+    errs = []
+    for r in range(theta.shape[0]):
+        mom = orc.moment_model(cfg, mi + 1, theta[r], iv)["moments"]
+        errs.append(np.max(np.abs(mom - gold[r]) / (np.abs(gold[r]) + 0.01)))
+    errs = np.array(errs)
+    assert np.median(errs) < 2.0e-2, errs
+    assert errs.max() < 5.0e-2, errs
+
+
+def test_stats_formulas_against_numpy(orc):
+    """Aggregation of abc_simulation.jl:23-46 restated independently in numpy."""
+    cfg = make_config("hour")
+    rng = np.random.default_rng(4)
+    m = np.abs(rng.normal(3, 1, (11, 5, 5)))
+    w = rng.uniform(0.0, 0.05, (5, 11))
+    got = orc.stats_from_moments(cfg, m, w)
+    A, J = 5, 11
+    want = np.zeros(53)
+    for j in range(J):
+        ww = w[:, j]
+        mu, ml, vu, cv, vl = (m[j, :, q] for q in range(5))
+        wc = lambda x, y: np.sum(ww * ((x - np.sum(ww * x)) * (y - np.sum(ww * y))))
+        want[4 * A + j] = np.sum(ww * ml) / (np.sum(ww * mu) + np.sum(ww * ml))
+        stds = math.sqrt(abs((np.sum(ww * vu) + wc(mu, mu)) * (np.sum(ww * vl) + wc(ml, ml))))
+        want[4 * A + J + j] = np.sum(ww * cv) / stds
+        want[4 * A + 2 * J + j] = wc(mu, ml) / stds
+        if j in (5, 6):
+            off = 0 if j == 5 else 2 * A
+            want[off:off + A] = mu + ml
+            want[off + A:off + 2 * A] = (vu + 2 * cv + vl) / (mu + ml)
+    assert np.allclose(got, want, rtol=1e-13, atol=1e-15)
+
+
+def test_ssa_oracle_bridge_to_moment_ode(orc):
+    """SSA oracle raw counts vs the moment-ODE expectations: per (condition,
+    age) mean of u and l within a few Monte Carlo standard errors."""
+    cfg = make_config("hour", precision=0)
+    cells = synthetic_cells(n_per_pulse=600, n_per_chase=600, seed=3)
+    theta = np.log10([0.5, 1.0, 20.0, 0.1, 0.7])
+    out = orc.simulate(cfg, cells, 1, theta[None, :], seed=7, n_threads=0)
+    assert out["status"] == 0
+    ode = orc.moment_model(cfg, 1, theta, np.array([0, 0.5, 0, 0, 0, 0, 0, 0, 0.0]))["moments"]
+    z = []
+    for j in range(11):
+        for a in range(5):
+            sel = (cells.cond == j) & (cells.age == a)
+            n = sel.sum()
+            for q, col in ((0, 0), (1, 1)):
+                x = out["counts"][0, sel, col].astype(float)
+                z.append((x.mean() - ode[j, a, q]) / math.sqrt(max(ode[j, a, 2 + 2 * q], 1e-9) / n))
+    z = np.array(z)
+    assert abs(z.mean()) < 0.5 and z.std() < 1.4 and np.abs(z).max() < 4.5, z
+
+
+def test_ssa_oracle_deterministic_and_offset(orc):
+    cfg = make_config("hour", precision=0)
+    cells = synthetic_cells(n_per_pulse=10, n_per_chase=10, seed=2)
+    th = orc.sample_prior(cfg, 3, 6, 1, reference_prior())
+    th[:, :5] = np.minimum(th[:, :5], 1.0)
+    th[:, 6] = np.minimum(th[:, 6], 1.5)
+    a = orc.simulate(cfg, cells, 3, th, seed=4)
+    b = orc.simulate(cfg, cells, 3, th, seed=4, n_threads=2)
+    assert np.array_equal(a["hash"], b["hash"]) and np.array_equal(a["counts"], b["counts"])
+    # particles keep their streams when split with particle_offset
+    c = orc.simulate(cfg, cells, 3, th[3:], seed=4, offset=3)
+    assert np.array_equal(c["counts"], a["counts"][3:]) and np.array_equal(c["hash"], a["hash"][3:])
+
+
+def test_event_cap_reports_status(orc):
+    cfg = make_config("hour", precision=0, event_cap=10)
+    cells = synthetic_cells(n_per_pulse=10, n_per_chase=10, seed=2)
+    th = np.log10([[5.0, 1.0, 50.0, 1.0, 0.7]])
+    out = orc.simulate(cfg, cells, 1, th, seed=1)
+    assert out["status"] == -4
+
+
+def _numpy_errors(data, se, stats, fam):
+    """compute_errors.jl:30-70 restated with numpy broadcasting."""
+    eps = np.where(se + data != 0.0, 0.0, 0.0001)
+    den = se ** 2 + 0.01 * data ** 2 + eps
+    t = (data[None, :, :] - stats[:, None, :]) ** 2 / den[None, :, :]
+    K = data.shape[1]
+    out = np.zeros(t.shape[:2])
+    k = 0
+    for f in fam:
+        out = out + t[:, :, k:k + f].sum(axis=2) / K
+        k += f
+    return np.minimum(out, 10.0, where=~np.isnan(out), out=out.copy())
+
+
+def test_errors_oracle_matches_numpy_on_reference_data(orc):
+    z = np.load(f"{GOLDEN}/summary_stats.npz")
+    data, se = z["data"][:64], z["se"][:64]
+    rng = np.random.default_rng(1)
+    stats = data[rng.integers(0, 64, 40)] * rng.lognormal(0, 0.3, (40, 53))
+    got = orc.errors(data, se, stats, REF_FAMILIES)
+    want = _numpy_errors(data, se, stats, REF_FAMILIES)
+    assert np.allclose(got, want, rtol=1e-12, atol=1e-14)
+    assert got.max() <= 10.0
+
+
+def test_accept_oracle_semantics(orc):
+    err = np.array([[1.0, 5.0], [0.5, np.nan], [1.0, 4.8], [9.9, 10.0]])
+    off, idx = orc.accept(err, 0, 4.8)
+    assert off.tolist() == [0, 3, 4]
+    assert idx.tolist() == [2, 1, 3, 3]   # ties by index; 1-based; NaN never accepted
+    off, idx = orc.accept(err, 1, 0.5)   # top ceil(0.5*4) = 2 per gene
+    assert off.tolist() == [0, 2, 4]
+    assert idx.tolist() == [2, 1, 3, 1]
+
+
+def test_capture_moment_transform_quirk(orc):
+    """downsample (model.jl:221-239) uses the sample variance of beta next to
+    the population second moment; the exact expectation of the empirical
+    moments differs from it by Var_pop(beta)/(n-1) * sigma^2."""
+    cfg = make_config("hour")
+    cells = synthetic_cells(seed=1)
+    bm = beta_moments(cells, 5)
+    th = np.log10([0.5, 1.0, 20.0, 0.1, 0.7])
+    iv = np.array([0, 0.5, 0, 0, 0, 0, 0, 0, 0.0])
+    a = orc.moment_model(cfg, 1, th, iv, beta_mom=bm, age_dist=cells.age_dist)["stats"]
+    b = orc.moment_model(cfg, 1, th, iv, beta_mom=bm, age_dist=cells.age_dist, exact_capture=True)["stats"]
+    assert np.allclose(a[:5], b[:5], rtol=1e-14)  # means agree exactly
+    assert np.max(np.abs(a - b) / np.abs(b)) < 2e-2
