@@ -188,6 +188,51 @@ class Context:
 
 
 # ---------------------------------------------------------------------------
+# Several GPUs: particles are independent (scripts/abc_simulation.jl:88-97), so
+# a run shards them by index with no data exchange; each shard keeps its
+# random streams through particle_offset.  Acceptance needs one host-side
+# merge per gene.
+# ---------------------------------------------------------------------------
+def shard_range(n_particles: int, rank: int, world: int) -> tuple[int, int]:
+    """[start, stop) of the particles simulated by `rank` of `world`."""
+    base, rem = divmod(n_particles, world)
+    start = rank * base + min(rank, rem)
+    return start, start + base + (1 if rank < rem else 0)
+
+
+def merge_accept_lists(parts, mode: int, eps_or_q: float, n_particles: int):
+    """Merge per-shard acceptance results into the single-run result.
+
+    parts: per shard (offsets[G+1], global 1-based indices, errors), each gene's
+    list sorted by (err, index) -- what Context.select returns with the shard's
+    start added to the indices.  mode 0 (err <= eps): concatenate and re-sort.
+    mode 1 (top ceil(q P)): every member of the global top k is in its shard's
+    top k, so each shard selects with the global k (q_local = k / P_shard) and
+    the merge keeps the k smallest (err, index) pairs."""
+    G = parts[0][0].shape[0] - 1
+    k = int(np.ceil(eps_or_q * n_particles)) if mode == 1 else None
+    offs = [0]
+    idx_out, err_out = [], []
+    for g in range(G):
+        e = np.concatenate([p[2][p[0][g]:p[0][g + 1]] for p in parts])
+        i = np.concatenate([p[1][p[0][g]:p[0][g + 1]] for p in parts])
+        order = np.lexsort((i, e))
+        if k is not None:
+            order = order[:k]
+        idx_out.append(i[order])
+        err_out.append(e[order])
+        offs.append(offs[-1] + order.shape[0])
+    return (np.asarray(offs, np.int64), np.concatenate(idx_out) if idx_out else np.zeros(0, np.int64),
+            np.concatenate(err_out) if err_out else np.zeros(0))
+
+
+def local_select_q(q: float, n_particles: int, n_shard: int) -> float:
+    """q for a shard's local top-q so that it keeps the global k = ceil(q P)."""
+    k = int(np.ceil(q * n_particles))
+    return min(1.0, k / max(n_shard, 1))
+
+
+# ---------------------------------------------------------------------------
 # Reference-named entry points (same argument meaning; batched over particles)
 # ---------------------------------------------------------------------------
 def fix_params(ctx: Context, model: int, n: int, seed: int, prior: AbcPrior, offset: int = 0) -> np.ndarray:

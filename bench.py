@@ -315,6 +315,8 @@ def main():
     stats_gbs = stats_bytes / (phase[2] / 1e3) / 1e9
     cpu = None
     try:
+        if args.cpu_seconds <= 0:
+            raise RuntimeError("CPU baseline skipped (--cpu-seconds 0)")
         rate, n, dt, ev = cpu_ssa_rate(cfg, cells, theta, models, args.cpu_seconds, os.cpu_count() or 1)
         cpu = {"value": rate, "unit": "events/s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"first {n} particles of the same batch (interleaved models) x {N_CELLS} cells, "
