@@ -137,6 +137,8 @@ def _declare(lib: C.CDLL) -> None:
         "abc_synchronize": (C.c_int, [vp]),
         "abc_simulate_batch": (C.c_int, [vp, i32p, dp, i64, i64, u64, i64, dp]),
         "abc_simulate_batch_device": (C.c_int, [vp, vp, vp, i64, i64, u64, i64, vp]),
+        "abc_simulate_noalloc": (C.c_int, [C.POINTER(AbcConfig), C.c_int, i64, i32p, i32p, dp, dp, vp, i64, u64,
+                                           i64, vp, vp]),
         "abc_simulate_cells": (C.c_int, [vp, C.c_int, dp, i64, u64, i64, i32p, i32p, i64p, u64p, dp]),
         "abc_last_counters": (C.c_int, [vp, i64p, i64p]),
         "abc_profile": (C.c_int, [vp, C.c_int]),
@@ -157,7 +159,7 @@ def _declare(lib: C.CDLL) -> None:
 ABI_SYMBOLS = [
     "abc_create", "abc_destroy", "abc_last_error", "abc_num_params", "abc_num_stats",
     "abc_stream", "abc_set_cells", "abc_sample_prior", "abc_simulate", "abc_simulate_device",
-    "abc_synchronize", "abc_simulate_batch", "abc_simulate_batch_device", "abc_simulate_cells", "abc_last_counters",
+    "abc_synchronize", "abc_simulate_batch", "abc_simulate_batch_device", "abc_simulate_noalloc", "abc_simulate_cells", "abc_last_counters",
     "abc_profile", "abc_profile_read", "abc_errors",
     "abc_errors_select", "abc_accept_fetch", "abc_select_counters",
 ]

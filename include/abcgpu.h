@@ -142,6 +142,27 @@ int abc_simulate_batch(abc_ctx* ctx, const int32_t* models, const double* theta,
 int abc_simulate_batch_device(abc_ctx* ctx, const int32_t* d_models, const double* d_theta, int64_t ld_theta,
                               int64_t n_particles, uint64_t seed, int64_t particle_offset, double* d_stats);
 
+/* abc_simulate_device without any device allocation by the library.  It has
+ * no counterpart in the reference.  For callers that may not call cudaMalloc
+ * while they run (a runtime that reserved all device memory in its own pool,
+ * or a latency-critical loop that must avoid the implicit synchronisation of
+ * cudaMalloc/cudaFree) and therefore cannot use abc_create.  Context-free:
+ * the cell table comes as host arrays (as for abc_set_cells), theta and the
+ * statistics are DEVICE pointers, and the work runs on the caller's stream
+ * (cudaStream_t as void*); the call waits for it to finish.  All scratch
+ * (particle records, per-cell counts, work counter, status word, sorted cell
+ * table) lives in one fixed 64 MiB device array owned by the library and held
+ * by every GPU that loads it until exit; particles x cells x 8 bytes plus
+ * about 500 bytes per particle must fit, else ABC_ERR_INVALID (e.g. up to
+ * ~4,000 particles with 2,000 cells).  The first call on a device looks up
+ * the array's device address (cudaGetSymbolAddress) and should come before
+ * any stream capture.  Calls share the array: calls that overlap on the GPU
+ * race, so serialise them. */
+int abc_simulate_noalloc(const abc_config* cfg, int model, int64_t n_cells, const int32_t* cell_cond,
+                         const int32_t* cell_age, const double* cell_beta, const double* age_dist,
+                         const double* d_theta, int64_t n_particles, uint64_t seed, int64_t particle_offset,
+                         double* d_stats, void* stream);
+
 /* Per-cell view of abc_simulate for parity tests: raw counts (u, l) at the
  * observation time, captured counts, fired-event counts and event-sequence
  * hashes, each P x C in the caller's cell order (any pointer may be NULL). */
