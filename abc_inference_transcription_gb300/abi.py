@@ -142,6 +142,8 @@ def _declare(lib: C.CDLL) -> None:
         "abc_simulate_cells": (C.c_int, [vp, C.c_int, dp, i64, u64, i64, i32p, i32p, i64p, u64p, dp]),
         "abc_last_counters": (C.c_int, [vp, i64p, i64p]),
         "abc_profile": (C.c_int, [vp, C.c_int]),
+        "abc_autotune": (C.c_int, [vp, C.c_int, dp, i64, u64, dp, C.POINTER(C.c_int)]),
+        "abc_set_variant": (C.c_int, [vp, C.c_int]),
         "abc_profile_read": (C.c_int, [vp, dp]),
         "abc_errors": (C.c_int, [vp, dp, dp, i64, C.c_int, C.c_int, i32p, dp, i64, dp]),
         "abc_errors_select": (C.c_int, [vp, dp, dp, i64, C.c_int, C.c_int, i32p, dp, i64, C.c_int,
@@ -149,6 +151,24 @@ def _declare(lib: C.CDLL) -> None:
         "abc_accept_fetch": (C.c_int, [vp, i64p, i64p, dp]),
         "abc_select_counters": (C.c_int, [vp, i64p, i64p]),
     }
+    sp = vp
+    sig.update({
+        "abc_surrogate_create": (C.c_int, [C.POINTER(vp), C.c_int, C.c_int, C.c_int, u64]),
+        "abc_surrogate_destroy": (C.c_int, [sp]),
+        "abc_surrogate_last_error": (C.c_char_p, [sp]),
+        "abc_surrogate_num_params": (C.c_int, [sp]),
+        "abc_surrogate_train": (C.c_int, [sp, dp, dp, i64, C.c_int, C.c_int, C.c_double, dp]),
+        "abc_surrogate_gradients": (C.c_int, [sp, dp, dp, i64, dp, C.POINTER(C.c_float)]),
+        "abc_surrogate_get_params": (C.c_int, [sp, C.POINTER(C.c_float)]),
+        "abc_surrogate_set_params": (C.c_int, [sp, C.POINTER(C.c_float)]),
+        "abc_surrogate_get_norm": (C.c_int, [sp, dp, dp, dp, dp]),
+        "abc_surrogate_set_norm": (C.c_int, [sp, dp, dp, dp, dp]),
+        "abc_surrogate_predict": (C.c_int, [sp, dp, i64, dp, dp, dp]),
+        "abc_surrogate_predict_device": (C.c_int, [sp, vp, C.c_int, i64, vp, vp, vp]),
+        "abc_surrogate_compact_device": (C.c_int, [sp, vp, vp, C.c_int, i64, vp, vp, i64p]),
+        "abc_surrogate_screen_device": (C.c_int, [sp, vp, C.c_int, i64, dp, dp, i64, dp, C.c_double, C.c_double, vp,
+                                                  i64p, dp]),
+    })
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
         fn.restype = res
@@ -160,6 +180,10 @@ ABI_SYMBOLS = [
     "abc_create", "abc_destroy", "abc_last_error", "abc_num_params", "abc_num_stats",
     "abc_stream", "abc_set_cells", "abc_sample_prior", "abc_simulate", "abc_simulate_device",
     "abc_synchronize", "abc_simulate_batch", "abc_simulate_batch_device", "abc_simulate_noalloc", "abc_simulate_cells", "abc_last_counters",
-    "abc_profile", "abc_profile_read", "abc_errors",
+    "abc_profile", "abc_profile_read", "abc_autotune", "abc_set_variant", "abc_errors",
     "abc_errors_select", "abc_accept_fetch", "abc_select_counters",
+    "abc_surrogate_create", "abc_surrogate_destroy", "abc_surrogate_last_error", "abc_surrogate_num_params",
+    "abc_surrogate_train", "abc_surrogate_gradients", "abc_surrogate_get_params", "abc_surrogate_set_params",
+    "abc_surrogate_get_norm", "abc_surrogate_set_norm", "abc_surrogate_predict", "abc_surrogate_predict_device",
+    "abc_surrogate_screen_device", "abc_surrogate_compact_device",
 ]

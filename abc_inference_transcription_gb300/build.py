@@ -29,6 +29,8 @@ UNITS = {
     "distance_fp64.cu": ["-fmad=false"],
     "distance_fp32.cu": [],
     "noalloc.cu": [],
+    "mlp.cu": [],
+    "surrogate.cu": [],
 }
 
 

@@ -61,6 +61,7 @@ struct abc_ctx {
   // simulation workspace
   DBuf<double> d_theta, d_stats;
   DBuf<int32_t> d_models;
+  DBuf<uint32_t> d_order, d_ohist;  // work order (heaviest particles first) and its counting-sort scratch
   DBuf<PRec> d_rec;
   DBuf<PRecF> d_recf;
   DBuf<int2> d_counts, d_captured;
@@ -69,6 +70,7 @@ struct abc_ctx {
   DBuf<unsigned long long> d_misc;  // [0] work counter, [1] events, [2] rejections
   DBuf<int> d_status;
   int64_t last_events = 0, last_rej = 0;
+  int variant = 0;  // production SSA kernel variant chosen by abc_autotune
   // per-phase device timing (abc_profile): 4 events per chunk
   bool prof = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -192,7 +194,7 @@ int abc_destroy(abc_ctx* c) {
   cudaStreamSynchronize(c->stream);
   c->d_cond.release(); c->d_age.release(); c->d_gstart.release(); c->d_id.release();
   c->d_beta.release(); c->d_age_dist.release(); c->d_theta.release(); c->d_stats.release();
-  c->d_models.release(); c->d_rec.release(); c->d_recf.release(); c->d_counts.release(); c->d_captured.release();
+  c->d_models.release(); c->d_order.release(); c->d_ohist.release(); c->d_rec.release(); c->d_recf.release(); c->d_counts.release(); c->d_captured.release();
   c->d_events.release(); c->d_hash.release(); c->d_misc.release(); c->d_status.release();
   c->d_data.release(); c->d_se.release(); c->d_sel_stats.release(); c->d_e64.release(); c->d_se64.release();
   c->d_out_err.release(); c->d_sw.release(); c->d_dw.release(); c->d_s32.release(); c->d_X.release();
@@ -335,6 +337,8 @@ static int enqueue_simulate(abc_ctx* c, int model, const int32_t* d_models, cons
   chunk = std::min<int64_t>(chunk, std::max<int64_t>(P, 1));
   CK(c->d_rec.ensure(chunk));
   CK(c->d_recf.ensure(chunk));
+  CK(c->d_order.ensure(chunk));
+  CK(c->d_ohist.ensure(128));
   CK(c->d_counts.ensure((size_t)chunk * C));
   if (want_cells) {
     CK(c->d_captured.ensure((size_t)chunk * C));
@@ -345,7 +349,7 @@ static int enqueue_simulate(abc_ctx* c, int model, const int32_t* d_models, cons
   CK(cudaMemsetAsync(c->d_status.p, 0, sizeof(int), c->stream));
   c->ev_used = 0;
   const bool fp64 = c->cfg.precision == ABC_FP64;
-  const int bps = fp64 ? ssa_blocks_per_sm_fp64() : ssa_blocks_per_sm_fp32();
+  const int bps = fp64 ? ssa_blocks_per_sm_fp64() : ssa_blocks_per_sm_fp32(c->variant);
   for (int64_t p0 = 0; p0 < P; p0 += chunk) {
     const int64_t n = std::min(chunk, P - p0);
     SetupArgs sa;
@@ -361,6 +365,7 @@ static int enqueue_simulate(abc_ctx* c, int model, const int32_t* d_models, cons
     sa.status = c->d_status.p;
     CK(prof_mark(c));
     CK(launch_setup(sa, c->stream));
+    CK(launch_work_order(c->d_rec.p, n, c->d_ohist.p, c->d_order.p, c->stream));
     CK(prof_mark(c));
     CK(cudaMemsetAsync(c->d_misc.p, 0, sizeof(unsigned long long), c->stream));
     SsaArgs ss;
@@ -370,7 +375,7 @@ static int enqueue_simulate(abc_ctx* c, int model, const int32_t* d_models, cons
     ss.cell_cond = c->d_cond.p;
     ss.cell_age = c->d_age.p;
     ss.cell_id = c->d_id.p;
-    ss.order = nullptr;
+    ss.order = c->d_order.p;
     ss.n_cells = C;
     ss.n_items = n * C;
     ss.p_offset = p_offset + p0;
@@ -386,7 +391,7 @@ static int enqueue_simulate(abc_ctx* c, int model, const int32_t* d_models, cons
     int64_t grid = (int64_t)std::max(1, bps) * c->sms;
     grid = std::min<int64_t>(grid, (warps_needed + 3) / 4);
     grid = std::max<int64_t>(grid, 1);
-    CK(fp64 ? launch_ssa_fp64(ss, (int)grid, c->stream) : launch_ssa_fp32(ss, (int)grid, c->stream));
+    CK(fp64 ? launch_ssa_fp64(ss, (int)grid, c->stream) : launch_ssa_fp32(ss, (int)grid, c->stream, c->variant));
     CK(prof_mark(c));
     StatsArgs st;
     st.cfg = sa.cfg;
@@ -546,6 +551,53 @@ int abc_simulate_cells(abc_ctx* c, int model, const double* theta, int64_t P, ui
       if (hash_out) hash_out[dst] = hs[src];
     }
   return st;
+}
+
+int abc_autotune(abc_ctx* c, int model, const double* theta, int64_t P, uint64_t seed, double* ms_out,
+                 int* chosen) {
+  if (!c) return ABC_ERR_INVALID;
+  int st = check_sim_args(c, model, P, 0);
+  if (st) return st;
+  if (P < 1 || !theta) return fail(c, ABC_ERR_INVALID, "abc_autotune: needs a theta sample");
+  if (c->cfg.precision != ABC_FP32) {
+    if (chosen) *chosen = 0;
+    return ABC_OK;  // the FP64 oracle mode has a single kernel
+  }
+  const int npar = npar_of(&c->cfg, model);
+  const int K = ABC_NSTATS(c->cfg.n_ages, c->cfg.n_conds);
+  CK(c->d_theta.ensure((size_t)P * npar));
+  CK(c->d_stats.ensure((size_t)P * K));
+  CK(cudaMemcpyAsync(c->d_theta.p, theta, sizeof(double) * P * npar, cudaMemcpyHostToDevice, c->stream));
+  const bool prof = c->prof;
+  c->prof = true;
+  double best = 1e300;
+  int best_v = 0;
+  for (int v = 0; v < kSsaVariants; ++v) {
+    c->variant = v;
+    st = enqueue_simulate(c, model, nullptr, c->d_theta.p, npar, P, seed, 0, c->d_stats.p, false);
+    if (!st) st = finish_status(c);
+    if (st) {
+      c->prof = prof;
+      c->variant = 0;
+      return st;
+    }
+    const double ms = c->phase_ms[1];
+    if (ms_out) ms_out[v] = ms;
+    if (ms < best) {
+      best = ms;
+      best_v = v;
+    }
+  }
+  c->prof = prof;
+  c->variant = best_v;
+  if (chosen) *chosen = best_v;
+  return ABC_OK;
+}
+
+int abc_set_variant(abc_ctx* c, int variant) {
+  if (!c || variant < 0 || variant >= kSsaVariants) return ABC_ERR_INVALID;
+  c->variant = variant;
+  return ABC_OK;
 }
 
 int abc_profile(abc_ctx* c, int enable) {

@@ -166,4 +166,97 @@ cudaError_t launch_dist_threshold(const float* esub, int64_t n_sub, int64_t G, i
 
 float dist_bound(float e, int K) { return dist_bound_f(e, K); }
 
+// Surrogate screen: expected error of particle p for gene g under the
+// predicted statistics N(mu_pk, var_pk),
+//   E[err_pg] = sum_k w_gk ((d_gk - mu_pk)^2 + var_pk) / K,
+// keep[p] = 1 when E[err_pg] <= X[g] for some gene (X = threshold + margin).
+// Same 128 x 128 tiling as dist_fast_kernel; three FMAs per (p, g, k).
+__global__ void __launch_bounds__(256) dist_screen_kernel(const float* __restrict__ mu,
+                                                          const float* __restrict__ var,
+                                                          const float* __restrict__ sw,
+                                                          const float* __restrict__ dw, int64_t P, int64_t G,
+                                                          int K, const float* __restrict__ X, uint8_t* keep,
+                                                          float* err_out) {
+  __shared__ float sm[kDistKc][kDistTile];
+  __shared__ float sv[kDistKc][kDistTile];
+  __shared__ float sa[kDistKc][kDistTile];
+  __shared__ float sd[kDistKc][kDistTile];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int64_t g0 = (int64_t)blockIdx.x * kDistTile;
+  const int64_t p0 = (int64_t)blockIdx.y * kDistTile;
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+  for (int k0 = 0; k0 < K; k0 += kDistKc) {
+    for (int idx = threadIdx.x; idx < kDistKc * kDistTile; idx += 256) {
+      const int r = idx / kDistKc, kk = idx - (idx / kDistKc) * kDistKc;
+      const int k = k0 + kk;
+      const int64_t p = p0 + r, g = g0 + r;
+      float m = 0.0f, v = 0.0f, a = 0.0f, d = 0.0f;
+      if (p < P && k < K) {
+        m = mu[p * K + k];
+        v = var[p * K + k];
+      }
+      if (g < G && k < K) {
+        a = sw[g * K + k];
+        d = dw[g * K + k];
+      }
+      sm[kk][r] = m;
+      sv[kk][r] = v;
+      sa[kk][r] = a;
+      sd[kk][r] = d;
+    }
+    __syncthreads();
+    const int kc = (K - k0) < kDistKc ? (K - k0) : kDistKc;
+#pragma unroll 2
+    for (int kk = 0; kk < kc; ++kk) {
+      float m[8], v[8], a[8], d[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        m[i] = sm[kk][ty + 16 * i];
+        v[i] = sv[kk][ty + 16 * i];
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        a[j] = sa[kk][tx + 16 * j];
+        d[j] = sd[kk][tx + 16 * j];
+      }
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const float t = fmaf(-a[j], m[i], d[j]);
+          acc[i][j] = fmaf(t, t, fmaf(a[j] * a[j], v[i], acc[i][j]));
+        }
+    }
+    __syncthreads();
+  }
+  const float invK = 1.0f / (float)K;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int64_t p = p0 + ty + 16 * i;
+    if (p >= P) continue;
+    bool any = false;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int64_t g = g0 + tx + 16 * j;
+      if (g >= G) continue;
+      const float e = acc[i][j] * invK;
+      if (err_out) err_out[p * G + g] = e;
+      any = any || (e <= X[g]);
+    }
+    if (any) keep[p] = 1;
+  }
+}
+
+cudaError_t launch_dist_screen(const float* mu, const float* var, const float* sw, const float* dw, int64_t P,
+                               int64_t G, int K, const float* X, uint8_t* keep, float* err_out, cudaStream_t s) {
+  if (P <= 0 || G <= 0) return cudaSuccess;
+  dim3 grid((unsigned)((G + kDistTile - 1) / kDistTile), (unsigned)((P + kDistTile - 1) / kDistTile));
+  dist_screen_kernel<<<grid, 256, 0, s>>>(mu, var, sw, dw, P, G, K, X, keep, err_out);
+  return cudaGetLastError();
+}
+
 }  // namespace abc

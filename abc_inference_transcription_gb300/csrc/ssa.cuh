@@ -55,6 +55,7 @@ struct SsaArgs {
   unsigned long long* totals;  // [0] fired events, [1] thinning rejections
   int* status;
   int want_hash;
+  uint32_t rk[20];           // Philox round keys (seed + r * Weyl), filled by the FP32 launcher
 };
 
 struct Traj {

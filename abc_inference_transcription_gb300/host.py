@@ -129,6 +129,17 @@ class Context:
             ptr(out["events"], C.c_int64), ptr(out["hash"], C.c_uint64), ptr(out["stats"])))
         return out
 
+    def autotune(self, model: int, theta: np.ndarray, seed: int = 1) -> tuple[int, list[float]]:
+        """Time the production kernel variants on `theta` and keep the fastest."""
+        th = np.ascontiguousarray(theta, np.float64)
+        ms = np.zeros(2)
+        chosen = C.c_int()
+        self._check(self.lib.abc_autotune(self.h, model, ptr(th), th.shape[0], seed, ptr(ms), C.byref(chosen)))
+        return chosen.value, ms.tolist()
+
+    def set_variant(self, variant: int) -> None:
+        self._check(self.lib.abc_set_variant(self.h, variant))
+
     def profile(self, enable: bool = True) -> None:
         self._check(self.lib.abc_profile(self.h, int(enable)))
 

@@ -147,10 +147,10 @@ def cpu_ssa_rate(cfg, cells, theta, models, seconds: float, threads: int):
     P = theta.shape[0]
     per_model = P // 5
     order = np.concatenate([[m * per_model + i for m in range(5)] for i in range(per_model)])
-    n = 5
-    while True:
-        sel = order[:n]
-        ev = 0
+    # increments of 10 particles (2 per model) until the time budget is spent
+    n, ev, dt = 0, 0, 0.0
+    while n < P and dt < seconds:
+        sel = order[n:n + 10]
         t0 = time.perf_counter()
         for m in range(1, 6):
             rows = sel[models[sel] == m]
@@ -159,10 +159,9 @@ def cpu_ssa_rate(cfg, cells, theta, models, seconds: float, threads: int):
             npar = 5 if m <= 2 else 9
             out = orc.simulate(cfg64, cells, m, theta[rows, :npar], seed=77, n_threads=threads, want_cells=True)
             ev += int(out["events"].sum())
-        dt = time.perf_counter() - t0
-        if dt >= seconds / 3 or n >= P:
-            return ev / dt, n, dt, ev
-        n = min(P, max(n + 5, int(n * max(2.0, seconds / 3 / max(dt, 1e-3)))))
+        dt += time.perf_counter() - t0
+        n += sel.shape[0]
+    return ev / dt, n, dt, ev
 
 
 def run_reference(args):
@@ -240,6 +239,9 @@ def main():
     d_models = torch.from_numpy(models).cuda()
     d_stats = torch.empty((P_rank, K), dtype=torch.float64, device="cuda")
     torch.cuda.synchronize()
+    # autotuner: kernel variant timed on a sample of the batch (model 1 rows)
+    n_tune = min(args.per_model, 1000)
+    variant, tune_ms = ctx.autotune(1, theta[:n_tune, :5], seed=7)
     ctx.profile(True)
 
     def step(seed):
@@ -344,7 +346,8 @@ def main():
                            "traffic": None, "peak_source": peak_src},
         "cpu_baseline": cpu,
         "e2e": e2e,
-        "gpu_launches": 3 * args.steps,
+        "gpu_launches": 5 * args.steps,  # setup, 2 work-order kernels, SSA, capture+statistics
+        "autotune": {"chosen_variant": variant, "ssa_ms_per_variant": tune_ms, "sample": f"{n_tune} particles"},
         "clocks": clocks,
     }
     print(json.dumps(line))

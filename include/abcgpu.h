@@ -178,6 +178,13 @@ int abc_last_counters(const abc_ctx* ctx, int64_t* events, int64_t* rejections);
  * abc_profile_read returns, for the last synchronized simulate call, the
  * milliseconds spent in [setup, SSA, capture+statistics] kernels. */
 int abc_profile(abc_ctx* ctx, int enable);
+/* Autotuner (no reference counterpart; the reference tunes nothing): times the
+ * production SSA kernel variants (register allocation for 8 or 10 resident
+ * blocks per SM) on a sample of particles and keeps the fastest for this
+ * context.  ms_out: kernel milliseconds per variant (2 entries, may be NULL). */
+int abc_autotune(abc_ctx* ctx, int model, const double* theta, int64_t n_particles, uint64_t seed,
+                 double* ms_out, int* chosen);
+int abc_set_variant(abc_ctx* ctx, int variant);
 int abc_profile_read(const abc_ctx* ctx, double* ms_out);
 
 /* Error matrix, compute_trunc_errors / nlsqerror_part (scripts/compute_errors.jl:30-70):
@@ -200,6 +207,52 @@ int abc_errors_select(abc_ctx* ctx, const double* data, const double* se, int64_
 int abc_accept_fetch(abc_ctx* ctx, int64_t* gene_offsets, int64_t* particle_idx, double* err);
 /* Counters of the last selection: FP32 candidates rechecked in FP64. */
 int abc_select_counters(const abc_ctx* ctx, int64_t* candidates, int64_t* rechecked);
+
+/* ------------------------------------------------------------------------
+ * Learned pre-screen.  No reference counterpart: the reference simulates
+ * every prior draw.  An ensemble of MLPs (log-parameters -> means and
+ * log-variances of the statistics; 3 x 256 SiLU hidden layers; FP32 master
+ * weights, BF16 tensor-core GEMMs) is trained on the pipeline's own SSA output;
+ * the screen keeps a prior draw when its predicted expected error
+ * sum_k w (d - mu)^2 + w var, / K, is within a gene's threshold plus a
+ * calibrated margin for some gene, or when the ensemble disagrees.
+ * ------------------------------------------------------------------------ */
+typedef struct abc_surrogate abc_surrogate;
+int abc_surrogate_create(abc_surrogate** out, int in_dim, int n_stats, int ensemble, uint64_t seed);
+int abc_surrogate_destroy(abc_surrogate* s);
+const char* abc_surrogate_last_error(const abc_surrogate* s);
+int abc_surrogate_num_params(const abc_surrogate* s);
+/* theta: N x in_dim (log10 rates), stats: N x n_stats (non-finite entries are
+ * masked).  Fits the input/output standardisation on this data, then runs
+ * `epochs` passes of Adam (batch rows per step).  epoch_loss: mean Gaussian NLL. */
+int abc_surrogate_train(abc_surrogate* s, const double* theta, const double* stats, int64_t n, int epochs,
+                        int batch, double lr, double* epoch_loss);
+/* Loss per member and gradients (members x num_params floats) of one batch, no update. */
+int abc_surrogate_gradients(abc_surrogate* s, const double* theta, const double* stats, int64_t n,
+                            double* loss, float* grads);
+int abc_surrogate_get_params(abc_surrogate* s, float* params);
+int abc_surrogate_set_params(abc_surrogate* s, const float* params);
+int abc_surrogate_get_norm(abc_surrogate* s, double* xmean, double* xstd, double* ymean, double* ystd);
+int abc_surrogate_set_norm(abc_surrogate* s, const double* xmean, const double* xstd, const double* ymean,
+                           const double* ystd);
+/* Ensemble mean, total predictive variance and disagreement
+ * (max_k sqrt(ensemble variance / mean aleatoric variance)) per row. */
+int abc_surrogate_predict(abc_surrogate* s, const double* theta, int64_t n, double* mean, double* var,
+                          double* disagree);
+int abc_surrogate_predict_device(abc_surrogate* s, const double* d_theta, int ld_theta, int64_t n,
+                                 double* d_mean, double* d_var, double* d_disagree);
+/* d_keep[p] = 1 for the draws to simulate exactly; data, se: G x n_stats
+ * (host), thr: per-gene error threshold (host), margin added to it.
+ * err_out (host, n x G, optional, small n only): predicted expected errors. */
+int abc_surrogate_screen_device(abc_surrogate* s, const double* d_theta, int ld_theta, int64_t n,
+                                const double* data, const double* se, int64_t n_genes, const double* thr,
+                                double margin, double disagree_max, uint8_t* d_keep, int64_t* n_keep,
+                                double* err_out);
+/* Survivors of a screen in ascending order: rows with d_keep != 0 copied from
+ * d_theta (row stride ld_theta) to d_theta_out and their indices to d_idx_out
+ * (either output may be NULL); *n_out = number of survivors. */
+int abc_surrogate_compact_device(abc_surrogate* s, const uint8_t* d_keep, const double* d_theta, int ld_theta,
+                                 int64_t n, double* d_theta_out, int64_t* d_idx_out, int64_t* n_out);
 
 #ifdef __cplusplus
 }

@@ -218,3 +218,34 @@ def test_capture_moment_transform_quirk(orc):
     b = orc.moment_model(cfg, 1, th, iv, beta_mom=bm, age_dist=cells.age_dist, exact_capture=True)["stats"]
     assert np.allclose(a[:5], b[:5], rtol=1e-14)  # means agree exactly
     assert np.max(np.abs(a - b) / np.abs(b)) < 2e-2
+
+
+def test_mlp_reference_gradients_finite_differences():
+    """The FP64 reference network (without BF16 rounding) against central
+    finite differences on random coordinates of every parameter block."""
+    from oracle import mlp_ref
+    rng = np.random.default_rng(2)
+    in_dim, K, N = 4, 7, 12
+    d = mlp_ref.dims(in_dim, K)
+    p = rng.normal(0, 0.08, d["n"])
+    th = rng.normal(0, 1, (N, in_dim))
+    st = rng.normal(0, 1, (N, K))
+    args = (np.zeros(in_dim), np.ones(in_dim), np.zeros(K), np.ones(K))
+    loss, g = mlp_ref.loss_and_grads(p, d, th, st, *args, rounding=False)
+    for name in ("w1", "b1", "w2", "b2", "w3", "b3", "w4", "b4"):
+        a, b = d[name]
+        if name == "w1":
+            idx = rng.integers(0, in_dim, 4) * 256 + rng.integers(0, 256, 4) + a
+        elif name == "w4" or name == "b4":
+            cols = rng.integers(0, 2 * K, 4)
+            idx = (rng.integers(0, 256, 4) * d["out_pad"] + cols + a) if name == "w4" else cols + a
+        else:
+            idx = rng.integers(a, b, 4)
+        for i in idx:
+            h = 1e-6
+            pp, pm = p.copy(), p.copy()
+            pp[i] += h
+            pm[i] -= h
+            fd = (mlp_ref.loss_and_grads(pp, d, th, st, *args, rounding=False)[0] -
+                  mlp_ref.loss_and_grads(pm, d, th, st, *args, rounding=False)[0]) / (2 * h)
+            assert abs(fd - g[i]) <= 1e-6 + 1e-4 * abs(fd), (name, i, fd, g[i])

@@ -1,0 +1,110 @@
+"""Surrogate pre-screen: gradients of the hand-written forward/backward kernels
+against the FP64 reference network (oracle/mlp_ref.py, BF16 rounding at the
+same points as the GPU GEMM inputs), and what the trained network gains in
+the ABC loop: fraction of prior draws that still need the exact SSA at a
+calibrated false-rejection rate."""
+import numpy as np
+import pytest
+
+from abc_inference_transcription_gb300 import abi
+from abc_inference_transcription_gb300.config import make_config, reference_prior, synthetic_cells
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def mods(built):
+    from abc_inference_transcription_gb300 import surrogate as S
+    from abc_inference_transcription_gb300.host import Context
+    return S, Context
+
+
+def test_gradients_match_fp64_reference(mods):
+    S, _ = mods
+    from oracle import mlp_ref
+    rng = np.random.default_rng(3)
+    in_dim, K, N = 5, 53, 96
+    theta = rng.uniform(-3, 3, (N, in_dim))
+    stats = rng.normal(2.0, 1.5, (N, K))
+    stats[3, 7] = np.nan   # masked target
+    with S.Surrogate(in_dim, K, ensemble=2, seed=11) as sg:
+        p = sg.params()
+        # perturb biases and output layer so every gradient block is non-trivial
+        p = p + rng.normal(0, 0.02, p.shape).astype(np.float32)
+        sg.set_params(p)
+        xm, xs = np.zeros(in_dim), np.full(in_dim, 1.7)
+        ym, ys = np.full(K, 2.0), np.full(K, 1.5)
+        sg.set_norm(xm, xs, ym, ys)
+        loss, grads = sg.gradients(theta, stats)
+        d = mlp_ref.dims(in_dim, K)
+        for e in range(2):
+            rl, rg = mlp_ref.loss_and_grads(p[e], d, theta, stats, xm, xs, ym, ys)
+            assert abs(loss[e] - rl) <= 2e-4 * abs(rl) + 1e-6
+            for name in ("w1", "b1", "w2", "b2", "w3", "b3", "w4", "b4"):
+                a, b = d[name]
+                gg, rr = grads[e, a:b].astype(np.float64), rg[a:b]
+                rel = np.linalg.norm(gg - rr) / max(np.linalg.norm(rr), 1e-12)
+                assert rel < 2e-2, (e, name, rel)
+
+
+def _exact(ctx, theta, seed):
+    return ctx.simulate(1, theta, seed=seed)
+
+
+def test_training_reduces_loss_and_predicts_held_out(mods):
+    S, Context = mods
+    cfg = make_config("hour", precision=abi.FP32)
+    cells = synthetic_cells(seed=4)
+    with Context(cfg, cells) as ctx:
+        th = ctx.sample_prior(1, 12000, 5, reference_prior())
+        th[:, 2] = np.minimum(th[:, 2], 2.0)
+        st = _exact(ctx, th, 1)
+    good = np.isfinite(st).all(axis=1)
+    th, st = th[good], st[good]
+    n_tr = int(0.9 * th.shape[0])
+    with S.Surrogate(5, 53, ensemble=4, seed=2) as sg:
+        loss = sg.train(th[:n_tr], st[:n_tr], epochs=25, batch=1024, lr=2e-3)
+        assert loss[-1] < loss[0] - 0.5, loss
+        mean, var, dis = sg.predict(th[n_tr:])
+        ym, ys = sg.norm()[2:]
+        z = (mean - st[n_tr:]) / ys
+        # held-out mean absolute standardised error well below the prior spread (1.0)
+        assert np.median(np.abs(z)) < 0.35, np.median(np.abs(z))
+        assert np.all(var > 0) and np.all(np.isfinite(dis))
+
+
+def test_screen_gain_at_calibrated_false_rejection(mods):
+    S, Context = mods
+    torch = pytest.importorskip("torch")
+    cfg = make_config("hour", precision=abi.FP32)
+    cells = synthetic_cells(seed=4)
+    rng = np.random.default_rng(8)
+    with Context(cfg, cells) as ctx:
+        th_tr = ctx.sample_prior(1, 16000, 21, reference_prior())
+        st_tr = _exact(ctx, th_tr, 2)
+        th_ex = ctx.sample_prior(1, 12000, 22, reference_prior(), offset=100000)
+        st_ex = _exact(ctx, th_ex, 3)
+        # 6 genes: statistics of random particles with 5 % noise; se ~ 10 % of the statistic
+        G = 6
+        src = np.flatnonzero(np.isfinite(st_ex).all(axis=1))[:G]
+        data = st_ex[src] * rng.lognormal(0, 0.05, (G, 53))
+        se = 0.1 * np.abs(data) * rng.lognormal(0, 0.5, (G, 53))
+        err = ctx.errors(data, se, st_ex)
+    ok = np.isfinite(st_tr).all(axis=1)
+    with S.Surrogate(5, 53, ensemble=4, seed=5) as sg:
+        sg.train(th_tr[ok], st_tr[ok], epochs=30, batch=1024, lr=2e-3)
+        thr = np.quantile(np.where(np.isfinite(err), err, 10.0), 0.02, axis=0)
+        half = th_ex.shape[0] // 2
+        d_th = torch.from_numpy(np.ascontiguousarray(th_ex)).cuda()
+        d_keep = torch.zeros(th_ex.shape[0], dtype=torch.uint8, device="cuda")
+        pred = np.zeros((half, G))
+        sg.screen_device(d_th.data_ptr(), 5, half, data, se, thr, 0.0, 1e30, d_keep.data_ptr(), err_out=pred)
+        margin = S.calibrate_margin(pred, err[:half], thr, 0.99)
+        n_keep = sg.screen_device(d_th[half:].data_ptr(), 5, th_ex.shape[0] - half, data, se, thr, margin, 3.0,
+                                  d_keep[half:].data_ptr())
+        keep = d_keep[half:].cpu().numpy()
+    frr, n_acc = S.false_rejection_rate(keep, err[half:], thr)
+    frac = n_keep / (th_ex.shape[0] - half)
+    assert n_acc > 50
+    assert frr <= 0.05, (frr, n_acc)
+    assert frac < 0.5, frac   # >= 2x fewer exact simulations per accepted particle
