@@ -148,6 +148,9 @@ def _declare(lib: C.CDLL) -> None:
         "abc_errors": (C.c_int, [vp, dp, dp, i64, C.c_int, C.c_int, i32p, dp, i64, dp]),
         "abc_errors_select": (C.c_int, [vp, dp, dp, i64, C.c_int, C.c_int, i32p, dp, i64, C.c_int,
                                         C.c_double, i64p]),
+        "abc_errors_select_thr": (C.c_int, [vp, dp, dp, i64, C.c_int, C.c_int, i32p, dp, i64, dp, i64p]),
+        "abc_errors_select_device": (C.c_int, [vp, dp, dp, i64, C.c_int, C.c_int, i32p, vp, i64, C.c_int,
+                                               C.c_double, dp, i64p]),
         "abc_accept_fetch": (C.c_int, [vp, i64p, i64p, dp]),
         "abc_select_counters": (C.c_int, [vp, i64p, i64p]),
     }
@@ -181,7 +184,8 @@ ABI_SYMBOLS = [
     "abc_stream", "abc_set_cells", "abc_sample_prior", "abc_simulate", "abc_simulate_device",
     "abc_synchronize", "abc_simulate_batch", "abc_simulate_batch_device", "abc_simulate_noalloc", "abc_simulate_cells", "abc_last_counters",
     "abc_profile", "abc_profile_read", "abc_autotune", "abc_set_variant", "abc_errors",
-    "abc_errors_select", "abc_accept_fetch", "abc_select_counters",
+    "abc_errors_select", "abc_errors_select_thr", "abc_errors_select_device", "abc_accept_fetch",
+    "abc_select_counters",
     "abc_surrogate_create", "abc_surrogate_destroy", "abc_surrogate_last_error", "abc_surrogate_num_params",
     "abc_surrogate_train", "abc_surrogate_gradients", "abc_surrogate_get_params", "abc_surrogate_set_params",
     "abc_surrogate_get_norm", "abc_surrogate_set_norm", "abc_surrogate_predict", "abc_surrogate_predict_device",

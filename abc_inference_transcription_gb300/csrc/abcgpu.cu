@@ -84,6 +84,7 @@ struct abc_ctx {
   DBuf<int64_t> d_gcount, d_goff, d_alen, d_aoff, d_out_idx;
   DBuf<unsigned long long> d_gcursor, d_ncand;
   DBuf<int> d_fail;
+  DBuf<double> d_thr;
   int64_t cand_cap = int64_t(1) << 22;
   int64_t sel_G = 0, sel_total = 0, sel_cands = 0, sel_rechecked = 0;
   bool sel_ready = false;
@@ -200,7 +201,7 @@ int abc_destroy(abc_ctx* c) {
   c->d_out_err.release(); c->d_sw.release(); c->d_dw.release(); c->d_s32.release(); c->d_X.release();
   c->d_esub.release(); c->d_cand.release(); c->d_sp.release(); c->d_gcount.release(); c->d_goff.release();
   c->d_alen.release(); c->d_aoff.release(); c->d_out_idx.release(); c->d_gcursor.release();
-  c->d_ncand.release(); c->d_fail.release();
+  c->d_ncand.release(); c->d_fail.release(); c->d_thr.release();
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   cudaStreamDestroy(c->stream);
   delete c;
@@ -624,7 +625,8 @@ int abc_last_counters(const abc_ctx* c, int64_t* events, int64_t* rejections) {
 // distance + acceptance
 // ---------------------------------------------------------------------------
 static int load_dist_inputs(abc_ctx* c, const double* data, const double* se, int64_t G, int K, int n_fam,
-                            const int32_t* fam, const double* stats, int64_t P, DistInputs& in) {
+                            const int32_t* fam, const double* stats, int64_t P, DistInputs& in,
+                            bool stats_on_device = false) {
   if (!data || !se || !stats || G <= 0 || P <= 0 || K <= 0)
     return fail(c, ABC_ERR_INVALID, "distance: bad arguments");
   if (P > (int64_t(1) << 31) - 1 || G > (int64_t(1) << 31) - 1)
@@ -648,13 +650,17 @@ static int load_dist_inputs(abc_ctx* c, const double* data, const double* se, in
   }
   CK(c->d_data.ensure((size_t)G * K));
   CK(c->d_se.ensure((size_t)G * K));
-  CK(c->d_sel_stats.ensure((size_t)P * K));
   CK(cudaMemcpyAsync(c->d_data.p, data, sizeof(double) * G * K, cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(c->d_se.p, se, sizeof(double) * G * K, cudaMemcpyHostToDevice, c->stream));
-  CK(cudaMemcpyAsync(c->d_sel_stats.p, stats, sizeof(double) * P * K, cudaMemcpyHostToDevice, c->stream));
   in.data = c->d_data.p;
   in.se = c->d_se.p;
-  in.stats = c->d_sel_stats.p;
+  if (stats_on_device) {
+    in.stats = stats;
+  } else {
+    CK(c->d_sel_stats.ensure((size_t)P * K));
+    CK(cudaMemcpyAsync(c->d_sel_stats.p, stats, sizeof(double) * P * K, cudaMemcpyHostToDevice, c->stream));
+    in.stats = c->d_sel_stats.p;
+  }
   return ABC_OK;
 }
 
@@ -694,17 +700,25 @@ static int candidate_pass(abc_ctx* c, const DistInputs& in, int64_t* n) {
   return fail(c, ABC_ERR_CAPACITY, "candidate buffer overflow");
 }
 
-int abc_errors_select(abc_ctx* c, const double* data, const double* se, int64_t G, int K, int n_fam,
-                      const int32_t* fam, const double* stats, int64_t P, int mode, double eps_or_q,
-                      int64_t* n_accepted_total) {
+// mode 0: err <= eps; mode 1: top ceil(q P) per gene; mode 2: err <= thr[g] per gene
+static int select_impl(abc_ctx* c, const double* data, const double* se, int64_t G, int K, int n_fam,
+                       const int32_t* fam, const double* stats, bool stats_on_device, int64_t P, int mode,
+                       double eps_or_q, const double* thr, int64_t* n_accepted_total) {
   if (!c) return ABC_ERR_INVALID;
   c->sel_ready = false;
-  if (mode != 0 && mode != 1) return fail(c, ABC_ERR_INVALID, "mode must be 0 (eps) or 1 (top-q)");
+  if (mode < 0 || mode > 2) return fail(c, ABC_ERR_INVALID, "mode must be 0 (eps), 1 (top-q) or 2 (per-gene thr)");
   if (mode == 1 && !(eps_or_q > 0.0 && eps_or_q <= 1.0)) return fail(c, ABC_ERR_INVALID, "q must be in (0, 1]");
   if (mode == 0 && eps_or_q != eps_or_q) return fail(c, ABC_ERR_INVALID, "eps is NaN");
+  if (mode == 2) {
+    if (!thr) return fail(c, ABC_ERR_INVALID, "mode 2 needs per-gene thresholds");
+    for (int64_t g = 0; g < G; ++g)
+      if (thr[g] != thr[g]) return fail(c, ABC_ERR_INVALID, "threshold is NaN");
+  }
   DistInputs in;
-  int st = load_dist_inputs(c, data, se, G, K, n_fam, fam, stats, P, in);
+  int st = load_dist_inputs(c, data, se, G, K, n_fam, fam, stats, P, in, stats_on_device);
   if (st) return st;
+  CK(c->d_thr.ensure((size_t)G));
+  if (mode == 2) CK(cudaMemcpyAsync(c->d_thr.p, thr, sizeof(double) * G, cudaMemcpyHostToDevice, c->stream));
   CK(c->d_sw.ensure((size_t)G * K));
   CK(c->d_dw.ensure((size_t)G * K));
   CK(c->d_s32.ensure((size_t)P * K));
@@ -719,18 +733,21 @@ int abc_errors_select(abc_ctx* c, const double* data, const double* se, int64_t 
   CK(launch_dist_prep(in, c->d_sw.p, c->d_dw.p, c->d_s32.p, c->stream));
   const int64_t kq = mode == 1 ? (int64_t)std::ceil(eps_or_q * (double)P) : 0;
   std::vector<float> hX((size_t)G);
-  if (mode == 0) {
-    float x;
-    if (eps_or_q >= 10.0) {
-      x = INFINITY;
-    } else if (eps_or_q < 0.0) {
-      x = -1.0f;
-    } else {
-      const float e = (float)eps_or_q;
-      x = e + 2.0f * dist_bound(e, K);
-      x = std::nextafter(x, INFINITY);
+  if (mode == 0 || mode == 2) {
+    for (int64_t g = 0; g < G; ++g) {
+      const double ev = mode == 0 ? eps_or_q : thr[g];
+      float x;
+      if (ev >= 10.0) {
+        x = INFINITY;
+      } else if (ev < 0.0) {
+        x = -1.0f;
+      } else {
+        const float e = (float)ev;
+        x = e + 2.0f * dist_bound(e, K);
+        x = std::nextafter(x, INFINITY);
+      }
+      hX[g] = x;
     }
-    std::fill(hX.begin(), hX.end(), x);
     CK(cudaMemcpyAsync(c->d_X.p, hX.data(), sizeof(float) * G, cudaMemcpyHostToDevice, c->stream));
   } else {
     // thresholds from a strided subsample
@@ -760,10 +777,11 @@ int abc_errors_select(abc_ctx* c, const double* data, const double* se, int64_t 
     CK(launch_dist_group_sort(c->d_cand.p, c->d_e64.p, ncand, G, c->d_gcount.p, c->d_goff.p, c->d_sp.p,
                               c->d_se64.p, c->d_gcursor.p, c->stream));
     CK(cudaMemsetAsync(c->d_fail.p, 0, sizeof(int) * G, c->stream));
-    CK(launch_dist_accept_len(c->d_goff.p, c->d_se64.p, G, mode, eps_or_q, kq, c->d_X.p, K, c->d_alen.p,
-                              c->d_fail.p, c->stream));
+    CK(launch_dist_accept_len(c->d_goff.p, c->d_se64.p, G, mode == 2 ? 0 : mode, eps_or_q,
+                              mode == 2 ? c->d_thr.p : nullptr, kq, c->d_X.p, K, c->d_alen.p, c->d_fail.p,
+                              c->stream));
     c->sel_rechecked += ncand;
-    if (mode == 0) break;
+    if (mode != 1) break;
     std::vector<int> hf((size_t)G);
     CK(cudaMemcpyAsync(hf.data(), c->d_fail.p, sizeof(int) * G, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -793,6 +811,25 @@ int abc_errors_select(abc_ctx* c, const double* data, const double* se, int64_t 
   c->sel_ready = true;
   if (n_accepted_total) *n_accepted_total = total;
   return ABC_OK;
+}
+
+int abc_errors_select(abc_ctx* c, const double* data, const double* se, int64_t G, int K, int n_fam,
+                      const int32_t* fam, const double* stats, int64_t P, int mode, double eps_or_q,
+                      int64_t* n_accepted_total) {
+  if (mode == 2) return fail(c, ABC_ERR_INVALID, "per-gene thresholds: use abc_errors_select_thr");
+  return select_impl(c, data, se, G, K, n_fam, fam, stats, false, P, mode, eps_or_q, nullptr, n_accepted_total);
+}
+
+int abc_errors_select_thr(abc_ctx* c, const double* data, const double* se, int64_t G, int K, int n_fam,
+                          const int32_t* fam, const double* stats, int64_t P, const double* thr,
+                          int64_t* n_accepted_total) {
+  return select_impl(c, data, se, G, K, n_fam, fam, stats, false, P, 2, 0.0, thr, n_accepted_total);
+}
+
+int abc_errors_select_device(abc_ctx* c, const double* data, const double* se, int64_t G, int K, int n_fam,
+                             const int32_t* fam, const double* d_stats, int64_t P, int mode, double eps_or_q,
+                             const double* thr, int64_t* n_accepted_total) {
+  return select_impl(c, data, se, G, K, n_fam, fam, d_stats, true, P, mode, eps_or_q, thr, n_accepted_total);
 }
 
 int abc_accept_fetch(abc_ctx* c, int64_t* gene_offsets, int64_t* particle_idx, double* err) {

@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(256) dist_screen_kernel(const float* __restric
     for (int j = 0; j < 8; ++j) {
       const int64_t g = g0 + tx + 16 * j;
       if (g >= G) continue;
-      const float e = acc[i][j] * invK;
+      const float e = acc[i][j] * invK;  // not clipped: far draws keep large expected errors
       if (err_out) err_out[p * G + g] = e;
       any = any || (e <= X[g]);
     }

@@ -197,10 +197,11 @@ cudaError_t launch_dist_group_sort(const Cand* cand, const double* e64, int64_t 
 // ---------------------------------------------------------------------------
 // accepted prefixes
 // ---------------------------------------------------------------------------
-__global__ void accept_len_kernel(const int64_t* goff, const double* se64, int64_t G, int mode, double eps,
-                                  int64_t k, const float* X, int K, int64_t* alen, int* fail) {
+__global__ void accept_len_kernel(const int64_t* goff, const double* se64, int64_t G, int mode, double eps_all,
+                                  const double* eps_g, int64_t k, const float* X, int K, int64_t* alen, int* fail) {
   const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= G) return;
+  const double eps = eps_g ? eps_g[g] : eps_all;
   const double* E = se64 + goff[g];
   const int64_t n = goff[g + 1] - goff[g];
   // number of finite (non-NaN) entries: NaN sorts last
@@ -237,9 +238,11 @@ __global__ void accept_len_kernel(const int64_t* goff, const double* se64, int64
 }
 
 cudaError_t launch_dist_accept_len(const int64_t* goff, const double* se64, int64_t G, int mode, double eps,
-                                   int64_t k, const float* X, int K, int64_t* alen, int* fail, cudaStream_t s) {
+                                   const double* eps_g, int64_t k, const float* X, int K, int64_t* alen, int* fail,
+                                   cudaStream_t s) {
   if (G <= 0) return cudaSuccess;
-  accept_len_kernel<<<(unsigned)((G + 127) / 128), 128, 0, s>>>(goff, se64, G, mode, eps, k, X, K, alen, fail);
+  accept_len_kernel<<<(unsigned)((G + 127) / 128), 128, 0, s>>>(goff, se64, G, mode, eps, eps_g, k, X, K, alen,
+                                                                fail);
   return cudaGetLastError();
 }
 

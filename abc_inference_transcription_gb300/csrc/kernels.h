@@ -84,7 +84,8 @@ cudaError_t launch_dist_group_sort(const Cand* cand, const double* e64, int64_t 
 // finite errors) and, in mode 1, a failure flag when the candidate threshold
 // X[g] could have excluded a member of the top k.
 cudaError_t launch_dist_accept_len(const int64_t* goff, const double* se64, int64_t G, int mode, double eps,
-                                   int64_t k, const float* X, int K, int64_t* alen, int* fail, cudaStream_t s);
+                                   const double* eps_g, int64_t k, const float* X, int K, int64_t* alen, int* fail,
+                                   cudaStream_t s);
 // compact the accepted prefixes: idx (1-based particle index + p_base) and err.
 cudaError_t launch_dist_compact(const int64_t* goff, const int32_t* sp, const double* se64, const int64_t* aoff,
                                 int64_t G, int64_t p_base, int64_t* idx, double* err, cudaStream_t s);

@@ -238,9 +238,12 @@ __global__ void mlp_adam_kernel(float* P, const float* G, float* m, float* v, __
 }
 
 // ensemble combination in standardised units -> caller units
+// Targets are learnt as z = (asinh(y / c) - m) / s (c = 0: z = (y - m) / s);
+// the predictive mean and variance map back through y = c sinh(m + s z)
+// (delta method for the variance).
 __global__ void mlp_combine_kernel(const float* Y, int N, int K, int out_pad, int members, int64_t sY,
-                                   const float* ymean, const float* ystd, double* mean_out, double* var_out,
-                                   double* disagree) {
+                                   const float* ymean, const float* ystd, const float* yscale, double* mean_out,
+                                   double* var_out, double* disagree, int aleatoric_only) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   float worst = 0.0f;
@@ -257,10 +260,19 @@ __global__ void mlp_combine_kernel(const float* Y, int N, int K, int out_pad, in
     mu *= inv;
     const float epi = fmaxf(mu2 * inv - mu * mu, 0.0f);
     ale *= inv;
-    const float var = ale + epi;
+    const float var = aleatoric_only ? ale : ale + epi;
     worst = fmaxf(worst, sqrtf(epi / fmaxf(ale, 1e-12f)));
-    if (mean_out) mean_out[(int64_t)i * K + k] = (double)mu * (double)ystd[k] + (double)ymean[k];
-    if (var_out) var_out[(int64_t)i * K + k] = (double)var * (double)ystd[k] * (double)ystd[k];
+    const double u = (double)mu * (double)ystd[k] + (double)ymean[k];
+    const double vu = (double)var * (double)ystd[k] * (double)ystd[k];
+    const double c = yscale ? (double)yscale[k] : 0.0;
+    if (c > 0.0) {
+      const double ch = c * cosh(u);
+      if (mean_out) mean_out[(int64_t)i * K + k] = c * sinh(u);
+      if (var_out) var_out[(int64_t)i * K + k] = ch * ch * vu;
+    } else {
+      if (mean_out) mean_out[(int64_t)i * K + k] = u;
+      if (var_out) var_out[(int64_t)i * K + k] = vu;
+    }
   }
   if (disagree) disagree[i] = worst;
 }
@@ -414,9 +426,10 @@ cudaError_t mlp_adam(const MlpDims& d, int members, float* P, const float* G, fl
 }
 
 cudaError_t mlp_combine(const MlpDims& d, int members, int N, const float* Y, const float* ymean, const float* ystd,
-                        double* mean_out, double* var_out, double* disagree, cudaStream_t s) {
+                        const float* yscale, double* mean_out, double* var_out, double* disagree, int aleatoric_only,
+                        cudaStream_t s) {
   mlp_combine_kernel<<<(N + 127) / 128, 128, 0, s>>>(Y, N, d.K, d.out_pad, members, (int64_t)N * d.out_pad, ymean,
-                                                     ystd, mean_out, var_out, disagree);
+                                                     ystd, yscale, mean_out, var_out, disagree, aleatoric_only);
   return cudaGetLastError();
 }
 

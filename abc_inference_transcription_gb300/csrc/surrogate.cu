@@ -33,7 +33,8 @@ cudaError_t mlp_loss(const MlpDims& d, int members, int B, int valid_rows, const
 cudaError_t mlp_adam(const MlpDims& d, int members, float* P, const float* G, float* m, float* v,
                      __nv_bfloat16* Ph, float lr, int step, cudaStream_t s);
 cudaError_t mlp_combine(const MlpDims& d, int members, int N, const float* Y, const float* ymean, const float* ystd,
-                        double* mean_out, double* var_out, double* disagree, cudaStream_t s);
+                        const float* yscale, double* mean_out, double* var_out, double* disagree, int aleatoric_only,
+                        cudaStream_t s);
 }  // namespace abc
 
 using namespace abc;
@@ -119,6 +120,41 @@ __global__ void norm_y_kernel(const double* st, int64_t N, int K, const double* 
     const int c = (int)(i % K);
     const double v = st[i];
     yf[i] = isfinite(v) ? (float)((v - mean[c]) / sd[c]) : __int_as_float(0x7fc00000);
+  }
+}
+
+// per statistic: scale c = mean |y| over finite values (1 if none), then y <- asinh(y / c) in place
+__global__ void asinh_scale_kernel(double* st, int64_t N, int K, float* scale) {
+  __shared__ double red[256];
+  __shared__ double cnt[256];
+  const int c = blockIdx.x;
+  double s = 0.0, n = 0.0;
+  for (int64_t i = threadIdx.x; i < N; i += blockDim.x) {
+    const double v = st[i * K + c];
+    if (isfinite(v)) { s += fabs(v); n += 1.0; }
+  }
+  red[threadIdx.x] = s;
+  cnt[threadIdx.x] = n;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) { red[threadIdx.x] += red[threadIdx.x + o]; cnt[threadIdx.x] += cnt[threadIdx.x + o]; }
+    __syncthreads();
+  }
+  double sc = cnt[0] > 0.0 ? red[0] / cnt[0] : 1.0;
+  if (!(sc > 1e-12)) sc = 1.0;
+  __syncthreads();
+  for (int64_t i = threadIdx.x; i < N; i += blockDim.x) {
+    const double v = st[i * K + c];
+    if (isfinite(v)) st[i * K + c] = asinh(v / sc);
+  }
+  if (threadIdx.x == 0) scale[c] = (float)sc;
+}
+
+__global__ void asinh_apply_kernel(double* st, int64_t N, int K, const float* scale) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N * K; i += (int64_t)gridDim.x * blockDim.x) {
+    const float c = scale[i % K];
+    const double v = st[i];
+    if (c > 0.0f && isfinite(v)) st[i] = asinh(v / (double)c);
   }
 }
 
@@ -219,7 +255,7 @@ struct abc_surrogate {
   std::string err;
   int step = 0;
   bool normed = false;
-  Buf<float> P, G, Am, Av, ymf, ysf;
+  Buf<float> P, G, Am, Av, ymf, ysf, yscf;  // yscf: asinh scale per statistic (0: identity)
   Buf<__nv_bfloat16> Ph;
   Buf<double> xm, xs, ym, ys;
   // training / batch scratch
@@ -282,7 +318,8 @@ int abc_surrogate_create(abc_surrogate** out, int in_dim, int n_stats, int ensem
   const size_t n = (size_t)s->d.n_params * ensemble;
   if (s->P.ensure(n) || s->G.ensure(n) || s->Am.ensure(n) || s->Av.ensure(n) || s->Ph.ensure(n) ||
       s->xm.ensure(kMlpInPad) || s->xs.ensure(kMlpInPad) || s->ym.ensure(n_stats) || s->ys.ensure(n_stats) ||
-      s->ymf.ensure(n_stats) || s->ysf.ensure(n_stats) || s->cnt.ensure(1)) {
+      s->ymf.ensure(n_stats) || s->ysf.ensure(n_stats) || s->yscf.ensure(n_stats) || s->cnt.ensure(1) ||
+      cudaMemset(s->yscf.p, 0, sizeof(float) * n_stats) != cudaSuccess) {
     cudaStreamDestroy(s->stream);
     delete s;
     return ABC_ERR_NOMEM;
@@ -302,6 +339,7 @@ int abc_surrogate_create(abc_surrogate** out, int in_dim, int n_stats, int ensem
 int abc_surrogate_destroy(abc_surrogate* s) {
   if (!s) return ABC_OK;
   cudaStreamSynchronize(s->stream);
+  s->yscf.release();
   s->P.release(); s->G.release(); s->Am.release(); s->Av.release(); s->Ph.release(); s->ymf.release();
   s->ysf.release(); s->xm.release(); s->xs.release(); s->ym.release(); s->ys.release(); s->th64.release();
   s->st64.release(); s->xn.release(); s->yn.release(); s->T.release(); s->Z.release(); s->Y.release();
@@ -329,12 +367,15 @@ static int load_training(abc_surrogate* s, const double* theta, const double* st
   SK(cudaMemcpyAsync(s->th64.p, theta, sizeof(double) * N * d.in_dim, cudaMemcpyHostToDevice, s->stream));
   SK(cudaMemcpyAsync(s->st64.p, stats, sizeof(double) * N * d.K, cudaMemcpyHostToDevice, s->stream));
   if (fit_norm) {
+    asinh_scale_kernel<<<d.K, 256, 0, s->stream>>>(s->st64.p, N, d.K, s->yscf.p);
     col_norm_kernel<<<d.in_dim, 256, 0, s->stream>>>(s->th64.p, N, d.in_dim, d.in_dim, s->xm.p, s->xs.p);
     col_norm_kernel<<<d.K, 256, 0, s->stream>>>(s->st64.p, N, d.K, d.K, s->ym.p, s->ys.p);
     SK(cudaGetLastError());
     d2f_kernel<<<1, 256, 0, s->stream>>>(s->ym.p, s->ymf.p, d.K);
     d2f_kernel<<<1, 256, 0, s->stream>>>(s->ys.p, s->ysf.p, d.K);
     s->normed = true;
+  } else {
+    asinh_apply_kernel<<<blocks(N * d.K), 256, 0, s->stream>>>(s->st64.p, N, d.K, s->yscf.p);
   }
   norm_x_kernel<<<blocks(N * d.in_pad), 256, 0, s->stream>>>(s->th64.p, N, d.in_dim, d.in_dim, s->xm.p, s->xs.p,
                                                               d.in_pad, s->xn.p, nullptr);
@@ -461,6 +502,7 @@ int abc_surrogate_set_norm(abc_surrogate* s, const double* xmean, const double* 
   SK(cudaMemcpy(s->ys.p, ystd, sizeof(double) * s->d.K, cudaMemcpyHostToDevice));
   d2f_kernel<<<1, 256, 0, s->stream>>>(s->ym.p, s->ymf.p, s->d.K);
   d2f_kernel<<<1, 256, 0, s->stream>>>(s->ys.p, s->ysf.p, s->d.K);
+  SK(cudaMemsetAsync(s->yscf.p, 0, sizeof(float) * s->d.K, s->stream));  // identity target transform
   SK(cudaStreamSynchronize(s->stream));
   s->normed = true;
   return ABC_OK;
@@ -469,7 +511,7 @@ int abc_surrogate_set_norm(abc_surrogate* s, const double* xmean, const double* 
 // predictions for device theta rows [0, N): mean, total variance (aleatoric +
 // ensemble), disagreement = max_k sqrt(ensemble var / aleatoric var)
 static int predict_chunk(abc_surrogate* s, const double* d_theta, int ld, int64_t n, double* d_mean, double* d_var,
-                         double* d_dis) {
+                         double* d_dis, int aleatoric_only = 0) {
   const MlpDims& d = s->d;
   const int E = s->members;
   SK(s->X0.ensure((size_t)n * d.in_pad));
@@ -479,7 +521,8 @@ static int predict_chunk(abc_surrogate* s, const double* d_theta, int ld, int64_
                                                               nullptr, s->X0.p);
   SK(cudaGetLastError());
   SK(mlp_forward(d, E, (int)n, s->X0.p, 0, s->Ph.p, s->P.p, nullptr, s->Ah.p, s->Y.p, s->stream));
-  SK(mlp_combine(d, E, (int)n, s->Y.p, s->ymf.p, s->ysf.p, d_mean, d_var, d_dis, s->stream));
+  SK(mlp_combine(d, E, (int)n, s->Y.p, s->ymf.p, s->ysf.p, s->yscf.p, d_mean, d_var, d_dis, aleatoric_only,
+                 s->stream));
   return ABC_OK;
 }
 
@@ -558,7 +601,7 @@ int abc_surrogate_screen_device(abc_surrogate* s, const double* d_theta, int ld_
   if (err_out) SK(eo.ensure((size_t)N * G));
   for (int64_t p0 = 0; p0 < N; p0 += kPredChunk) {
     const int64_t n = std::min<int64_t>(kPredChunk, N - p0);
-    int st = predict_chunk(s, d_theta + p0 * ld_theta, ld_theta, n, s->pm.p, s->pv.p, s->pd.p);
+    int st = predict_chunk(s, d_theta + p0 * ld_theta, ld_theta, n, s->pm.p, s->pv.p, s->pd.p, 1);
     if (st) return st;
     d2f_kernel<<<blocks(n * K), 256, 0, s->stream>>>(s->pm.p, s->pmf.p, n * K);
     d2f_kernel<<<blocks(n * K), 256, 0, s->stream>>>(s->pv.p, s->pvf.p, n * K);

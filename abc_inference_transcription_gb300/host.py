@@ -192,6 +192,40 @@ class Context:
         self._check(self.lib.abc_accept_fetch(self.h, ptr(off, C.c_int64), ptr(idx, C.c_int64), ptr(err)))
         return off, idx[:tot.value], err[:tot.value]
 
+    def _fetch(self, G: int, total: int):
+        off = np.zeros(G + 1, np.int64)
+        idx = np.zeros(max(total, 1), np.int64)
+        err = np.zeros(max(total, 1))
+        self._check(self.lib.abc_accept_fetch(self.h, ptr(off, C.c_int64), ptr(idx, C.c_int64), ptr(err)))
+        return off, idx[:total], err[:total]
+
+    def select_thr(self, data: np.ndarray, se: np.ndarray, stats: np.ndarray, thr: np.ndarray, families=None):
+        """Acceptance with one threshold per gene."""
+        d = np.ascontiguousarray(data, np.float64)
+        e = np.ascontiguousarray(se, np.float64)
+        s = np.ascontiguousarray(stats, np.float64)
+        t = np.ascontiguousarray(thr, np.float64)
+        G, K = d.shape
+        nf, f = self._fam(families, K)
+        tot = C.c_int64()
+        self._check(self.lib.abc_errors_select_thr(self.h, ptr(d), ptr(e), G, K, nf, ptr(f, C.c_int32), ptr(s),
+                                                   s.shape[0], ptr(t), C.byref(tot)))
+        return self._fetch(G, tot.value)
+
+    def select_device(self, data: np.ndarray, se: np.ndarray, d_stats: int, n: int, mode: int, eps_or_q: float = 0.0,
+                      thr: np.ndarray | None = None, families=None):
+        """Acceptance with the statistics already in device memory."""
+        d = np.ascontiguousarray(data, np.float64)
+        e = np.ascontiguousarray(se, np.float64)
+        t = None if thr is None else np.ascontiguousarray(thr, np.float64)
+        G, K = d.shape
+        nf, f = self._fam(families, K)
+        tot = C.c_int64()
+        self._check(self.lib.abc_errors_select_device(self.h, ptr(d), ptr(e), G, K, nf, ptr(f, C.c_int32),
+                                                      C.c_void_p(d_stats), n, mode, float(eps_or_q), ptr(t),
+                                                      C.byref(tot)))
+        return self._fetch(G, tot.value)
+
     def select_counters(self) -> tuple[int, int]:
         a, b = C.c_int64(), C.c_int64()
         self._check(self.lib.abc_select_counters(self.h, C.byref(a), C.byref(b)))

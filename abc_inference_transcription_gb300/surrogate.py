@@ -118,13 +118,26 @@ class Surrogate:
 
 
 def calibrate_margin(pred_err: np.ndarray, exact_err: np.ndarray, thr: np.ndarray, quantile: float = 0.99) -> float:
-    """Margin m such that a fraction `quantile` of the truly accepted (p, g)
-    pairs of a calibration set (exact_err <= thr) have pred_err <= thr + m."""
+    """Additive margin m such that a fraction `quantile` of the truly accepted
+    (p, g) pairs of a calibration set (exact_err <= thr) have pred_err <= thr + m."""
     acc = exact_err <= thr[None, :]
     if not acc.any():
         return 0.0
     short = (pred_err - thr[None, :])[acc]
     return float(max(0.0, np.quantile(short, quantile)))
+
+
+def calibrate_factor(pred_err: np.ndarray, exact_err: np.ndarray, thr: np.ndarray, quantile: float = 0.99) -> float:
+    """Multiplicative margin f (screen keeps pred_err <= f thr) such that a
+    fraction `quantile` of the truly accepted pairs of a calibration set pass.
+    Predicted errors are heavy-tailed, so a ratio calibrates better than a
+    difference."""
+    acc = exact_err <= thr[None, :]
+    if not acc.any():
+        return 1.0
+    ratio = (pred_err / np.maximum(thr[None, :], 1e-12))[acc]
+    ratio = np.where(np.isfinite(ratio), ratio, np.inf)
+    return float(max(1.0, np.quantile(ratio, quantile)))
 
 
 def false_rejection_rate(keep: np.ndarray, exact_err: np.ndarray, thr: np.ndarray) -> tuple[float, int]:

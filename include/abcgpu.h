@@ -202,6 +202,17 @@ int abc_errors_select(abc_ctx* ctx, const double* data, const double* se, int64_
                       int K, int n_families, const int32_t* family_sizes,
                       const double* stats, int64_t n_particles, int mode, double eps_or_q,
                       int64_t* n_accepted_total);
+/* Acceptance with a threshold per gene (thr: G entries, host), e.g. the
+ * thresholds a top-q selection produced; same output as abc_errors_select. */
+int abc_errors_select_thr(abc_ctx* ctx, const double* data, const double* se, int64_t n_genes, int K,
+                          int n_families, const int32_t* family_sizes, const double* stats,
+                          int64_t n_particles, const double* thr, int64_t* n_accepted_total);
+/* abc_errors_select with the statistics in device memory (e.g. the d_stats of
+ * abc_simulate_device); mode 2 takes per-gene thresholds thr (host). */
+int abc_errors_select_device(abc_ctx* ctx, const double* data, const double* se, int64_t n_genes, int K,
+                             int n_families, const int32_t* family_sizes, const double* d_stats,
+                             int64_t n_particles, int mode, double eps_or_q, const double* thr,
+                             int64_t* n_accepted_total);
 /* gene_offsets: G+1 entries; particle_idx: 1-based, n_accepted_total entries;
  * err: FP64 errors of the accepted pairs (may be NULL). */
 int abc_accept_fetch(abc_ctx* ctx, int64_t* gene_offsets, int64_t* particle_idx, double* err);
@@ -241,7 +252,10 @@ int abc_surrogate_predict(abc_surrogate* s, const double* theta, int64_t n, doub
                           double* disagree);
 int abc_surrogate_predict_device(abc_surrogate* s, const double* d_theta, int ld_theta, int64_t n,
                                  double* d_mean, double* d_var, double* d_disagree);
-/* d_keep[p] = 1 for the draws to simulate exactly; data, se: G x n_stats
+/* d_keep[p] = 1 for the draws to simulate exactly: min(10, sum_k w ((d - mu)^2
+ * + aleatoric var) / K) <= thr[g] + margin for some gene, or disagreement >
+ * disagree_max (epistemic uncertainty is handled by that rule, not by the
+ * error).  data, se: G x n_stats
  * (host), thr: per-gene error threshold (host), margin added to it.
  * err_out (host, n x G, optional, small n only): predicted expected errors. */
 int abc_surrogate_screen_device(abc_surrogate* s, const double* d_theta, int ld_theta, int64_t n,

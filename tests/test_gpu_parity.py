@@ -254,3 +254,33 @@ def test_accepted_particles_reference_format(Ctx, orc):
     for g in range(32):
         want = ridx[roff[g]:roff[g + 1]].tolist() or [0]
         assert lists[g] == want
+
+
+def test_select_per_gene_thresholds_and_device_stats(Ctx, orc):
+    """Per-gene thresholds (the screened pipeline's acceptance) and device-resident
+    statistics give the oracle's accepted sets."""
+    torch = pytest.importorskip("torch")
+    data, se = _ref_data()
+    data, se = data[:48], se[:48]
+    rng = np.random.default_rng(12)
+    stats = _stats_near(data, 3000, rng, spread=0.3)
+    err = orc.errors(data, se, stats, REF_FAMILIES)
+    thr = np.quantile(err, 0.03, axis=0)
+    thr[5] = -1.0  # a gene with no acceptance
+    want_off, want_idx = [0], []
+    for g in range(48):
+        o, i = orc.accept(err[:, g:g + 1], 0, thr[g])
+        want_idx.append(i)
+        want_off.append(want_off[-1] + i.shape[0])
+    want_idx = np.concatenate(want_idx)
+    with Ctx(make_config("hour"), None) as ctx:
+        off, idx, e = ctx.select_thr(data, se, stats, thr, REF_FAMILIES)
+        assert np.array_equal(off, want_off) and np.array_equal(idx, want_idx)
+        d_stats = torch.from_numpy(np.ascontiguousarray(stats)).cuda()
+        off2, idx2, _ = ctx.select_device(data, se, d_stats.data_ptr(), stats.shape[0], 2, thr=thr,
+                                          families=REF_FAMILIES)
+        assert np.array_equal(off2, want_off) and np.array_equal(idx2, want_idx)
+        off3, idx3, _ = ctx.select_device(data, se, d_stats.data_ptr(), stats.shape[0], 1, 0.01,
+                                          families=REF_FAMILIES)
+        roff, ridx = orc.accept(err, 1, 0.01)
+        assert np.array_equal(off3, roff) and np.array_equal(idx3, ridx)

@@ -59,52 +59,61 @@ def test_training_reduces_loss_and_predicts_held_out(mods):
         th = ctx.sample_prior(1, 12000, 5, reference_prior())
         th[:, 2] = np.minimum(th[:, 2], 2.0)
         st = _exact(ctx, th, 1)
-    good = np.isfinite(st).all(axis=1)
-    th, st = th[good], st[good]
     n_tr = int(0.9 * th.shape[0])
     with S.Surrogate(5, 53, ensemble=4, seed=2) as sg:
         loss = sg.train(th[:n_tr], st[:n_tr], epochs=25, batch=1024, lr=2e-3)
         assert loss[-1] < loss[0] - 0.5, loss
         mean, var, dis = sg.predict(th[n_tr:])
-        ym, ys = sg.norm()[2:]
-        z = (mean - st[n_tr:]) / ys
+        z = (mean - st[n_tr:]) / np.nanstd(st[:n_tr], axis=0)
         # held-out mean absolute standardised error well below the prior spread (1.0)
-        assert np.median(np.abs(z)) < 0.35, np.median(np.abs(z))
+        assert np.nanmedian(np.abs(z)) < 0.35, np.nanmedian(np.abs(z))
         assert np.all(var > 0) and np.all(np.isfinite(dis))
 
 
 def test_screen_gain_at_calibrated_false_rejection(mods):
+    """Train on SSA output, calibrate the margin (99 % of truly accepted pairs)
+    and the disagreement cut (99th percentile) on one half of an exact set,
+    then screen the other half: the false-rejection rate stays near 1 % while
+    far fewer draws need the exact SSA."""
     S, Context = mods
     torch = pytest.importorskip("torch")
     cfg = make_config("hour", precision=abi.FP32)
     cells = synthetic_cells(seed=4)
     rng = np.random.default_rng(8)
     with Context(cfg, cells) as ctx:
-        th_tr = ctx.sample_prior(1, 16000, 21, reference_prior())
+        th_tr = ctx.sample_prior(1, 48000, 21, reference_prior())
         st_tr = _exact(ctx, th_tr, 2)
         th_ex = ctx.sample_prior(1, 12000, 22, reference_prior(), offset=100000)
         st_ex = _exact(ctx, th_ex, 3)
-        # 6 genes: statistics of random particles with 5 % noise; se ~ 10 % of the statistic
-        G = 6
-        src = np.flatnonzero(np.isfinite(st_ex).all(axis=1))[:G]
-        data = st_ex[src] * rng.lognormal(0, 0.05, (G, 53))
-        se = 0.1 * np.abs(data) * rng.lognormal(0, 0.5, (G, 53))
+        # candidate genes: statistics of random particles with 5 % noise, se ~ 10 %
+        # of the statistic; keep the genes whose top-1 % threshold is informative
+        # (below the clip at 10 by a margin), as ABC genes with a posterior are
+        src = np.flatnonzero(np.isfinite(st_ex).all(axis=1))[:60]
+        data = st_ex[src] * rng.lognormal(0, 0.05, (src.shape[0], 53))
+        se = 0.1 * np.abs(data) * rng.lognormal(0, 0.5, data.shape)
         err = ctx.errors(data, se, st_ex)
-    ok = np.isfinite(st_tr).all(axis=1)
+    k = int(0.01 * th_ex.shape[0])
+    thr = np.sort(np.where(np.isfinite(err), err, np.inf), axis=0)[k - 1]
+    genes = np.flatnonzero(thr < 8.0)[:6]
+    assert genes.shape[0] >= 3, thr
+    data, se, err, thr = data[genes], se[genes], err[:, genes], thr[genes]
+    G = genes.shape[0]
     with S.Surrogate(5, 53, ensemble=4, seed=5) as sg:
-        sg.train(th_tr[ok], st_tr[ok], epochs=30, batch=1024, lr=2e-3)
-        thr = np.quantile(np.where(np.isfinite(err), err, 10.0), 0.02, axis=0)
+        sg.train(th_tr, st_tr, epochs=40, batch=2048, lr=2e-3)
         half = th_ex.shape[0] // 2
+        _, _, dis = sg.predict(th_ex[:half])
+        dmax = float(np.quantile(dis, 0.99))
         d_th = torch.from_numpy(np.ascontiguousarray(th_ex)).cuda()
         d_keep = torch.zeros(th_ex.shape[0], dtype=torch.uint8, device="cuda")
         pred = np.zeros((half, G))
         sg.screen_device(d_th.data_ptr(), 5, half, data, se, thr, 0.0, 1e30, d_keep.data_ptr(), err_out=pred)
-        margin = S.calibrate_margin(pred, err[:half], thr, 0.99)
-        n_keep = sg.screen_device(d_th[half:].data_ptr(), 5, th_ex.shape[0] - half, data, se, thr, margin, 3.0,
-                                  d_keep[half:].data_ptr())
+        factor = S.calibrate_factor(pred, err[:half], thr, 0.99)
+        n_keep = sg.screen_device(d_th[half:].data_ptr(), 5, th_ex.shape[0] - half, data, se, thr * factor, 0.0,
+                                  dmax, d_keep[half:].data_ptr())
         keep = d_keep[half:].cpu().numpy()
     frr, n_acc = S.false_rejection_rate(keep, err[half:], thr)
     frac = n_keep / (th_ex.shape[0] - half)
-    assert n_acc > 50
-    assert frr <= 0.05, (frr, n_acc)
-    assert frac < 0.5, frac   # >= 2x fewer exact simulations per accepted particle
+    info = dict(thr=thr.round(3).tolist(), factor=factor, dmax=dmax, frr=frr, n_acc=n_acc, frac=frac)
+    assert n_acc > 50, info
+    assert frr <= 0.03, info
+    assert frac < 0.5, info   # >= 2x fewer exact simulations per accepted particle
