@@ -132,6 +132,7 @@ def _declare(lib: C.CDLL) -> None:
         "abc_stream": (vp, [vp]),
         "abc_set_cells": (C.c_int, [vp, i64, i32p, i32p, dp, dp]),
         "abc_sample_prior": (C.c_int, [vp, C.c_int, i64, u64, i64, C.POINTER(AbcPrior), dp]),
+        "abc_sample_prior_device": (C.c_int, [vp, C.c_int, i64, u64, i64, C.POINTER(AbcPrior), vp]),
         "abc_simulate": (C.c_int, [vp, C.c_int, dp, i64, u64, i64, dp]),
         "abc_simulate_device": (C.c_int, [vp, C.c_int, vp, i64, u64, i64, vp]),
         "abc_synchronize": (C.c_int, [vp]),
@@ -153,6 +154,7 @@ def _declare(lib: C.CDLL) -> None:
                                                C.c_double, dp, i64p]),
         "abc_accept_fetch": (C.c_int, [vp, i64p, i64p, dp]),
         "abc_select_counters": (C.c_int, [vp, i64p, i64p]),
+        "abc_select_profile_read": (C.c_int, [vp, dp, C.POINTER(C.c_int)]),
     }
     sp = vp
     sig.update({
@@ -169,8 +171,8 @@ def _declare(lib: C.CDLL) -> None:
         "abc_surrogate_predict": (C.c_int, [sp, dp, i64, dp, dp, dp]),
         "abc_surrogate_predict_device": (C.c_int, [sp, vp, C.c_int, i64, vp, vp, vp]),
         "abc_surrogate_compact_device": (C.c_int, [sp, vp, vp, C.c_int, i64, vp, vp, i64p]),
-        "abc_surrogate_screen_device": (C.c_int, [sp, vp, C.c_int, i64, dp, dp, i64, dp, C.c_double, C.c_double, vp,
-                                                  i64p, dp]),
+        "abc_surrogate_screen_device": (C.c_int, [sp, vp, C.c_int, i64, dp, dp, i64, dp, C.c_double, C.c_double,
+                                                  C.c_double, vp, i64p, dp]),
     })
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -181,11 +183,11 @@ def _declare(lib: C.CDLL) -> None:
 # Every symbol include/abcgpu.h declares (checked by the CPU test suite).
 ABI_SYMBOLS = [
     "abc_create", "abc_destroy", "abc_last_error", "abc_num_params", "abc_num_stats",
-    "abc_stream", "abc_set_cells", "abc_sample_prior", "abc_simulate", "abc_simulate_device",
+    "abc_stream", "abc_set_cells", "abc_sample_prior", "abc_sample_prior_device", "abc_simulate", "abc_simulate_device",
     "abc_synchronize", "abc_simulate_batch", "abc_simulate_batch_device", "abc_simulate_noalloc", "abc_simulate_cells", "abc_last_counters",
     "abc_profile", "abc_profile_read", "abc_autotune", "abc_set_variant", "abc_errors",
     "abc_errors_select", "abc_errors_select_thr", "abc_errors_select_device", "abc_accept_fetch",
-    "abc_select_counters",
+    "abc_select_counters", "abc_select_profile_read",
     "abc_surrogate_create", "abc_surrogate_destroy", "abc_surrogate_last_error", "abc_surrogate_num_params",
     "abc_surrogate_train", "abc_surrogate_gradients", "abc_surrogate_get_params", "abc_surrogate_set_params",
     "abc_surrogate_get_norm", "abc_surrogate_set_norm", "abc_surrogate_predict", "abc_surrogate_predict_device",

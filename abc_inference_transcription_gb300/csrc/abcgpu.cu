@@ -85,6 +85,9 @@ struct abc_ctx {
   DBuf<unsigned long long> d_gcursor, d_ncand;
   DBuf<int> d_fail;
   DBuf<double> d_thr;
+  cudaEvent_t sel_ev[2] = {nullptr, nullptr};
+  double sel_fast_ms = 0.0;  // candidate-pass kernel time of the last selection (abc_profile)
+  int sel_fast_passes = 0;
   int64_t cand_cap = int64_t(1) << 22;
   int64_t sel_G = 0, sel_total = 0, sel_cands = 0, sel_rechecked = 0;
   bool sel_ready = false;
@@ -203,6 +206,8 @@ int abc_destroy(abc_ctx* c) {
   c->d_alen.release(); c->d_aoff.release(); c->d_out_idx.release(); c->d_gcursor.release();
   c->d_ncand.release(); c->d_fail.release(); c->d_thr.release();
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+  for (cudaEvent_t e : c->sel_ev)
+    if (e) cudaEventDestroy(e);
   cudaStreamDestroy(c->stream);
   delete c;
   return ABC_OK;
@@ -275,8 +280,8 @@ int abc_set_cells(abc_ctx* c, int64_t n_cells, const int32_t* cell_cond, const i
   return ABC_OK;
 }
 
-int abc_sample_prior(abc_ctx* c, int model, int64_t P, uint64_t seed, int64_t particle_offset,
-                     const abc_prior* prior, double* theta_out) {
+static int sample_prior_impl(abc_ctx* c, int model, int64_t P, uint64_t seed, int64_t particle_offset,
+                             const abc_prior* prior, double* theta_out, bool device_out) {
   if (!c) return ABC_ERR_INVALID;
   const int npar = npar_of(&c->cfg, model);
   if (npar < 0 || P < 0 || !prior || (!theta_out && P > 0)) return fail(c, ABC_ERR_INVALID, "abc_sample_prior: bad arguments");
@@ -304,12 +309,27 @@ int abc_sample_prior(abc_ctx* c, int model, int64_t P, uint64_t seed, int64_t pa
   a.vary_mode = prior->vary_mode;
   a.lf0 = prior->vary_mode == 1 ? xlog(prior->factor[0]) / ABC_LN10 : 0.0;
   a.lf1 = prior->vary_mode == 1 ? xlog(prior->factor[1]) / ABC_LN10 : 0.0;
+  if (device_out) {
+    a.theta = theta_out;
+    CK(launch_prior(a, c->stream));
+    return ABC_OK;
+  }
   CK(c->d_theta.ensure((size_t)P * npar));
   a.theta = c->d_theta.p;
   CK(launch_prior(a, c->stream));
   CK(cudaMemcpyAsync(theta_out, c->d_theta.p, sizeof(double) * P * npar, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return ABC_OK;
+}
+
+int abc_sample_prior(abc_ctx* c, int model, int64_t P, uint64_t seed, int64_t particle_offset,
+                     const abc_prior* prior, double* theta_out) {
+  return sample_prior_impl(c, model, P, seed, particle_offset, prior, theta_out, false);
+}
+
+int abc_sample_prior_device(abc_ctx* c, int model, int64_t P, uint64_t seed, int64_t particle_offset,
+                            const abc_prior* prior, double* d_theta_out) {
+  return sample_prior_impl(c, model, P, seed, particle_offset, prior, d_theta_out, true);
 }
 
 // Enqueue setup -> SSA -> capture/statistics for particles [0, P) of
@@ -686,15 +706,32 @@ static int candidate_pass(abc_ctx* c, const DistInputs& in, int64_t* n) {
   for (int attempt = 0; attempt < 2; ++attempt) {
     CK(c->d_cand.ensure((size_t)c->cand_cap));
     CK(cudaMemsetAsync(c->d_ncand.p, 0, sizeof(unsigned long long), c->stream));
+    if (c->prof && !c->sel_ev[0]) {
+      CK(cudaEventCreate(&c->sel_ev[0]));
+      CK(cudaEventCreate(&c->sel_ev[1]));
+    }
+    if (c->prof) CK(cudaEventRecord(c->sel_ev[0], c->stream));
     CK(launch_dist_fast(c->d_s32.p, c->d_sw.p, c->d_dw.p, in.P, in.G, in.K, c->d_X.p, c->d_cand.p, c->d_ncand.p,
                         c->cand_cap, nullptr, 0, 0, c->stream));
+    if (c->prof) CK(cudaEventRecord(c->sel_ev[1], c->stream));
     unsigned long long h = 0;
     CK(cudaMemcpyAsync(&h, c->d_ncand.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    if (c->prof) {
+      float ms = 0.0f;
+      CK(cudaEventElapsedTime(&ms, c->sel_ev[0], c->sel_ev[1]));
+      c->sel_fast_ms += ms;
+      c->sel_fast_passes += 1;
+    }
     if ((int64_t)h <= c->cand_cap) {
       *n = (int64_t)h;
       return ABC_OK;
     }
+    // candidates carry 8 B each plus 20 B in the recheck and sort buffers
+    const int64_t limit = int64_t(1) << 28;
+    if ((int64_t)h > limit)
+      return fail(c, ABC_ERR_CAPACITY,
+                  "more than 2^28 candidates (a threshold at the clip value 10 ties too many particles)");
     c->cand_cap = (int64_t)h + (int64_t)h / 8 + 1024;
   }
   return fail(c, ABC_ERR_CAPACITY, "candidate buffer overflow");
@@ -730,6 +767,8 @@ static int select_impl(abc_ctx* c, const double* data, const double* se, int64_t
   CK(c->d_alen.ensure((size_t)G));
   CK(c->d_aoff.ensure((size_t)G + 1));
   CK(c->d_fail.ensure((size_t)G));
+  c->sel_fast_ms = 0.0;
+  c->sel_fast_passes = 0;
   CK(launch_dist_prep(in, c->d_sw.p, c->d_dw.p, c->d_s32.p, c->stream));
   const int64_t kq = mode == 1 ? (int64_t)std::ceil(eps_or_q * (double)P) : 0;
   std::vector<float> hX((size_t)G);
@@ -844,6 +883,13 @@ int abc_accept_fetch(abc_ctx* c, int64_t* gene_offsets, int64_t* particle_idx, d
       CK(cudaMemcpyAsync(err, c->d_out_err.p, sizeof(double) * c->sel_total, cudaMemcpyDeviceToHost, c->stream));
   }
   CK(cudaStreamSynchronize(c->stream));
+  return ABC_OK;
+}
+
+int abc_select_profile_read(const abc_ctx* c, double* fast_ms, int* fast_passes) {
+  if (!c) return ABC_ERR_INVALID;
+  if (fast_ms) *fast_ms = c->sel_fast_ms;
+  if (fast_passes) *fast_passes = c->sel_fast_passes;
   return ABC_OK;
 }
 

@@ -166,17 +166,18 @@ cudaError_t launch_dist_threshold(const float* esub, int64_t n_sub, int64_t G, i
 
 float dist_bound(float e, int K) { return dist_bound_f(e, K); }
 
-// Surrogate screen: expected error of particle p for gene g under the
-// predicted statistics N(mu_pk, var_pk),
-//   E[err_pg] = sum_k w_gk ((d_gk - mu_pk)^2 + var_pk) / K,
-// keep[p] = 1 when E[err_pg] <= X[g] for some gene (X = threshold + margin).
-// Same 128 x 128 tiling as dist_fast_kernel; three FMAs per (p, g, k).
+// Surrogate screen: a lower confidence bound of the error of particle p for
+// gene g under the predicted statistics (mean mu_pk, predictive std sd_pk):
+//   L_pg = sum_k w_gk max(0, |d_gk - mu_pk| - z sd_pk)^2 / K,
+// keep[p] = 1 when L_pg <= X[g] for some gene (X = calibrated threshold).
+// A draw is dropped only when it is confidently far from every gene.  Same
+// 128 x 128 tiling as dist_fast_kernel.
 __global__ void __launch_bounds__(256) dist_screen_kernel(const float* __restrict__ mu,
                                                           const float* __restrict__ var,
                                                           const float* __restrict__ sw,
                                                           const float* __restrict__ dw, int64_t P, int64_t G,
-                                                          int K, const float* __restrict__ X, uint8_t* keep,
-                                                          float* err_out) {
+                                                          int K, const float* __restrict__ X, float z,
+                                                          uint8_t* keep, float* err_out) {
   __shared__ float sm[kDistKc][kDistTile];
   __shared__ float sv[kDistKc][kDistTile];
   __shared__ float sa[kDistKc][kDistTile];
@@ -197,7 +198,7 @@ __global__ void __launch_bounds__(256) dist_screen_kernel(const float* __restric
       float m = 0.0f, v = 0.0f, a = 0.0f, d = 0.0f;
       if (p < P && k < K) {
         m = mu[p * K + k];
-        v = var[p * K + k];
+        v = z * sqrtf(fmaxf(var[p * K + k], 0.0f));  // z x predictive std
       }
       if (g < G && k < K) {
         a = sw[g * K + k];
@@ -227,8 +228,8 @@ __global__ void __launch_bounds__(256) dist_screen_kernel(const float* __restric
       for (int i = 0; i < 8; ++i)
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-          const float t = fmaf(-a[j], m[i], d[j]);
-          acc[i][j] = fmaf(t, t, fmaf(a[j] * a[j], v[i], acc[i][j]));
+          const float t = fmaxf(fabsf(fmaf(-a[j], m[i], d[j])) - a[j] * v[i], 0.0f);
+          acc[i][j] = fmaf(t, t, acc[i][j]);
         }
     }
     __syncthreads();
@@ -252,10 +253,11 @@ __global__ void __launch_bounds__(256) dist_screen_kernel(const float* __restric
 }
 
 cudaError_t launch_dist_screen(const float* mu, const float* var, const float* sw, const float* dw, int64_t P,
-                               int64_t G, int K, const float* X, uint8_t* keep, float* err_out, cudaStream_t s) {
+                               int64_t G, int K, const float* X, float z, uint8_t* keep, float* err_out,
+                               cudaStream_t s) {
   if (P <= 0 || G <= 0) return cudaSuccess;
   dim3 grid((unsigned)((G + kDistTile - 1) / kDistTile), (unsigned)((P + kDistTile - 1) / kDistTile));
-  dist_screen_kernel<<<grid, 256, 0, s>>>(mu, var, sw, dw, P, G, K, X, keep, err_out);
+  dist_screen_kernel<<<grid, 256, 0, s>>>(mu, var, sw, dw, P, G, K, X, z, keep, err_out);
   return cudaGetLastError();
 }
 

@@ -100,9 +100,10 @@ cudaError_t launch_ssa_fp64(const SsaArgs& a, int grid, cudaStream_t s);
 constexpr int kSsaVariants = 2;
 cudaError_t launch_ssa_fp32(const SsaArgs& a, int grid, cudaStream_t s, int variant = 0);
 cudaError_t launch_stats(const StatsArgs& a, cudaStream_t s);
-// surrogate screen: keep[p] = 1 if sum_k w ((d - mu)^2 + var) / K <= X[g] for some g
+// surrogate screen: keep[p] = 1 if sum_k w max(0, |d - mu| - z sqrt(var))^2 / K <= X[g] for some g
 cudaError_t launch_dist_screen(const float* mu, const float* var, const float* sw, const float* dw, int64_t P,
-                               int64_t G, int K, const float* X, uint8_t* keep, float* err_out, cudaStream_t s);
+                               int64_t G, int K, const float* X, float z, uint8_t* keep, float* err_out,
+                               cudaStream_t s);
 
 // particles ordered by expected trajectory cost, descending (hist128: 128 scratch words)
 cudaError_t launch_work_order(const PRec* rec, int64_t P, unsigned int* hist128, uint32_t* order, cudaStream_t s);

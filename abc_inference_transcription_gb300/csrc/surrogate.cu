@@ -563,8 +563,8 @@ int abc_surrogate_predict(abc_surrogate* s, const double* theta, int64_t N, doub
 // thr: per-gene error threshold; X = thr + margin.  err_out (optional, host,
 // N x G): the predicted expected errors (for calibration on small sets).
 int abc_surrogate_screen_device(abc_surrogate* s, const double* d_theta, int ld_theta, int64_t N, const double* data,
-                                const double* se, int64_t G, const double* thr, double margin, double disagree_max,
-                                uint8_t* d_keep, int64_t* n_keep, double* err_out) {
+                                const double* se, int64_t G, const double* thr, double margin, double z,
+                                double disagree_max, uint8_t* d_keep, int64_t* n_keep, double* err_out) {
   if (!s) return ABC_ERR_INVALID;
   if (!s->normed) return sfail(s, ABC_ERR_STATE, "surrogate not trained");
   const int K = s->d.K;
@@ -601,11 +601,11 @@ int abc_surrogate_screen_device(abc_surrogate* s, const double* d_theta, int ld_
   if (err_out) SK(eo.ensure((size_t)N * G));
   for (int64_t p0 = 0; p0 < N; p0 += kPredChunk) {
     const int64_t n = std::min<int64_t>(kPredChunk, N - p0);
-    int st = predict_chunk(s, d_theta + p0 * ld_theta, ld_theta, n, s->pm.p, s->pv.p, s->pd.p, 1);
+    int st = predict_chunk(s, d_theta + p0 * ld_theta, ld_theta, n, s->pm.p, s->pv.p, s->pd.p, 0);
     if (st) return st;
     d2f_kernel<<<blocks(n * K), 256, 0, s->stream>>>(s->pm.p, s->pmf.p, n * K);
     d2f_kernel<<<blocks(n * K), 256, 0, s->stream>>>(s->pv.p, s->pvf.p, n * K);
-    SK(launch_dist_screen(s->pmf.p, s->pvf.p, s->sw.p, s->dw.p, n, G, K, s->X.p, d_keep + p0,
+    SK(launch_dist_screen(s->pmf.p, s->pvf.p, s->sw.p, s->dw.p, n, G, K, s->X.p, (float)z, d_keep + p0,
                           err_out ? eo.p + p0 * G : nullptr, s->stream));
     disagree_keep_kernel<<<blocks(n), 256, 0, s->stream>>>(s->pd.p, n, disagree_max, d_keep + p0);
     SK(cudaGetLastError());

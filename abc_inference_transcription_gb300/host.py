@@ -87,6 +87,11 @@ class Context:
         self._check(self.lib.abc_sample_prior(self.h, model, n, seed, offset, C.byref(prior), ptr(th)))
         return th
 
+    def sample_prior_device(self, model: int, n: int, seed: int, prior: AbcPrior, d_out: int, offset: int = 0) -> None:
+        """Prior draw into device memory (n x npar doubles at d_out), on self.stream."""
+        self._check(self.lib.abc_sample_prior_device(self.h, model, n, seed, offset, C.byref(prior),
+                                                     C.c_void_p(d_out)))
+
     # -- simulation -------------------------------------------------------
     def simulate(self, model: int, theta: np.ndarray, seed: int, offset: int = 0) -> np.ndarray:
         th = np.ascontiguousarray(theta, np.float64)
@@ -225,6 +230,12 @@ class Context:
                                                       C.c_void_p(d_stats), n, mode, float(eps_or_q), ptr(t),
                                                       C.byref(tot)))
         return self._fetch(G, tot.value)
+
+    def select_profile(self) -> tuple[float, int]:
+        """(candidate-pass kernel ms, passes) of the last selection (needs profile(True))."""
+        ms, n = C.c_double(), C.c_int()
+        self._check(self.lib.abc_select_profile_read(self.h, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
 
     def select_counters(self) -> tuple[int, int]:
         a, b = C.c_int64(), C.c_int64()

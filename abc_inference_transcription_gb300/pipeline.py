@@ -1,0 +1,210 @@
+"""Plain and surrogate-screened ABC runs on one GPU.
+
+Plain ABC (the reference's workflow, scripts/abc_simulation.jl:88-97 then
+scripts/compute_errors.jl and scripts/accepted_particles.jl): draw particles of
+the five models from the prior, simulate every draw exactly, accept per gene.
+
+Screened ABC: a surrogate ensemble trained on the pipeline's own exact
+simulations predicts each draw's statistics; only draws whose predicted
+expected error is within a calibrated factor of a gene's threshold (or whose
+ensemble disagrees) are simulated exactly and go through the exact,
+FP64-checked acceptance.  Draws, statistics and flags stay in device memory;
+torch tensors serve only as device buffers and for row gathers.
+"""
+from __future__ import annotations
+
+import time
+
+import numpy as np
+
+from .config import factor_prior, make_config, synthetic_cells
+from .host import Context
+from .surrogate import Surrogate, calibrate_factor
+
+LD = 9         # theta row stride of the five-model batch (largest npar)
+IN_DIM = 14    # surrogate input: padded theta (9) + one-hot model (5)
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def draw(ctx: Context, per_model: int, seed: int, prior, offset: int = 0):
+    """Prior draws of the five models on the device: theta [5 per_model, 9] and model ids."""
+    torch = _torch()
+    P = 5 * per_model
+    theta = torch.zeros((P, LD), dtype=torch.float64, device="cuda")
+    models = torch.empty(P, dtype=torch.int32, device="cuda")
+    for m in range(1, 6):
+        npar = ctx.num_params(m)
+        tmp = torch.empty((per_model, npar), dtype=torch.float64, device="cuda")
+        ctx.sample_prior_device(m, per_model, seed + m, prior, tmp.data_ptr(), offset=offset + (m - 1) * per_model)
+        torch.cuda.synchronize()
+        theta[(m - 1) * per_model:m * per_model, :npar] = tmp
+        models[(m - 1) * per_model:m * per_model] = m
+    return theta, models
+
+
+def surrogate_input(theta, models):
+    torch = _torch()
+    onehot = torch.nn.functional.one_hot((models - 1).long(), 5).to(torch.float64)
+    return torch.cat([theta, onehot], dim=1).contiguous()
+
+
+def simulate(ctx: Context, theta, models, seed: int, offset: int = 0):
+    torch = _torch()
+    P = theta.shape[0]
+    stats = torch.empty((P, ctx.K), dtype=torch.float64, device="cuda")
+    if P:
+        ctx.simulate_batch_device(models.data_ptr(), theta.data_ptr(), LD, P, seed, stats.data_ptr(), offset=offset)
+        ctx.synchronize()
+    return stats
+
+
+def make_genes(stats: np.ndarray, G: int, rng: np.random.Generator):
+    """Synthetic genes: statistics of simulated particles plus 5 % Gaussian noise;
+    standard errors log-normal (sigma 0.5) around 10 % of the statistic."""
+    ok = np.flatnonzero(np.isfinite(stats).all(axis=1))
+    src = stats[rng.choice(ok, size=G, replace=ok.shape[0] < G)]
+    data = src + rng.normal(0.0, 1.0, src.shape) * 0.05 * np.abs(src)
+    se = 0.1 * np.abs(data) * rng.lognormal(0.0, 0.5, data.shape)
+    return data, se
+
+
+CLIP = 10.0  # errors are clipped at 10 (scripts/compute_errors.jl:159-161)
+
+
+def thresholds_from_lists(off: np.ndarray, err: np.ndarray) -> np.ndarray:
+    """Per-gene threshold = largest accepted error of a top-k selection that is
+    below the clip value.  A clipped error (10) says only "far away": when the
+    k-th error of a gene is the clip, its top-k would be an arbitrary set of
+    tied particles, so such a gene accepts only its unclipped particles (and
+    none when it has none; threshold -1)."""
+    G = off.shape[0] - 1
+    thr = np.full(G, -1.0)
+    for g in range(G):
+        e = err[off[g]:off[g + 1]]
+        e = e[e < CLIP]
+        if e.shape[0]:
+            thr[g] = e[-1]
+    return thr
+
+
+def _screened(ctx, sg, data, se, thr, factor, dmax, per_model_s, prior, seed, offset, z=2.0):
+    """Screened ABC: draw, screen, compact, simulate the survivors, accept with
+    the per-gene thresholds.  Returns (accepted pairs, simulated draws, times)."""
+    torch = _torch()
+    t0 = time.perf_counter()
+    th_s, m_s = draw(ctx, per_model_s, seed, prior, offset=offset)
+    x_s = surrogate_input(th_s, m_s)
+    keep = torch.zeros(th_s.shape[0], dtype=torch.uint8, device="cuda")
+    n_keep = sg.screen_device(x_s.data_ptr(), IN_DIM, th_s.shape[0], data, se, thr * factor, 0.0, dmax,
+                              keep.data_ptr(), z=z)
+    sidx = torch.empty(max(n_keep, 1), dtype=torch.int64, device="cuda")
+    sg.compact_device(keep.data_ptr(), 0, LD, th_s.shape[0], 0, sidx.data_ptr())
+    sel = sidx[:n_keep]
+    th_k, m_k = th_s[sel].contiguous(), m_s[sel].contiguous()
+    torch.cuda.synchronize()
+    t_screen = time.perf_counter() - t0
+    st_k = simulate(ctx, th_k, m_k, seed + 7, offset=offset)
+    t_sim = time.perf_counter() - t0 - t_screen
+    acc = 0
+    if n_keep:
+        off_k, _, _ = ctx.select_device(data, se, st_k.data_ptr(), n_keep, 2, thr=thr)
+        acc = int(off_k[-1])
+    torch.cuda.synchronize()
+    return acc, int(n_keep), int(th_s.shape[0]), time.perf_counter() - t0, t_screen, t_sim
+
+
+def run(genes=(2000,), per_model_train: int = 20000, per_model_plain: int = 2000, screen_factor: int = 10,
+        q: float = 0.001, seed: int = 1, epochs: int = 40, ensemble: int = 4, cells=None, z: float = 2.0) -> dict:
+    """Plain vs screened ABC on the five-model batch for each gene-set size in
+    `genes` (one surrogate, trained once on the pipeline's own simulations)."""
+    torch = _torch()
+    cfg = make_config("hour")
+    cells = cells if cells is not None else synthetic_cells(seed=1)
+    prior = factor_prior()
+    rng = np.random.default_rng(seed)
+    out = {"q": q, "screen_factor": screen_factor, "z": z, "runs": []}
+    with Context(cfg, cells) as ctx:
+        ctx.autotune(1, ctx.sample_prior(1, 500, seed + 99, prior)[:, :5], seed=3)
+        # ---- training data: exact simulations the pipeline generates itself
+        t0 = time.perf_counter()
+        th_tr, m_tr = draw(ctx, per_model_train, seed * 1000 + 10, prior, offset=0)
+        st_tr = simulate(ctx, th_tr, m_tr, seed + 1, offset=0)
+        t_gen = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        sg = Surrogate(IN_DIM, ctx.K, ensemble=ensemble, seed=seed + 5)
+        loss = sg.train(surrogate_input(th_tr, m_tr).cpu().numpy(), st_tr.cpu().numpy(), epochs=epochs,
+                        batch=2048, lr=2e-3)
+        t_train = time.perf_counter() - t0
+        out["surrogate"] = {"train_draws": int(th_tr.shape[0]), "epochs": epochs, "final_nll": float(loss[-1]),
+                            "train_seconds": t_train, "data_generation_seconds": t_gen}
+        # ---- plain ABC draws (simulated once, shared by the gene sets)
+        off_plain = 5 * per_model_train
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        th_p, m_p = draw(ctx, per_model_plain, seed * 1000 + 20, prior, offset=off_plain)
+        st_p = simulate(ctx, th_p, m_p, seed + 2, offset=off_plain)
+        t_sim_plain = time.perf_counter() - t0
+        st_host = st_p.cpu().numpy()
+        Pp = th_p.shape[0]
+        x_p = surrogate_input(th_p, m_p)
+        rows = rng.permutation(Pp)
+        cal, hold = np.sort(rows[:Pp // 2]), np.sort(rows[Pp // 2:])
+        x_cal = x_p[torch.from_numpy(cal).cuda()].contiguous()
+        x_hold = x_p[torch.from_numpy(hold).cuda()].contiguous()
+        _, _, dis = sg.predict(x_cal.cpu().numpy())
+        dmax = float(np.quantile(dis, 0.99))
+        for gi, G in enumerate(genes):
+            res = {"genes": G}
+            data, se = make_genes(st_host, G, rng)
+            t0 = time.perf_counter()
+            off, idx, err = ctx.select_device(data, se, st_p.data_ptr(), Pp, 1, q)
+            torch.cuda.synchronize()
+            t_plain = t_sim_plain + (time.perf_counter() - t0)
+            thr = thresholds_from_lists(off, err)
+            below = err < CLIP
+            gene_of = np.repeat(np.arange(G), np.diff(off))[below]
+            p_of = idx[below] - 1
+            acc_plain = int(below.sum())
+            res["informative_genes"] = int((thr >= 0).sum())
+            res["plain"] = {"draws": int(Pp), "accepted_pairs": acc_plain, "seconds": t_plain,
+                            "accepted_per_s": acc_plain / t_plain}
+            # calibration half: multiplicative factor at the 99th percentile of
+            # pred/thr over truly accepted pairs; held-out half: false rejection
+            keep_cal = torch.zeros(cal.shape[0], dtype=torch.uint8, device="cuda")
+            pred = np.zeros((cal.shape[0], G))
+            sg.screen_device(x_cal.data_ptr(), IN_DIM, cal.shape[0], data, se, thr, 0.0, 1e30, keep_cal.data_ptr(),
+                             err_out=pred, z=z)
+            pos = np.full(Pp, -1, np.int64)
+            pos[cal] = np.arange(cal.shape[0])
+            in_cal = pos[p_of] >= 0
+            ratios = pred[pos[p_of[in_cal]], gene_of[in_cal]] / np.maximum(thr[gene_of[in_cal]], 1e-12)
+            ratios = np.where(np.isfinite(ratios), ratios, np.inf)
+            # the 99th percentile of bound / threshold over truly accepted pairs; below 1
+            # when the bound is conservative (the screen then tightens)
+            factor = float(max(0.05, np.quantile(ratios, 0.99))) if ratios.size else 1.0
+            keep_h = torch.zeros(hold.shape[0], dtype=torch.uint8, device="cuda")
+            sg.screen_device(x_hold.data_ptr(), IN_DIM, hold.shape[0], data, se, thr * factor, 0.0, dmax,
+                             keep_h.data_ptr(), z=z)
+            kept = np.zeros(Pp, bool)
+            kept[hold] = keep_h.cpu().numpy().astype(bool)
+            n_hold = int((~in_cal).sum())
+            frr = float((~kept[p_of[~in_cal]]).sum() / max(n_hold, 1))
+            res["calibration"] = {"factor": factor, "disagree_max": dmax, "calibration_pairs": int(in_cal.sum()),
+                                  "held_out_pairs": n_hold, "false_rejection_rate": frr}
+            # warm-up of the whole screened path, then the timed run
+            _screened(ctx, sg, data, se, thr, factor, dmax, 64, prior, seed * 1000 + 40 + gi, 10 ** 8, z)
+            acc, n_sim, n_draw, t_all, t_scr, t_sim = _screened(
+                ctx, sg, data, se, thr, factor, dmax, per_model_plain * screen_factor, prior,
+                seed * 1000 + 30 + gi, off_plain + Pp + gi * 5 * per_model_plain * screen_factor, z)
+            res["screened"] = {"draws": n_draw, "simulated": n_sim, "simulated_fraction": n_sim / n_draw,
+                               "accepted_pairs": acc, "seconds": t_all, "screen_seconds": t_scr,
+                               "ssa_seconds": t_sim, "accepted_per_s": acc / t_all}
+            res["gain_accepted_per_s"] = res["screened"]["accepted_per_s"] / max(res["plain"]["accepted_per_s"],
+                                                                                  1e-30)
+            out["runs"].append(res)
+        sg.close()
+    return out

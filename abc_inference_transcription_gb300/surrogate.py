@@ -98,13 +98,14 @@ class Surrogate:
         return mean, var, dis
 
     def screen_device(self, d_theta: int, ld: int, n: int, data, se, thr, margin: float, disagree_max: float,
-                      d_keep: int, err_out: np.ndarray | None = None) -> int:
+                      d_keep: int, err_out: np.ndarray | None = None, z: float = 2.0) -> int:
         d = np.ascontiguousarray(data, np.float64)
         e = np.ascontiguousarray(se, np.float64)
         t = np.ascontiguousarray(thr, np.float64)
         nk = C.c_int64()
         self._check(self.lib.abc_surrogate_screen_device(self.h, C.c_void_p(d_theta), ld, n, ptr(d), ptr(e),
-                                                         d.shape[0], ptr(t), float(margin), float(disagree_max),
+                                                         d.shape[0], ptr(t), float(margin), float(z),
+                                                         float(disagree_max),
                                                          C.c_void_p(d_keep), C.byref(nk), ptr(err_out)))
         return nk.value
 
@@ -129,15 +130,15 @@ def calibrate_margin(pred_err: np.ndarray, exact_err: np.ndarray, thr: np.ndarra
 
 def calibrate_factor(pred_err: np.ndarray, exact_err: np.ndarray, thr: np.ndarray, quantile: float = 0.99) -> float:
     """Multiplicative margin f (screen keeps pred_err <= f thr) such that a
-    fraction `quantile` of the truly accepted pairs of a calibration set pass.
-    Predicted errors are heavy-tailed, so a ratio calibrates better than a
-    difference."""
+    fraction `quantile` of the truly accepted pairs of a calibration set pass
+    (f < 1 when the screen statistic is conservative).  Predicted errors are
+    heavy-tailed, so a ratio calibrates better than a difference."""
     acc = exact_err <= thr[None, :]
     if not acc.any():
         return 1.0
     ratio = (pred_err / np.maximum(thr[None, :], 1e-12))[acc]
     ratio = np.where(np.isfinite(ratio), ratio, np.inf)
-    return float(max(1.0, np.quantile(ratio, quantile)))
+    return float(max(0.05, np.quantile(ratio, quantile)))
 
 
 def false_rejection_rate(keep: np.ndarray, exact_err: np.ndarray, thr: np.ndarray) -> tuple[float, int]:

@@ -121,6 +121,11 @@ int abc_set_cells(abc_ctx* ctx, int64_t n_cells, const int32_t* cell_cond,
 int abc_sample_prior(abc_ctx* ctx, int model, int64_t n_particles, uint64_t seed,
                      int64_t particle_offset, const abc_prior* prior, double* theta_out);
 
+/* Same draw written to device memory (d_theta_out: P x npar), stream-ordered
+ * on abc_stream(ctx). */
+int abc_sample_prior_device(abc_ctx* ctx, int model, int64_t n_particles, uint64_t seed,
+                            int64_t particle_offset, const abc_prior* prior, double* d_theta_out);
+
 /* Simulate particles and return their statistics, abc_sim
  * (scripts/abc_simulation.jl:13-62; the per-particle loop at :88-97).
  * theta: P x npar (log10 rates), stats_out: P x nstats.  Particle p uses the
@@ -218,6 +223,9 @@ int abc_errors_select_device(abc_ctx* ctx, const double* data, const double* se,
 int abc_accept_fetch(abc_ctx* ctx, int64_t* gene_offsets, int64_t* particle_idx, double* err);
 /* Counters of the last selection: FP32 candidates rechecked in FP64. */
 int abc_select_counters(const abc_ctx* ctx, int64_t* candidates, int64_t* rechecked);
+/* With abc_profile on: device milliseconds of the FP32 candidate-pass kernel
+ * of the last selection, summed over its passes, and the number of passes. */
+int abc_select_profile_read(const abc_ctx* ctx, double* fast_ms, int* fast_passes);
 
 /* ------------------------------------------------------------------------
  * Learned pre-screen.  No reference counterpart: the reference simulates
@@ -252,15 +260,15 @@ int abc_surrogate_predict(abc_surrogate* s, const double* theta, int64_t n, doub
                           double* disagree);
 int abc_surrogate_predict_device(abc_surrogate* s, const double* d_theta, int ld_theta, int64_t n,
                                  double* d_mean, double* d_var, double* d_disagree);
-/* d_keep[p] = 1 for the draws to simulate exactly: min(10, sum_k w ((d - mu)^2
- * + aleatoric var) / K) <= thr[g] + margin for some gene, or disagreement >
- * disagree_max (epistemic uncertainty is handled by that rule, not by the
- * error).  data, se: G x n_stats
- * (host), thr: per-gene error threshold (host), margin added to it.
- * err_out (host, n x G, optional, small n only): predicted expected errors. */
+/* d_keep[p] = 1 for the draws to simulate exactly: the lower confidence
+ * bound sum_k w max(0, |d - mu| - z sd)^2 / K of the error (mu, sd: predicted
+ * mean and total predictive std of each statistic) is <= thr[g] + margin for
+ * some gene, or the disagreement exceeds disagree_max.  data, se: G x n_stats
+ * (host), thr: per-gene error threshold (host).  err_out (host, n x G,
+ * optional, small n only): the bounds, for calibration. */
 int abc_surrogate_screen_device(abc_surrogate* s, const double* d_theta, int ld_theta, int64_t n,
                                 const double* data, const double* se, int64_t n_genes, const double* thr,
-                                double margin, double disagree_max, uint8_t* d_keep, int64_t* n_keep,
+                                double margin, double z, double disagree_max, uint8_t* d_keep, int64_t* n_keep,
                                 double* err_out);
 /* Survivors of a screen in ascending order: rows with d_keep != 0 copied from
  * d_theta (row stride ld_theta) to d_theta_out and their indices to d_idx_out

@@ -117,3 +117,19 @@ def test_screen_gain_at_calibrated_false_rejection(mods):
     assert n_acc > 50, info
     assert frr <= 0.03, info
     assert frac < 0.5, info   # >= 2x fewer exact simulations per accepted particle
+
+
+def test_screened_pipeline_small(mods):
+    """End-to-end five-model run at a small size: plain ABC, surrogate trained on
+    the pipeline's own exact simulations, calibrated screen, screened ABC with
+    the plain run's per-gene thresholds."""
+    pytest.importorskip("torch")
+    from abc_inference_transcription_gb300 import pipeline
+    out = pipeline.run(genes=(8,), per_model_train=12000, per_model_plain=1500, screen_factor=4, q=0.01, seed=3,
+                       epochs=30)
+    res = out["runs"][0]
+    assert res["plain"]["accepted_pairs"] > 0, res
+    assert res["screened"]["draws"] == 4 * res["plain"]["draws"]
+    assert 0.0 <= res["calibration"]["false_rejection_rate"] <= 0.05, res
+    assert res["screened"]["simulated_fraction"] < 0.6, res
+    assert res["screened"]["accepted_pairs"] > 0, res
