@@ -155,6 +155,10 @@ def _declare(lib: C.CDLL) -> None:
         "abc_accept_fetch": (C.c_int, [vp, i64p, i64p, dp]),
         "abc_select_counters": (C.c_int, [vp, i64p, i64p]),
         "abc_select_profile_read": (C.c_int, [vp, dp, C.POINTER(C.c_int)]),
+        "abc_set_distance_mode": (C.c_int, [vp, C.c_int]),
+        "abc_get_distance_mode": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "abc_errors_candidate": (C.c_int, [vp, dp, dp, C.c_int64, C.c_int, C.c_int, C.POINTER(C.c_int32), dp,
+                                           C.c_int64, C.POINTER(C.c_float), dp, dp, C.POINTER(C.c_int)]),
     }
     sp = vp
     sig.update({
@@ -187,7 +191,8 @@ ABI_SYMBOLS = [
     "abc_synchronize", "abc_simulate_batch", "abc_simulate_batch_device", "abc_simulate_noalloc", "abc_simulate_cells", "abc_last_counters",
     "abc_profile", "abc_profile_read", "abc_autotune", "abc_set_variant", "abc_errors",
     "abc_errors_select", "abc_errors_select_thr", "abc_errors_select_device", "abc_accept_fetch",
-    "abc_select_counters", "abc_select_profile_read",
+    "abc_select_counters", "abc_select_profile_read", "abc_set_distance_mode", "abc_get_distance_mode",
+    "abc_errors_candidate",
     "abc_surrogate_create", "abc_surrogate_destroy", "abc_surrogate_last_error", "abc_surrogate_num_params",
     "abc_surrogate_train", "abc_surrogate_gradients", "abc_surrogate_get_params", "abc_surrogate_set_params",
     "abc_surrogate_get_norm", "abc_surrogate_set_norm", "abc_surrogate_predict", "abc_surrogate_predict_device",

@@ -28,6 +28,7 @@ UNITS = {
     "kernels_fp32.cu": [],
     "distance_fp64.cu": ["-fmad=false"],
     "distance_fp32.cu": [],
+    "distance_tc.cu": [],
     "noalloc.cu": [],
     "mlp.cu": [],
     "surrogate.cu": [],

@@ -80,6 +80,16 @@ struct abc_ctx {
   DBuf<double> d_data, d_se, d_sel_stats, d_e64, d_se64, d_out_err;
   DBuf<float> d_sw, d_dw, d_s32, d_X, d_esub;
   DBuf<Cand> d_cand;
+  DBuf<float> d_cande;  // FP32 error of each candidate
+  // tensor-core candidate pass: operands, per-gene terms, per-CTA output segments
+  int dist_mode = 2;       // 0 FP32 CUDA cores, 1 TF32 one-term, 2 TF32 three-term
+  int dist_mode_used = -1;
+  DBuf<float> d_tcA, d_tcB, d_cg32, d_b0, d_Y, d_Xt, d_seg_e;
+  DBuf<double> d_cg64;
+  DBuf<unsigned> d_tcflags, d_segcount, d_hist;
+  DBuf<int> d_tcerr;
+  DBuf<Cand> d_seg, d_cand2;
+  int64_t seg_cap = int64_t(1) << 16;
   DBuf<int32_t> d_sp;
   DBuf<int64_t> d_gcount, d_goff, d_alen, d_aoff, d_out_idx;
   DBuf<unsigned long long> d_gcursor, d_ncand;
@@ -89,7 +99,7 @@ struct abc_ctx {
   double sel_fast_ms = 0.0;  // candidate-pass kernel time of the last selection (abc_profile)
   int sel_fast_passes = 0;
   int64_t cand_cap = int64_t(1) << 22;
-  int64_t sel_G = 0, sel_total = 0, sel_cands = 0, sel_rechecked = 0;
+  int64_t sel_G = 0, sel_total = 0, sel_cands = 0, sel_rechecked = 0, sel_cands_emitted = 0;
   bool sel_ready = false;
 };
 
@@ -203,6 +213,9 @@ int abc_destroy(abc_ctx* c) {
   c->d_data.release(); c->d_se.release(); c->d_sel_stats.release(); c->d_e64.release(); c->d_se64.release();
   c->d_out_err.release(); c->d_sw.release(); c->d_dw.release(); c->d_s32.release(); c->d_X.release();
   c->d_esub.release(); c->d_cand.release(); c->d_sp.release(); c->d_gcount.release(); c->d_goff.release();
+  c->d_cande.release(); c->d_tcA.release(); c->d_tcB.release(); c->d_cg32.release(); c->d_b0.release();
+  c->d_Y.release(); c->d_Xt.release(); c->d_seg_e.release(); c->d_cg64.release(); c->d_tcflags.release();
+  c->d_segcount.release(); c->d_hist.release(); c->d_tcerr.release(); c->d_seg.release(); c->d_cand2.release();
   c->d_alen.release(); c->d_aoff.release(); c->d_out_idx.release(); c->d_gcursor.release();
   c->d_ncand.release(); c->d_fail.release(); c->d_thr.release();
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
@@ -701,40 +714,162 @@ int abc_errors(abc_ctx* c, const double* data, const double* se, int64_t G, int 
   return ABC_OK;
 }
 
-// candidate pass with capacity handling; returns candidate count in *n
-static int candidate_pass(abc_ctx* c, const DistInputs& in, int64_t* n) {
+static const int64_t kCandLimit = int64_t(1) << 28;  // candidates carry 12 B plus 20 B in the recheck and sort
+
+static int prof_begin(abc_ctx* c) {
+  if (c->prof && !c->sel_ev[0]) {
+    CK(cudaEventCreate(&c->sel_ev[0]));
+    CK(cudaEventCreate(&c->sel_ev[1]));
+  }
+  if (c->prof) CK(cudaEventRecord(c->sel_ev[0], c->stream));
+  return ABC_OK;
+}
+
+static int prof_end(abc_ctx* c) {
+  if (!c->prof) return ABC_OK;
+  CK(cudaEventRecord(c->sel_ev[1], c->stream));
+  CK(cudaEventSynchronize(c->sel_ev[1]));
+  float ms = 0.0f;
+  CK(cudaEventElapsedTime(&ms, c->sel_ev[0], c->sel_ev[1]));
+  c->sel_fast_ms += ms;
+  c->sel_fast_passes += 1;
+  return ABC_OK;
+}
+
+// FP32 candidate pass on the CUDA cores; candidates and their FP32 errors in
+// d_cand / d_cande, count in *n.
+static int candidate_pass_simt(abc_ctx* c, const DistInputs& in, int64_t* n) {
   for (int attempt = 0; attempt < 2; ++attempt) {
     CK(c->d_cand.ensure((size_t)c->cand_cap));
+    CK(c->d_cande.ensure((size_t)c->cand_cap));
     CK(cudaMemsetAsync(c->d_ncand.p, 0, sizeof(unsigned long long), c->stream));
-    if (c->prof && !c->sel_ev[0]) {
-      CK(cudaEventCreate(&c->sel_ev[0]));
-      CK(cudaEventCreate(&c->sel_ev[1]));
-    }
-    if (c->prof) CK(cudaEventRecord(c->sel_ev[0], c->stream));
-    CK(launch_dist_fast(c->d_s32.p, c->d_sw.p, c->d_dw.p, in.P, in.G, in.K, c->d_X.p, c->d_cand.p, c->d_ncand.p,
-                        c->cand_cap, nullptr, 0, 0, c->stream));
-    if (c->prof) CK(cudaEventRecord(c->sel_ev[1], c->stream));
+    int st = prof_begin(c);
+    if (st) return st;
+    CK(launch_dist_fast(c->d_s32.p, c->d_sw.p, c->d_dw.p, in.P, in.G, in.K, c->d_X.p, c->d_cand.p, c->d_cande.p,
+                        c->d_ncand.p, c->cand_cap, nullptr, 0, 0, c->stream));
+    st = prof_end(c);
+    if (st) return st;
     unsigned long long h = 0;
     CK(cudaMemcpyAsync(&h, c->d_ncand.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    if (c->prof) {
-      float ms = 0.0f;
-      CK(cudaEventElapsedTime(&ms, c->sel_ev[0], c->sel_ev[1]));
-      c->sel_fast_ms += ms;
-      c->sel_fast_passes += 1;
-    }
     if ((int64_t)h <= c->cand_cap) {
       *n = (int64_t)h;
       return ABC_OK;
     }
-    // candidates carry 8 B each plus 20 B in the recheck and sort buffers
-    const int64_t limit = int64_t(1) << 28;
-    if ((int64_t)h > limit)
+    if ((int64_t)h > kCandLimit)
       return fail(c, ABC_ERR_CAPACITY,
                   "more than 2^28 candidates (a threshold at the clip value 10 ties too many particles)");
     c->cand_cap = (int64_t)h + (int64_t)h / 8 + 1024;
   }
   return fail(c, ABC_ERR_CAPACITY, "candidate buffer overflow");
+}
+
+// Tensor-core candidate pass: each CTA appends to its own segment; the
+// segments are concatenated into d_cand / d_cande.
+static int candidate_pass_tc(abc_ctx* c, const DistInputs& in, int nh, int64_t* n) {
+  const int grid = tc_grid(in.P, in.G, c->sms);
+  const int KA = tc_ka(in.K);
+  CK(launch_tc_y(c->d_X.p, c->d_cg64.p, in.G, in.K, c->d_Y.p, c->stream));
+  CK(c->d_segcount.ensure((size_t)grid));
+  CK(c->d_tcerr.ensure(1));
+  std::vector<unsigned> cnt((size_t)grid);
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    CK(c->d_seg.ensure((size_t)grid * (size_t)c->seg_cap));
+    CK(c->d_seg_e.ensure((size_t)grid * (size_t)c->seg_cap));
+    CK(cudaMemsetAsync(c->d_segcount.p, 0, sizeof(unsigned) * grid, c->stream));
+    CK(cudaMemsetAsync(c->d_tcerr.p, 0, sizeof(int), c->stream));
+    TcArgs a;
+    a.P = in.P;
+    a.G = in.G;
+    a.K = in.K;
+    a.KA = KA;
+    a.n_chunks = KA / 32;
+    a.nM = (int)((in.P + 127) / 128);
+    a.nN = (int)((in.G + 255) / 256);
+    a.Y = c->d_Y.p;
+    a.cg = c->d_cg32.p;
+    a.cand = c->d_seg.p;
+    a.cand_e = c->d_seg_e.p;
+    a.seg_cap = c->seg_cap;
+    a.seg_count = c->d_segcount.p;
+    a.err = c->d_tcerr.p;
+    int st = prof_begin(c);
+    if (st) return st;
+    CK(launch_dist_tc(nh, c->d_tcA.p, c->d_tcB.p, a, grid, c->stream));
+    st = prof_end(c);
+    if (st) return st;
+    int herr = 0;
+    CK(cudaMemcpyAsync(cnt.data(), c->d_segcount.p, sizeof(unsigned) * grid, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&herr, c->d_tcerr.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (herr)
+      return fail(c, ABC_ERR_CUDA,
+                  "tensor-core distance pass: a bounded wait ran out (code " + std::to_string(herr) + ")");
+    int64_t total = 0, mx = 0;
+    for (int b = 0; b < grid; ++b) {
+      total += cnt[b];
+      mx = std::max<int64_t>(mx, cnt[b]);
+    }
+    if (total > kCandLimit)
+      return fail(c, ABC_ERR_CAPACITY,
+                  "more than 2^28 candidates (a threshold at the clip value 10 ties too many particles)");
+    if (mx <= c->seg_cap) {
+      CK(c->d_cand.ensure((size_t)std::max<int64_t>(total, 1)));
+      CK(c->d_cande.ensure((size_t)std::max<int64_t>(total, 1)));
+      CK(launch_tc_gather(c->d_seg.p, c->d_seg_e.p, c->d_segcount.p, grid, c->seg_cap, c->d_cand.p, c->d_cande.p,
+                          c->stream));
+      *n = total;
+      return ABC_OK;
+    }
+    c->seg_cap = mx + mx / 4 + 1024;
+  }
+  return fail(c, ABC_ERR_CAPACITY, "candidate segment overflow");
+}
+
+// Operands of the candidate pass and its error bound |e32 - e| <= b0[g] + b1 e.
+// Tensor cores (the requested mode) unless an operand is infinite or w s^2
+// could leave the FP32 range; then the FP32 CUDA-core pass.
+static int prepare_candidate_pass(abc_ctx* c, const DistInputs& in, int* dmode_out, float* b1_out) {
+  const int64_t G = in.G, P = in.P;
+  const int K = in.K;
+  CK(c->d_sw.ensure((size_t)G * K));
+  CK(c->d_dw.ensure((size_t)G * K));
+  CK(c->d_s32.ensure((size_t)P * K));
+  CK(c->d_b0.ensure((size_t)G));
+  CK(launch_dist_prep(in, c->d_sw.p, c->d_dw.p, c->d_s32.p, c->stream));
+  int dmode = c->dist_mode;
+  float b1 = 0.0f;
+  if (dmode) {
+    const int KA = tc_ka(K);
+    CK(c->d_tcA.ensure((size_t)P * dmode * KA));
+    CK(c->d_tcB.ensure((size_t)G * dmode * KA));
+    CK(c->d_cg64.ensure((size_t)G));
+    CK(c->d_cg32.ensure((size_t)G));
+    CK(c->d_Y.ensure((size_t)G));
+    CK(c->d_tcflags.ensure(3));
+    CK(cudaMemsetAsync(c->d_tcflags.p, 0, sizeof(unsigned) * 3, c->stream));
+    const double beta = tc_beta(K, dmode);
+    CK(launch_tc_prep(in, dmode, beta, c->d_tcA.p, c->d_tcB.p, c->d_cg64.p, c->d_cg32.p, c->d_b0.p,
+                      c->d_tcflags.p, c->stream));
+    unsigned fl[3];
+    CK(cudaMemcpyAsync(fl, c->d_tcflags.p, sizeof(fl), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    float maxw, maxs2;
+    memcpy(&maxw, &fl[1], 4);
+    memcpy(&maxs2, &fl[2], 4);
+    if (fl[0] || (double)maxw * (double)maxs2 * (4.0 * K) > 1e37) dmode = 0;
+    else b1 = (float)(4.0 * beta);
+  }
+  if (dmode == 0) {
+    // 1.5 u (64 sqrt(e) + (K + 8) e) <= 48 u + 1.5 u (K + 40) e, u = 2^-24
+    const double u = 5.9604644775390625e-08;
+    b1 = (float)(1.5 * u * (K + 40));
+    CK(launch_fill(c->d_b0.p, G, (float)(48.0 * u), c->stream));
+  }
+  c->dist_mode_used = dmode;
+  *dmode_out = dmode;
+  *b1_out = b1;
+  return ABC_OK;
 }
 
 // mode 0: err <= eps; mode 1: top ceil(q P) per gene; mode 2: err <= thr[g] per gene
@@ -756,9 +891,6 @@ static int select_impl(abc_ctx* c, const double* data, const double* se, int64_t
   if (st) return st;
   CK(c->d_thr.ensure((size_t)G));
   if (mode == 2) CK(cudaMemcpyAsync(c->d_thr.p, thr, sizeof(double) * G, cudaMemcpyHostToDevice, c->stream));
-  CK(c->d_sw.ensure((size_t)G * K));
-  CK(c->d_dw.ensure((size_t)G * K));
-  CK(c->d_s32.ensure((size_t)P * K));
   CK(c->d_X.ensure((size_t)G));
   CK(c->d_ncand.ensure(1));
   CK(c->d_gcount.ensure((size_t)G));
@@ -769,25 +901,14 @@ static int select_impl(abc_ctx* c, const double* data, const double* se, int64_t
   CK(c->d_fail.ensure((size_t)G));
   c->sel_fast_ms = 0.0;
   c->sel_fast_passes = 0;
-  CK(launch_dist_prep(in, c->d_sw.p, c->d_dw.p, c->d_s32.p, c->stream));
+  int dmode = 0;
+  float b1 = 0.0f;
+  st = prepare_candidate_pass(c, in, &dmode, &b1);
+  if (st) return st;
   const int64_t kq = mode == 1 ? (int64_t)std::ceil(eps_or_q * (double)P) : 0;
   std::vector<float> hX((size_t)G);
   if (mode == 0 || mode == 2) {
-    for (int64_t g = 0; g < G; ++g) {
-      const double ev = mode == 0 ? eps_or_q : thr[g];
-      float x;
-      if (ev >= 10.0) {
-        x = INFINITY;
-      } else if (ev < 0.0) {
-        x = -1.0f;
-      } else {
-        const float e = (float)ev;
-        x = e + 2.0f * dist_bound(e, K);
-        x = std::nextafter(x, INFINITY);
-      }
-      hX[g] = x;
-    }
-    CK(cudaMemcpyAsync(c->d_X.p, hX.data(), sizeof(float) * G, cudaMemcpyHostToDevice, c->stream));
+    CK(launch_x_from_thr(mode == 2 ? c->d_thr.p : nullptr, eps_or_q, G, c->d_b0.p, b1, c->d_X.p, c->stream));
   } else {
     // thresholds from a strided subsample
     const int64_t n_sub = std::min<int64_t>(P, 32768);
@@ -798,28 +919,47 @@ static int select_impl(abc_ctx* c, const double* data, const double* se, int64_t
       CK(cudaMemcpyAsync(c->d_X.p, hX.data(), sizeof(float) * G, cudaMemcpyHostToDevice, c->stream));
     } else {
       CK(c->d_esub.ensure((size_t)n_sub * G));
-      CK(launch_dist_fast(c->d_s32.p, c->d_sw.p, c->d_dw.p, P, G, K, nullptr, nullptr, nullptr, 0, c->d_esub.p,
-                          stride, n_sub, c->stream));
-      CK(launch_dist_threshold(c->d_esub.p, n_sub, G, k_sub, K, c->d_X.p, c->stream));
+      CK(launch_dist_fast(c->d_s32.p, c->d_sw.p, c->d_dw.p, P, G, K, nullptr, nullptr, nullptr, nullptr, 0,
+                          c->d_esub.p, stride, n_sub, c->stream));
+      CK(launch_dist_threshold(c->d_esub.p, n_sub, G, k_sub, c->d_b0.p, b1, c->d_X.p, c->stream));
       CK(cudaMemcpyAsync(hX.data(), c->d_X.p, sizeof(float) * G, cudaMemcpyDeviceToHost, c->stream));
     }
   }
   int64_t ncand = 0;
   c->sel_rechecked = 0;
+  c->sel_cands_emitted = 0;
   for (int round = 0; round < 4; ++round) {
-    st = candidate_pass(c, in, &ncand);
+    st = dmode ? candidate_pass_tc(c, in, dmode, &ncand) : candidate_pass_simt(c, in, &ncand);
     if (st) return st;
-    CK(c->d_e64.ensure((size_t)ncand));
-    CK(c->d_se64.ensure((size_t)ncand));
-    CK(c->d_sp.ensure((size_t)ncand));
-    CK(launch_dist_recheck(in, c->d_cand.p, ncand, c->d_e64.p, c->stream));
-    CK(launch_dist_group_sort(c->d_cand.p, c->d_e64.p, ncand, G, c->d_gcount.p, c->d_goff.p, c->d_sp.p,
-                              c->d_se64.p, c->d_gcursor.p, c->stream));
+    const Cand* rc = c->d_cand.p;
+    const float* Xacc = c->d_X.p;
+    int64_t nre = ncand;
+    if (mode == 1) {
+      // only candidates that can still be among the k smallest go to the FP64 recheck
+      CK(c->d_hist.ensure((size_t)G * kHistBins));
+      CK(c->d_Xt.ensure((size_t)G));
+      CK(c->d_cand2.ensure((size_t)std::max<int64_t>(ncand, 1)));
+      CK(launch_refine(c->d_cand.p, c->d_cande.p, ncand, G, kq, c->d_X.p, c->d_b0.p, b1, c->d_hist.p, c->d_Xt.p,
+                       c->d_cand2.p, c->d_ncand.p, c->stream));
+      unsigned long long h = 0;
+      CK(cudaMemcpyAsync(&h, c->d_ncand.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+      nre = (int64_t)h;
+      rc = c->d_cand2.p;
+      Xacc = c->d_Xt.p;
+    }
+    CK(c->d_e64.ensure((size_t)std::max<int64_t>(nre, 1)));
+    CK(c->d_se64.ensure((size_t)std::max<int64_t>(nre, 1)));
+    CK(c->d_sp.ensure((size_t)std::max<int64_t>(nre, 1)));
+    CK(launch_dist_recheck(in, rc, nre, c->d_e64.p, c->stream));
+    CK(launch_dist_group_sort(rc, c->d_e64.p, nre, G, c->d_gcount.p, c->d_goff.p, c->d_sp.p, c->d_se64.p,
+                              c->d_gcursor.p, c->stream));
     CK(cudaMemsetAsync(c->d_fail.p, 0, sizeof(int) * G, c->stream));
     CK(launch_dist_accept_len(c->d_goff.p, c->d_se64.p, G, mode == 2 ? 0 : mode, eps_or_q,
-                              mode == 2 ? c->d_thr.p : nullptr, kq, c->d_X.p, K, c->d_alen.p, c->d_fail.p,
+                              mode == 2 ? c->d_thr.p : nullptr, kq, Xacc, c->d_b0.p, b1, c->d_alen.p, c->d_fail.p,
                               c->stream));
-    c->sel_rechecked += ncand;
+    c->sel_cands_emitted += ncand;
+    c->sel_rechecked += nre;
     if (mode != 1) break;
     std::vector<int> hf((size_t)G);
     CK(cudaMemcpyAsync(hf.data(), c->d_fail.p, sizeof(int) * G, cudaMemcpyDeviceToHost, c->stream));
@@ -846,7 +986,7 @@ static int select_impl(abc_ctx* c, const double* data, const double* se, int64_t
   CK(cudaStreamSynchronize(c->stream));
   c->sel_G = G;
   c->sel_total = total;
-  c->sel_cands = ncand;
+  c->sel_cands = c->sel_cands_emitted;
   c->sel_ready = true;
   if (n_accepted_total) *n_accepted_total = total;
   return ABC_OK;
@@ -871,6 +1011,43 @@ int abc_errors_select_device(abc_ctx* c, const double* data, const double* se, i
   return select_impl(c, data, se, G, K, n_fam, fam, d_stats, true, P, mode, eps_or_q, thr, n_accepted_total);
 }
 
+int abc_errors_candidate(abc_ctx* c, const double* data, const double* se, int64_t G, int K, int n_fam,
+                         const int32_t* fam, const double* stats, int64_t P, float* err_out, double* b0_out,
+                         double* b1_out, int* mode_used) {
+  if (!c) return ABC_ERR_INVALID;
+  if (!err_out) return fail(c, ABC_ERR_INVALID, "abc_errors_candidate: null output");
+  if (P * G > kCandLimit) return fail(c, ABC_ERR_INVALID, "abc_errors_candidate: P G must be <= 2^28");
+  DistInputs in;
+  int st = load_dist_inputs(c, data, se, G, K, n_fam, fam, stats, P, in);
+  if (st) return st;
+  int dmode = 0;
+  float b1 = 0.0f;
+  st = prepare_candidate_pass(c, in, &dmode, &b1);
+  if (st) return st;
+  CK(c->d_X.ensure((size_t)G));
+  CK(c->d_ncand.ensure(1));
+  CK(launch_fill(c->d_X.p, G, INFINITY, c->stream));
+  int64_t n = 0;
+  c->cand_cap = std::max<int64_t>(c->cand_cap, P * G);
+  st = dmode ? candidate_pass_tc(c, in, dmode, &n) : candidate_pass_simt(c, in, &n);
+  if (st) return st;
+  DBuf<float> out;
+  CK(out.ensure((size_t)P * G));
+  CK(launch_fill(out.p, P * G, NAN, c->stream));
+  CK(launch_scatter_errors(c->d_cand.p, c->d_cande.p, n, G, out.p, c->stream));
+  cudaError_t e = cudaMemcpyAsync(err_out, out.p, sizeof(float) * P * G, cudaMemcpyDeviceToHost, c->stream);
+  std::vector<float> hb0((size_t)G);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hb0.data(), c->d_b0.p, sizeof(float) * G, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  out.release();
+  if (e != cudaSuccess) return cuda_fail(c, e, "abc_errors_candidate");
+  if (b0_out)
+    for (int64_t g = 0; g < G; ++g) b0_out[g] = hb0[g];
+  if (b1_out) *b1_out = b1;
+  if (mode_used) *mode_used = dmode;
+  return ABC_OK;
+}
+
 int abc_accept_fetch(abc_ctx* c, int64_t* gene_offsets, int64_t* particle_idx, double* err) {
   if (!c) return ABC_ERR_INVALID;
   if (!c->sel_ready) return fail(c, ABC_ERR_STATE, "no selection result: call abc_errors_select first");
@@ -890,6 +1067,20 @@ int abc_select_profile_read(const abc_ctx* c, double* fast_ms, int* fast_passes)
   if (!c) return ABC_ERR_INVALID;
   if (fast_ms) *fast_ms = c->sel_fast_ms;
   if (fast_passes) *fast_passes = c->sel_fast_passes;
+  return ABC_OK;
+}
+
+int abc_set_distance_mode(abc_ctx* c, int mode) {
+  if (!c) return ABC_ERR_INVALID;
+  if (mode < 0 || mode > 2) return fail(c, ABC_ERR_INVALID, "distance mode must be 0, 1 or 2");
+  c->dist_mode = mode;
+  return ABC_OK;
+}
+
+int abc_get_distance_mode(const abc_ctx* c, int* requested, int* used) {
+  if (!c) return ABC_ERR_INVALID;
+  if (requested) *requested = c->dist_mode;
+  if (used) *used = c->dist_mode_used;
   return ABC_OK;
 }
 

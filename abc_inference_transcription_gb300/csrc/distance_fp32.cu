@@ -13,8 +13,8 @@ __global__ void __launch_bounds__(256) dist_fast_kernel(const float* __restrict_
                                                         const float* __restrict__ sw,
                                                         const float* __restrict__ dw, int64_t P, int64_t G,
                                                         int K, const float* __restrict__ X, Cand* cand,
-                                                        unsigned long long* n_cand, int64_t cap, float* esub,
-                                                        int64_t stride, int64_t n_sub) {
+                                                        float* cand_e, unsigned long long* n_cand, int64_t cap,
+                                                        float* esub, int64_t stride, int64_t n_sub) {
   __shared__ float ss[kDistKc][kDistTile];
   __shared__ float sa[kDistKc][kDistTile];
   __shared__ float sd[kDistKc][kDistTile];
@@ -92,6 +92,7 @@ __global__ void __launch_bounds__(256) dist_fast_kernel(const float* __restrict_
           c.p = (int32_t)row;
           c.g = (int32_t)g;
           cand[slot] = c;
+          if (cand_e) cand_e[slot] = e;
         }
       }
     }
@@ -99,20 +100,50 @@ __global__ void __launch_bounds__(256) dist_fast_kernel(const float* __restrict_
 }
 
 cudaError_t launch_dist_fast(const float* s32, const float* sw, const float* dw, int64_t P, int64_t G, int K,
-                             const float* X, Cand* cand, unsigned long long* n_cand, int64_t cap,
+                             const float* X, Cand* cand, float* cand_e, unsigned long long* n_cand, int64_t cap,
                              float* esub, int64_t stride, int64_t n_sub, cudaStream_t s) {
   const int64_t rows = esub ? n_sub : P;
   if (rows <= 0 || G <= 0) return cudaSuccess;
   dim3 grid((unsigned)((G + kDistTile - 1) / kDistTile), (unsigned)((rows + kDistTile - 1) / kDistTile));
-  dist_fast_kernel<<<grid, 256, 0, s>>>(s32, sw, dw, P, G, K, X, cand, n_cand, cap, esub, stride, n_sub);
+  dist_fast_kernel<<<grid, 256, 0, s>>>(s32, sw, dw, P, G, K, X, cand, cand_e, n_cand, cap, esub, stride, n_sub);
   return cudaGetLastError();
+}
+
+// Cumulative histogram search shared by the threshold and refinement kernels:
+// the first bin at which the running count of hist[0..kHistBins) reaches k
+// (-1 if it never does).  One CTA of 256 threads; csum is 256 words of shared memory.
+__device__ int hist_find(const unsigned int* hist, int64_t k, unsigned int* csum) {
+  const int per = kHistBins / 256;
+  unsigned int local = 0;
+  for (int b = 0; b < per; ++b) local += hist[threadIdx.x * per + b];
+  csum[threadIdx.x] = local;
+  __syncthreads();
+  int found = -1;
+  if (threadIdx.x == 0) {
+    unsigned long long run = 0;
+    for (int t = 0; t < 256 && found < 0; ++t) {
+      if (run + csum[t] >= (unsigned long long)k) {
+        for (int b = 0; b < per; ++b) {
+          run += hist[t * per + b];
+          if (run >= (unsigned long long)k) {
+            found = t * per + b;
+            break;
+          }
+        }
+      } else {
+        run += csum[t];
+      }
+    }
+  }
+  return found;  // meaningful in thread 0
 }
 
 // One CTA per gene: histogram of the subsample errors on a sqrt scale, then
 // the bin where the running count reaches k_sub gives X[g] (its upper edge
-// widened by twice the FP32 error bound).
+// widened by twice the error bound b0_g + b1 e of the candidate pass).
 __global__ void __launch_bounds__(256) dist_threshold_kernel(const float* __restrict__ esub, int64_t n_sub,
-                                                             int64_t G, int64_t k_sub, int K, float* X) {
+                                                             int64_t G, int64_t k_sub, const float* b0, float b1,
+                                                             float* X) {
   __shared__ unsigned int hist[kHistBins];
   __shared__ unsigned int csum[256];
   const int64_t g = blockIdx.x;
@@ -123,48 +154,152 @@ __global__ void __launch_bounds__(256) dist_threshold_kernel(const float* __rest
     if (e == e) atomicAdd(&hist[hist_bin(e)], 1u);
   }
   __syncthreads();
-  // per-thread chunk sums (16 bins each) and an exclusive scan by thread 0
-  const int per = kHistBins / 256;
-  unsigned int local = 0;
-  for (int b = 0; b < per; ++b) local += hist[threadIdx.x * per + b];
-  csum[threadIdx.x] = local;
-  __syncthreads();
+  const int found = hist_find(hist, k_sub, csum);
   if (threadIdx.x == 0) {
-    unsigned long long run = 0;
-    int found = -1;
-    for (int t = 0; t < 256 && found < 0; ++t) {
-      if (run + csum[t] >= (unsigned long long)k_sub) {
-        for (int b = 0; b < per; ++b) {
-          run += hist[t * per + b];
-          if (run >= (unsigned long long)k_sub) {
-            found = t * per + b;
-            break;
-          }
-        }
-      } else {
-        run += csum[t];
-      }
-    }
     float x;
     if (found < 0 || k_sub <= 0) {
       x = INFINITY;
     } else {
-      float up = hist_upper(found);
-      float xp = up + 1.01f * dist_bound_f(up, K);
-      x = xp + 1.01f * dist_bound_f(xp, K);
+      const float bg = b0[g];
+      const float up = hist_upper(found);
+      const float xp = up + 1.01f * (bg + b1 * up);
+      x = xp + 1.01f * (bg + b1 * xp);
     }
     X[g] = x;
   }
 }
 
-cudaError_t launch_dist_threshold(const float* esub, int64_t n_sub, int64_t G, int64_t k_sub, int K, float* X,
-                                  cudaStream_t s) {
+cudaError_t launch_dist_threshold(const float* esub, int64_t n_sub, int64_t G, int64_t k_sub, const float* b0,
+                                  float b1, float* X, cudaStream_t s) {
   if (G <= 0) return cudaSuccess;
-  dist_threshold_kernel<<<(unsigned)G, 256, 0, s>>>(esub, n_sub, G, k_sub, K, X);
+  dist_threshold_kernel<<<(unsigned)G, 256, 0, s>>>(esub, n_sub, G, k_sub, b0, b1, X);
   return cudaGetLastError();
 }
 
-float dist_bound(float e, int K) { return dist_bound_f(e, K); }
+// ---------------------------------------------------------------------------
+// thresholds of the candidate pass and the refinement before the FP64 recheck
+// ---------------------------------------------------------------------------
+
+__global__ void fill_kernel(float* x, int64_t n, float v) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = v;
+}
+
+cudaError_t launch_fill(float* x, int64_t n, float v, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, n, v);
+  return cudaGetLastError();
+}
+
+// X_g for an error threshold e_g (eps, or thr[g]): every pair with err <= e_g
+// has a candidate-pass error <= e_g + B_g(e_g) <= X_g = e_g + 2 B_g(e_g)
+// (e_g rounded up to FP32 first).  e_g >= 10: every finite pair; e_g < 0: none.
+__global__ void x_from_thr_kernel(const double* thr, double eps, int64_t G, const float* b0, float b1, float* X) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= G) return;
+  const double ev = thr ? thr[g] : eps;
+  float x;
+  if (ev >= 10.0) {
+    x = INFINITY;
+  } else if (ev < 0.0) {
+    x = -1.0f;
+  } else {
+    const float e = __double2float_ru(ev);
+    x = __fadd_ru(e, __fmul_ru(2.0f, __fmaf_ru(b1, e, b0[g])));
+  }
+  X[g] = x;
+}
+
+cudaError_t launch_x_from_thr(const double* thr, double eps, int64_t G, const float* b0, float b1, float* X,
+                              cudaStream_t s) {
+  if (G <= 0) return cudaSuccess;
+  x_from_thr_kernel<<<(unsigned)((G + 255) / 256), 256, 0, s>>>(thr, eps, G, b0, b1, X);
+  return cudaGetLastError();
+}
+
+// Histogram of the candidates' FP32 errors per gene (G x kHistBins counters).
+__global__ void cand_hist_kernel(const Cand* cand, const float* e, int64_t n, unsigned int* hist) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float x = e[i];
+    if (x == x) atomicAdd(&hist[(int64_t)cand[i].g * kHistBins + hist_bin(fmaxf(x, 0.0f))], 1u);
+  }
+}
+
+// Per gene: when at least k candidates have an FP32 error <= a (the upper edge
+// of the bin that completes k), k particles have err <= a' = (a + b0)/(1 - b1),
+// so the k smallest errors are <= a', and every particle with err <= a' has an
+// FP32 error <= a' + B(a').  Xt = a' + 2 B(a') keeps them all and passes the
+// acceptance check (Xt - B(Xt) >= a' for b1 <= 1/2).  Xt never exceeds X.
+// Only for a' < 10: at the clip value every particle beyond it ties at 10,
+// whatever its unclipped error, so no tighter threshold is safe there.
+__global__ void __launch_bounds__(256) refine_kernel(const unsigned int* hist, int64_t G, int64_t k, const float* X,
+                                                     const float* b0, float b1, float* Xt) {
+  __shared__ unsigned int csum[256];
+  const int64_t g = blockIdx.x;
+  const int found = hist_find(hist + g * kHistBins, k, csum);
+  if (threadIdx.x == 0) {
+    float x = X[g];
+    if (found >= 0 && k > 0) {
+      const float a = hist_upper(found);
+      if (a < 10.0f) {
+        const float bg = b0[g];
+        const float a1 = __fdiv_ru(__fadd_ru(a, bg), __fsub_rd(1.0f, b1));
+        const float xt = __fadd_ru(a1, __fmul_ru(2.0f, __fmaf_ru(b1, a1, bg)));
+        if (a1 < 10.0f && xt < x) x = xt;
+      }
+    }
+    Xt[g] = x;
+  }
+}
+
+// Keep candidates with e <= Xt[g] (warp-aggregated append).
+__global__ void cand_filter_kernel(const Cand* cand, const float* e, int64_t n, const float* Xt, Cand* out,
+                                   unsigned long long* count) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x; i0 < n; i0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = i0 + threadIdx.x;
+    bool keep = false;
+    Cand cd;
+    if (i < n) {
+      cd = cand[i];
+      keep = e[i] <= Xt[cd.g];
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (m) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(m));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (keep) out[base + __popc(m & ((1u << lane) - 1u))] = cd;
+    }
+  }
+}
+
+__global__ void scatter_errors_kernel(const Cand* cand, const float* e, int64_t n, int64_t G, float* out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[(int64_t)cand[i].p * G + cand[i].g] = e[i];
+}
+
+cudaError_t launch_scatter_errors(const Cand* cand, const float* e, int64_t n, int64_t G, float* out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int blocks = (int)((n + 255) / 256 < 16384 ? (n + 255) / 256 : 16384);
+  scatter_errors_kernel<<<blocks, 256, 0, s>>>(cand, e, n, G, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_refine(const Cand* cand, const float* cand_e, int64_t n, int64_t G, int64_t k, const float* X,
+                          const float* b0, float b1, unsigned int* hist, float* Xt, Cand* out,
+                          unsigned long long* count, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(unsigned int) * (size_t)G * kHistBins, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(count, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  if (G <= 0) return cudaSuccess;
+  const int blocks = (int)((n + 255) / 256 < 16384 ? (n + 255) / 256 : 16384);
+  if (n > 0) cand_hist_kernel<<<blocks, 256, 0, s>>>(cand, cand_e, n, hist);
+  refine_kernel<<<(unsigned)G, 256, 0, s>>>(hist, G, k, X, b0, b1, Xt);
+  if (n > 0) cand_filter_kernel<<<blocks, 256, 0, s>>>(cand, cand_e, n, Xt, out, count);
+  return cudaGetLastError();
+}
+
 
 // Surrogate screen: a lower confidence bound of the error of particle p for
 // gene g under the predicted statistics (mean mu_pk, predictive std sd_pk):

@@ -198,7 +198,8 @@ cudaError_t launch_dist_group_sort(const Cand* cand, const double* e64, int64_t 
 // accepted prefixes
 // ---------------------------------------------------------------------------
 __global__ void accept_len_kernel(const int64_t* goff, const double* se64, int64_t G, int mode, double eps_all,
-                                  const double* eps_g, int64_t k, const float* X, int K, int64_t* alen, int* fail) {
+                                  const double* eps_g, int64_t k, const float* X, const float* b0, float b1,
+                                  int64_t* alen, int* fail) {
   const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= G) return;
   const double eps = eps_g ? eps_g[g] : eps_all;
@@ -229,7 +230,8 @@ __global__ void accept_len_kernel(const int64_t* goff, const double* se64, int64
     } else if (len < k) {
       ok = false;
     } else {
-      const double L = (double)x - (double)dist_bound_f(x, K);
+      // every particle with err <= L had a candidate-pass error <= X
+      const double L = (double)x - ((double)b0[g] + (double)b1 * (double)x);
       ok = E[k - 1] <= L;
     }
     if (!ok) fail[g] = 1;
@@ -238,11 +240,11 @@ __global__ void accept_len_kernel(const int64_t* goff, const double* se64, int64
 }
 
 cudaError_t launch_dist_accept_len(const int64_t* goff, const double* se64, int64_t G, int mode, double eps,
-                                   const double* eps_g, int64_t k, const float* X, int K, int64_t* alen, int* fail,
-                                   cudaStream_t s) {
+                                   const double* eps_g, int64_t k, const float* X, const float* b0, float b1,
+                                   int64_t* alen, int* fail, cudaStream_t s) {
   if (G <= 0) return cudaSuccess;
-  accept_len_kernel<<<(unsigned)((G + 127) / 128), 128, 0, s>>>(goff, se64, G, mode, eps, eps_g, k, X, K, alen,
-                                                                fail);
+  accept_len_kernel<<<(unsigned)((G + 127) / 128), 128, 0, s>>>(goff, se64, G, mode, eps, eps_g, k, X, b0, b1,
+                                                                alen, fail);
   return cudaGetLastError();
 }
 

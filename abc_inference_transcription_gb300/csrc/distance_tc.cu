@@ -1,0 +1,575 @@
+// distance_tc.cu — the particle x gene candidate pass as a TF32 tensor-core
+// GEMM (tcgen05 MMA, accumulators in tensor memory, operands staged by TMA)
+// with a fused candidate epilogue.
+//
+// The reference error (scripts/compute_errors.jl:30-43) of particle p for gene g
+// is (1/K) sum_k w_gk (d_gk - s_pk)^2, w_gk = 1/((se_gk^2 + 0.01 d_gk^2) + eps_gk).
+// Expanded:
+//   K err_pg = c_g + sum_k [ (-2 w_gk d_gk) s_pk + w_gk s_pk^2 ],   c_g = sum_k w_gk d_gk^2,
+// i.e. one GEMM of A = [s | s^2] (particles, K-major rows) against
+// B = [-2 w d | w] (genes, K-major rows) of depth 2K, FP32 accumulation.
+// Three-term mode splits each operand into TF32 hi + lo parts and accumulates
+// hi*hi + hi*lo + lo*hi, so every product is exact to ~2^-21.
+//
+// CTA: 6 warps, one persistent CTA per SM.  Warp 0 issues TMA loads of
+// 128 x 32 (A) and 256 x 32 (B) FP32 boxes with the 128-byte swizzle into a
+// ring of shared-memory stages; warp 1 owns 512 tensor-memory columns (two
+// 128 x 256 FP32 accumulators) and issues the MMAs; warps 2-5 read the
+// finished accumulator (one TMEM lane quarter each), compare acc <= Y_g
+// (Y_g = K X_g - c_g rounded up) and append candidates, with their FP32
+// error clipped at 10 like the reference's, to this CTA's own output segment
+// through a shared-memory counter.  The epilogue of one tile
+// overlaps the MMAs of the next.  Every wait on an mbarrier is bounded by a
+// clock limit; a wait that runs out sets an error bit, the CTA stops issuing
+// work, waits (bounded) for its copies and MMAs in flight, frees its tensor
+// memory and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+
+#include "kernels.h"
+
+namespace abc {
+namespace {
+
+constexpr int BM = 128;          // particles per tile = TMEM lanes
+constexpr int BN = 256;          // genes per tile = TMEM columns per accumulator
+constexpr int BK = 32;           // FP32 values per 128-byte swizzled row (one TMA box width)
+constexpr int kThreads = 192;
+constexpr uint32_t kTmemCols = 512;
+constexpr long long kWaitLimit = 1ll << 31;  // SM cycles (about one second) per wait
+constexpr uint32_t kABytes = BM * BK * 4;    // 16 KB
+constexpr uint32_t kBBytes = BN * BK * 4;    // 32 KB
+
+template <int NH>
+struct Cfg {
+  static constexpr int kStages = NH == 1 ? 4 : 2;
+  static constexpr uint32_t kStageBytes = NH * (kABytes + kBBytes);
+  static constexpr uint32_t kTileBytes = kStages * kStageBytes;
+  // tiles + barriers (2 S + 5) + tmem slot + counters + per-gene Y and c of a tile
+  static constexpr uint32_t kSmem = 1024 + kTileBytes + 256 + 2 * BN * 4;
+};
+
+__device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(b)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(su32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Wait for the completion of the phase with the given parity; false after the limit.
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
+  if (mbar_try(b, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try(b, parity))
+    if (clock64() - t0 > kWaitLimit) return false;
+  return true;
+}
+
+__device__ __forceinline__ void tma_load(uint32_t dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], "
+      "[%2];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(su32(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, rows of
+// 128 bytes, 8-row groups 1024 bytes apart (the layout TMA writes for a
+// 32-wide FP32 box with CU_TENSOR_MAP_SWIZZLE_128B into a 1024-aligned buffer).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;             // leading byte offset (16 B; unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset between 8-row groups
+  d |= (uint64_t)1 << 46;             // descriptor version for tcgen05
+  d |= (uint64_t)2 << 61;             // 128-byte swizzle
+  return d;
+}
+
+// Instruction descriptor: D = F32, A = B = TF32, both K-major, M = 128, N = 256.
+constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                            ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+
+enum : int { kErrProducer = 1, kErrMma = 2, kErrEpilogue = 4, kErrDrain = 8 };
+
+template <int NH>
+__global__ void __launch_bounds__(kThreads, 1)
+    dist_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs a) {
+  using C = Cfg<NH>;
+  constexpr int S = C::kStages;
+  extern __shared__ uint8_t smem_raw[];
+  // 128-byte swizzle atoms repeat every 1024 bytes of shared-space address
+  uint8_t* smem = smem_raw + ((1024u - (su32(smem_raw) & 1023u)) & 1023u);
+  uint64_t* full = (uint64_t*)(smem + C::kTileBytes);
+  uint64_t* empty = full + S;
+  uint64_t* tfull = empty + S;
+  uint64_t* tempty = tfull + 2;
+  uint64_t* drain = tempty + 2;
+  uint32_t* tslot = (uint32_t*)(drain + 1);
+  uint32_t* s_count = tslot + 1;
+  uint32_t* s_abort = tslot + 2;
+  float* Ys = (float*)(smem + C::kTileBytes + 256);
+  float* Cs = Ys + BN;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], 128);
+    }
+    mbar_init(drain, 1);
+    *s_count = 0;
+    *s_abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tslot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = *tslot;
+  const int n_tiles = a.nM * a.nN;
+  const uint32_t smem_base = su32(smem);
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---------------- TMA producer
+      int stage = 0;
+      uint32_t phase = 0;
+      uint32_t issued = 0;       // bit s: stage s has a load in flight or consumed
+      uint32_t issued_par = 0;   // bit s: parity of the last phase issued on full[s]
+      bool ok = true;
+      for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+        const int m = t / a.nN, n = t - (t / a.nN) * a.nN;
+        for (int c = 0; c < a.n_chunks; ++c) {
+          if (!mbar_wait(&empty[stage], phase ^ 1)) {
+            atomicOr(a.err, kErrProducer);
+            ok = false;
+            break;
+          }
+          mbar_expect_tx(&full[stage], C::kStageBytes);
+          const uint32_t st = smem_base + stage * C::kStageBytes;
+#pragma unroll
+          for (int h = 0; h < NH; ++h)
+            tma_load(st + h * kABytes, &tmA, &full[stage], h * a.KA + c * BK, m * BM);
+#pragma unroll
+          for (int h = 0; h < NH; ++h)
+            tma_load(st + NH * kABytes + h * kBBytes, &tmB, &full[stage], h * a.KA + c * BK, n * BN);
+          issued |= 1u << stage;
+          issued_par = (issued_par & ~(1u << stage)) | (phase << stage);
+          if (++stage == S) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+      }
+      // loads still in flight land before the CTA leaves
+      for (int s = 0; s < S; ++s)
+        if ((issued >> s) & 1u)
+          if (!mbar_wait(&full[s], (issued_par >> s) & 1u)) atomicOr(a.err, kErrDrain);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---------------- MMA issuer
+      int stage = 0;
+      uint32_t phase = 0;
+      int acc = 0;
+      uint32_t acc_phase = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+        if (!mbar_wait(&tempty[acc], acc_phase ^ 1)) {
+          atomicOr(a.err, kErrMma);
+          break;
+        }
+        tc_fence_after();
+        const uint32_t d_tmem = tbase + (uint32_t)(acc * BN);
+        for (int c = 0; c < a.n_chunks; ++c) {
+          if (!mbar_wait(&full[stage], phase)) {
+            atomicOr(a.err, kErrMma);
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t st = smem_base + stage * C::kStageBytes;
+          const uint64_t a0 = sw128_desc(st), b0 = sw128_desc(st + NH * kABytes);
+#pragma unroll
+          for (int kk = 0; kk < BK / 8; ++kk) {
+            const uint64_t adv = (uint64_t)(kk * 32) >> 4;  // 8 TF32 = 32 bytes along K
+            mma_tf32(d_tmem, a0 + adv, b0 + adv, (c | kk) != 0);
+            if (NH == 2) {
+              const uint64_t a1 = sw128_desc(st + kABytes), b1 = sw128_desc(st + NH * kABytes + kBBytes);
+              mma_tf32(d_tmem, a0 + adv, b1 + adv, 1u);  // hi x lo
+              mma_tf32(d_tmem, a1 + adv, b0 + adv, 1u);  // lo x hi
+            }
+          }
+          mma_commit(&empty[stage]);  // stage reusable once these MMAs have read it
+          if (++stage == S) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+        if (!ok) break;
+        mma_commit(&tfull[acc]);
+        if (++acc == 2) {
+          acc = 0;
+          acc_phase ^= 1;
+        }
+      }
+      mma_commit(drain);
+      if (!mbar_wait(drain, 0)) atomicOr(a.err, kErrDrain);
+    }
+  } else {
+    // ---------------- epilogue: warps 2..5, TMEM lane quarter = warp % 4
+    const int et = threadIdx.x - 64;
+    const int q = warp & 3;
+    const float invK = 1.0f / (float)a.K;
+    int acc = 0;
+    uint32_t acc_phase = 0;
+    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+      const int m = t / a.nN, n = t - (t / a.nN) * a.nN;
+      epi_bar();  // readers of the previous tile's Y / c are done
+      for (int j = et; j < BN; j += 128) {
+        const int64_t g = (int64_t)n * BN + j;
+        Ys[j] = g < a.G ? a.Y[g] : -INFINITY;
+        Cs[j] = g < a.G ? a.cg[g] : 0.0f;
+      }
+      const bool got = mbar_wait(&tfull[acc], acc_phase);
+      if (!got) atomicOr(s_abort, 1u);
+      epi_bar();
+      if (*(volatile uint32_t*)s_abort) {
+        atomicOr(a.err, kErrEpilogue);
+        break;
+      }
+      tc_fence_after();
+      const int64_t row = (int64_t)m * BM + q * 32 + lane;
+      const bool valid = row < a.P;
+      const uint32_t lane_addr = tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN);
+#pragma unroll 1
+      for (int cc = 0; cc < BN / 32; ++cc) {
+        __syncwarp();
+        uint32_t v[32];
+        tmem_ld32(lane_addr + (uint32_t)(cc * 32), v);
+        uint32_t msk = 0;
+        const float4* Y4 = reinterpret_cast<const float4*>(Ys + cc * 32);
+#pragma unroll
+        for (int j4 = 0; j4 < 8; ++j4) {
+          const float4 y = Y4[j4];
+          msk |= (uint32_t)(__uint_as_float(v[4 * j4 + 0]) <= y.x) << (4 * j4 + 0);
+          msk |= (uint32_t)(__uint_as_float(v[4 * j4 + 1]) <= y.y) << (4 * j4 + 1);
+          msk |= (uint32_t)(__uint_as_float(v[4 * j4 + 2]) <= y.z) << (4 * j4 + 2);
+          msk |= (uint32_t)(__uint_as_float(v[4 * j4 + 3]) <= y.w) << (4 * j4 + 3);
+        }
+        if (!valid) msk = 0;
+        if (__any_sync(0xffffffffu, msk != 0)) {
+          const uint32_t cnt = __popc(msk);
+          uint32_t incl = cnt;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+          }
+          uint32_t base = 0;
+          if (lane == 31) base = atomicAdd(s_count, incl);
+          base = __shfl_sync(0xffffffffu, base, 31);
+          uint32_t pos = base + incl - cnt;
+          // unrolled so that v[] stays in registers
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            if (msk & (1u << j)) {
+              if ((int64_t)pos < a.seg_cap) {
+                const int64_t slot = (int64_t)blockIdx.x * a.seg_cap + pos;
+                Cand cd;
+                cd.p = (int32_t)row;
+                cd.g = (int32_t)((int64_t)n * BN + cc * 32 + j);
+                a.cand[slot] = cd;
+                a.cand_e[slot] = fminf((__uint_as_float(v[j]) + Cs[cc * 32 + j]) * invK, 10.0f);
+              }
+              ++pos;
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&tempty[acc]);
+      if (++acc == 2) {
+        acc = 0;
+        acc_phase ^= 1;
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(kTmemCols));
+  if (threadIdx.x == 0) a.seg_count[blockIdx.x] = *s_count;
+}
+
+// ---------------------------------------------------------------------------
+// operand preparation
+// ---------------------------------------------------------------------------
+
+// FP32 -> TF32 with round-to-nearest (ties away from zero on the magnitude),
+// NaN and infinities passed through.
+__device__ __forceinline__ float tf32_rn(float x) {
+  uint32_t u = __float_as_uint(x);
+  if ((u & 0x7F800000u) == 0x7F800000u) return x;
+  u = (u + 0x1000u) & 0xFFFFE000u;
+  return __uint_as_float(u);
+}
+
+// hi/lo TF32 parts of an FP64 value: hi = tf32(x), lo = tf32(x - hi)
+__device__ __forceinline__ void split_tf32(double x, float& hi, float& lo) {
+  hi = tf32_rn((float)x);
+  const double r = x - (double)hi;
+  lo = (hi == hi && fabs(hi) < INFINITY) ? tf32_rn((float)r) : 0.0f;
+}
+
+// flags[0]: bit 0 = an operand is infinite in FP32; flags[1] / flags[2] = the
+// largest w and the largest s^2 (FP32 bit patterns of non-negative values,
+// ordered like unsigned integers), so the host can check that no w s^2 product
+// leaves the FP32 range.
+__device__ __forceinline__ void note_max(unsigned* slot, float v) {
+  if (v == v) atomicMax(slot, __float_as_uint(fabsf(v)));
+}
+
+// A rows: [s (K) | s^2 (K) | 0 ...] per half.
+__global__ void tc_prep_rows_kernel(const double* stats, int64_t P, int K, int KA, int NH, float* A,
+                                    unsigned* flags) {
+  const int64_t n = P * (int64_t)KA;
+  const int64_t ld = (int64_t)NH * KA;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = i / KA;
+    const int k = (int)(i - p * KA);
+    double v = 0.0;
+    if (k < 2 * K) {
+      const double s = stats[p * K + (k < K ? k : k - K)];
+      v = k < K ? s : s * s;
+      const float f = (float)v;
+      if (fabsf(f) == INFINITY) atomicOr(&flags[0], 1u);
+      if (k >= K) note_max(&flags[2], f);
+    }
+    float hi, lo;
+    split_tf32(v, hi, lo);
+    A[p * ld + k] = hi;
+    if (NH == 2) A[p * ld + KA + k] = lo;
+  }
+}
+
+// B rows: [-2 w d (K) | w (K) | 0 ...] per half; c_g = sum_k w d^2 in FP64; the
+// per-gene term of the error bound b0_g = 5 beta c_g / K.
+__global__ void tc_prep_genes_kernel(const double* data, const double* se, int64_t G, int K, int KA, int NH,
+                                     double beta, float* B, double* cg64, float* cg32, float* b0, unsigned* flags) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= G) return;
+  const int64_t ld = (int64_t)NH * KA;
+  const double sig2 = 0.1 * 0.1;
+  double c = 0.0;
+  bool bad = false;
+  for (int k = 0; k < KA; ++k) {
+    double v = 0.0;
+    if (k < 2 * K) {
+      const int kk = k < K ? k : k - K;
+      const double d = data[g * K + kk], e = se[g * K + kk];
+      const double eps = (e + d != 0.0) ? 0.0 : 0.0001;
+      const double w = 1.0 / ((e * e + sig2 * (d * d)) + eps);
+      v = k < K ? -2.0 * w * d : w;
+      if (fabsf((float)v) == INFINITY) bad = true;
+      if (k >= K) note_max(&flags[1], (float)w);
+      else c += w * d * d;
+    }
+    float hi, lo;
+    split_tf32(v, hi, lo);
+    B[g * ld + k] = hi;
+    if (NH == 2) B[g * ld + KA + k] = lo;
+  }
+  if (bad) atomicOr(&flags[0], 1u);
+  cg64[g] = c;
+  cg32[g] = (float)c;
+  b0[g] = (float)(5.0 * beta * c / (double)K);
+}
+
+// Y_g = K X_g - c_g rounded up; X < 0 accepts no pair.  Errors are clipped at
+// 10 (scripts/compute_errors.jl:159-161), so X >= 10 accepts every finite pair,
+// however large its unclipped error.
+__global__ void tc_y_kernel(const float* X, const double* cg64, int64_t G, int K, float* Y) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= G) return;
+  const float x = X[g];
+  float y;
+  if (x != x) y = x;
+  else if (x >= 10.0f) y = INFINITY;
+  else if (x < 0.0f) y = -INFINITY;
+  else y = __double2float_ru((double)x * (double)K - cg64[g]);
+  Y[g] = y;
+}
+
+// Concatenate the per-CTA segments: out[off_b + i] = seg_b[i].
+__global__ void tc_gather_kernel(const Cand* seg, const float* seg_e, const unsigned* count, int n_seg,
+                                 int64_t seg_cap, Cand* out, float* out_e) {
+  __shared__ int64_t off;
+  const int b = blockIdx.x;
+  if (threadIdx.x == 0) {
+    int64_t o = 0;
+    for (int i = 0; i < b; ++i) o += count[i];
+    off = o;
+  }
+  __syncthreads();
+  const int64_t n = count[b];
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    out[off + i] = seg[(int64_t)b * seg_cap + i];
+    out_e[off + i] = seg_e[(int64_t)b * seg_cap + i];
+  }
+}
+
+bool make_map(CUtensorMap* map, const float* base, int64_t rows, int64_t cols, int box_rows) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+      return false;
+    encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  }
+  memset(map, 0, sizeof(*map));
+  cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)cols * 4};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  return encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, estr,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int NH>
+cudaError_t launch_nh(const float* A, const float* B, const TcArgs& args, int grid, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(dist_tc_kernel<NH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)Cfg<NH>::kSmem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  CUtensorMap ma, mb;
+  const int64_t ld = (int64_t)NH * args.KA;
+  if (!make_map(&ma, A, args.P, ld, BM) || !make_map(&mb, B, args.G, ld, BN)) return cudaErrorInvalidValue;
+  dist_tc_kernel<NH><<<grid, kThreads, Cfg<NH>::kSmem, s>>>(ma, mb, args);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+int tc_ka(int K) { return ((2 * K + BK - 1) / BK) * BK; }
+
+double tc_beta(int K, int nh) {
+  // |K e32 - K e| <= beta * sum_k |term_k| with sum_k |term_k| <= 5 c_g + 4 K e:
+  //   one term: products of two round-to-nearest TF32 values, relative error
+  //     (1 + 2^-11)^2 - 1 (plus 2^-24 from the FP64 -> FP32 step), exact FP32 products,
+  //     2K accumulations at <= 2^-23 each (truncating adder);
+  //   three terms: representation error of hi + lo <= 2^-21 per operand, the
+  //     dropped lo*lo <= 2^-22, 6K accumulations.
+  // Plus the final FP32 rounding of Y / e, with a 10 % safety factor.
+  const double u23 = 1.1920928955078125e-07;
+  double b;
+  if (nh == 1)
+    b = (std::pow(1.0 + 4.8828125e-04 + 5.960464477539063e-08, 2) - 1.0) + (2.0 * K + 4) * u23;
+  else
+    b = 2.0 * 4.76837158203125e-07 + 2.384185791015625e-07 + (6.0 * K + 4) * u23;
+  return 1.1 * b;
+}
+
+cudaError_t launch_tc_prep(const DistInputs& in, int nh, double beta, float* A, float* B, double* cg64, float* cg32,
+                           float* b0, unsigned* flags, cudaStream_t s) {
+  const int KA = tc_ka(in.K);
+  if (in.P > 0) {
+    const int64_t n = in.P * (int64_t)KA;
+    int blocks = (int)((n + 255) / 256 < 65536 ? (n + 255) / 256 : 65536);
+    tc_prep_rows_kernel<<<blocks, 256, 0, s>>>(in.stats, in.P, in.K, KA, nh, A, flags);
+  }
+  if (in.G > 0)
+    tc_prep_genes_kernel<<<(unsigned)((in.G + 127) / 128), 128, 0, s>>>(in.data, in.se, in.G, in.K, KA, nh, beta,
+                                                                        B, cg64, cg32, b0, flags);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tc_y(const float* X, const double* cg64, int64_t G, int K, float* Y, cudaStream_t s) {
+  if (G <= 0) return cudaSuccess;
+  tc_y_kernel<<<(unsigned)((G + 255) / 256), 256, 0, s>>>(X, cg64, G, K, Y);
+  return cudaGetLastError();
+}
+
+int tc_grid(int64_t P, int64_t G, int sms) {
+  const int64_t tiles = ((P + BM - 1) / BM) * ((G + BN - 1) / BN);
+  return (int)(tiles < sms ? tiles : sms);
+}
+
+cudaError_t launch_dist_tc(int nh, const float* A, const float* B, const TcArgs& args, int grid, cudaStream_t s) {
+  if (args.P <= 0 || args.G <= 0) return cudaSuccess;
+  return nh == 2 ? launch_nh<2>(A, B, args, grid, s) : launch_nh<1>(A, B, args, grid, s);
+}
+
+cudaError_t launch_tc_gather(const Cand* seg, const float* seg_e, const unsigned* count, int n_seg, int64_t seg_cap,
+                             Cand* out, float* out_e, cudaStream_t s) {
+  if (n_seg <= 0) return cudaSuccess;
+  tc_gather_kernel<<<n_seg, 256, 0, s>>>(seg, seg_e, count, n_seg, seg_cap, out, out_e);
+  return cudaGetLastError();
+}
+
+}  // namespace abc

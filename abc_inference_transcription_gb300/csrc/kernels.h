@@ -63,17 +63,56 @@ struct Cand {
   int32_t p, g;
 };
 
+// Tensor-core candidate pass (distance_tc.cu).  A = [s | s^2] per particle and
+// B = [-2 w d | w] per gene, TF32, rows of tc_ka(K) values per half (hi, and lo
+// in three-term mode); K err = c_g + A.B accumulated in FP32.
+struct TcArgs {
+  int64_t P, G;
+  int K, KA, n_chunks, nM, nN;
+  const float* Y;       // per gene: K X_g - c_g rounded up (candidate iff acc <= Y_g)
+  const float* cg;      // per gene c_g in FP32 (for the reported FP32 error)
+  Cand* cand;           // per-CTA segments of seg_cap entries
+  float* cand_e;        // FP32 error of each candidate
+  int64_t seg_cap;
+  unsigned* seg_count;  // per CTA: candidates found (may exceed seg_cap)
+  int* err;             // nonzero: a bounded wait ran out
+};
+int tc_ka(int K);
+// relative error factor beta: |e32 - e| <= beta (5 c_g / K + 4 e)
+double tc_beta(int K, int nh);
+int tc_grid(int64_t P, int64_t G, int sms);
+// flags[0] bit 0: an operand is infinite in FP32; flags[1], flags[2]: max w, max s^2 (FP32 bits)
+cudaError_t launch_tc_prep(const DistInputs& in, int nh, double beta, float* A, float* B, double* cg64, float* cg32,
+                           float* b0, unsigned* flags, cudaStream_t s);
+cudaError_t launch_tc_y(const float* X, const double* cg64, int64_t G, int K, float* Y, cudaStream_t s);
+cudaError_t launch_dist_tc(int nh, const float* A, const float* B, const TcArgs& args, int grid, cudaStream_t s);
+cudaError_t launch_tc_gather(const Cand* seg, const float* seg_e, const unsigned* count, int n_seg, int64_t seg_cap,
+                             Cand* out, float* out_e, cudaStream_t s);
+
 // per (g,k): sw = sqrt(w), dw = sqrt(w) d in FP32, w = 1/((se^2 + 0.01 d^2) + eps)
 cudaError_t launch_dist_prep(const DistInputs& in, float* sw, float* dw, float* s32, cudaStream_t s);
 // FP32 direct distance: emit (p, g) with min(10, err32) <= X[g] (mode emit), or
 // write err32 of the particles p = row*stride into esub[row][g] (mode sample).
 cudaError_t launch_dist_fast(const float* s32, const float* sw, const float* dw, int64_t P, int64_t G, int K,
-                             const float* X, Cand* cand, unsigned long long* n_cand, int64_t cap,
+                             const float* X, Cand* cand, float* cand_e, unsigned long long* n_cand, int64_t cap,
                              float* esub, int64_t stride, int64_t n_sub, cudaStream_t s);
+// Error bound of a candidate pass, linear per gene: |e32 - e| <= b0[g] + b1 e.
 // per gene: X[g] = upper edge of the histogram bin where the count of esub
 // reaches k_sub, plus the bound (+inf when fewer than k_sub finite values).
-cudaError_t launch_dist_threshold(const float* esub, int64_t n_sub, int64_t G, int64_t k_sub, int K,
-                                  float* X, cudaStream_t s);
+cudaError_t launch_dist_threshold(const float* esub, int64_t n_sub, int64_t G, int64_t k_sub, const float* b0,
+                                  float b1, float* X, cudaStream_t s);
+cudaError_t launch_fill(float* x, int64_t n, float v, cudaStream_t s);
+// dense[p G + g] = e of candidate (p, g)
+cudaError_t launch_scatter_errors(const Cand* cand, const float* e, int64_t n, int64_t G, float* out, cudaStream_t s);
+// X[g] = e_g + 2 B_g(e_g) for e_g = thr[g] (or eps when thr is null); +inf for e_g >= 10, -1 for e_g < 0.
+cudaError_t launch_x_from_thr(const double* thr, double eps, int64_t G, const float* b0, float b1, float* X,
+                              cudaStream_t s);
+// top-k refinement before the FP64 recheck: per-gene histogram of the
+// candidates' FP32 errors, a tighter Xt <= X from the bin completing k, and
+// the candidates with e <= Xt appended to out (count in *count).
+cudaError_t launch_refine(const Cand* cand, const float* cand_e, int64_t n, int64_t G, int64_t k, const float* X,
+                          const float* b0, float b1, unsigned int* hist, float* Xt, Cand* out,
+                          unsigned long long* count, cudaStream_t s);
 // FP64 error of each candidate, in the reference's operation order.
 cudaError_t launch_dist_recheck(const DistInputs& in, const Cand* cand, int64_t n, double* e64, cudaStream_t s);
 // group candidates by gene and sort each gene's list by (err, p).
@@ -84,15 +123,14 @@ cudaError_t launch_dist_group_sort(const Cand* cand, const double* e64, int64_t 
 // finite errors) and, in mode 1, a failure flag when the candidate threshold
 // X[g] could have excluded a member of the top k.
 cudaError_t launch_dist_accept_len(const int64_t* goff, const double* se64, int64_t G, int mode, double eps,
-                                   const double* eps_g, int64_t k, const float* X, int K, int64_t* alen, int* fail,
-                                   cudaStream_t s);
+                                   const double* eps_g, int64_t k, const float* X, const float* b0, float b1,
+                                   int64_t* alen, int* fail, cudaStream_t s);
 // compact the accepted prefixes: idx (1-based particle index + p_base) and err.
 cudaError_t launch_dist_compact(const int64_t* goff, const int32_t* sp, const double* se64, const int64_t* aoff,
                                 int64_t G, int64_t p_base, int64_t* idx, double* err, cudaStream_t s);
 cudaError_t launch_scan(const int64_t* cnt, int64_t G, int64_t* off, cudaStream_t s);
 // full FP64 error matrix [P][G]
 cudaError_t launch_dist_full(const DistInputs& in, double* err, cudaStream_t s);
-float dist_bound(float e, int K);
 
 cudaError_t launch_prior(const PriorArgs& a, cudaStream_t s);
 cudaError_t launch_setup(const SetupArgs& a, cudaStream_t s);

@@ -180,6 +180,22 @@ class Context:
                                         ptr(out)))
         return out
 
+    def errors_candidate(self, data: np.ndarray, se: np.ndarray, stats: np.ndarray, families=None):
+        """FP32 errors of the candidate pass for every pair [P, G], the bound
+        terms (b0[G], b1) with |err32 - err| <= b0[g] + b1 err, and the mode used."""
+        d = np.ascontiguousarray(data, np.float64)
+        e = np.ascontiguousarray(se, np.float64)
+        s = np.ascontiguousarray(stats, np.float64)
+        G, K = d.shape
+        nf, f = self._fam(families, K)
+        out = np.zeros((s.shape[0], G), np.float32)
+        b0 = np.zeros(G)
+        b1, used = C.c_double(), C.c_int()
+        self._check(self.lib.abc_errors_candidate(self.h, ptr(d), ptr(e), G, K, nf, ptr(f, C.c_int32), ptr(s),
+                                                  s.shape[0], ptr(out, C.c_float), ptr(b0), C.byref(b1),
+                                                  C.byref(used)))
+        return out, b0, b1.value, used.value
+
     def select(self, data: np.ndarray, se: np.ndarray, stats: np.ndarray, mode: int, eps_or_q: float,
                families=None) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
         """Accepted particles per gene: (offsets[G+1], 1-based indices, errors)."""
@@ -238,8 +254,20 @@ class Context:
         return ms.value, n.value
 
     def select_counters(self) -> tuple[int, int]:
+        """(pairs emitted by the FP32 candidate pass, pairs rechecked in FP64) of the last selection."""
         a, b = C.c_int64(), C.c_int64()
         self._check(self.lib.abc_select_counters(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def set_distance_mode(self, mode: int) -> None:
+        """Candidate pass: 0 FP32 CUDA cores, 1 TF32 tensor cores (one term),
+        2 TF32 tensor cores with hi/lo splits (default)."""
+        self._check(self.lib.abc_set_distance_mode(self.h, int(mode)))
+
+    def distance_mode(self) -> tuple[int, int]:
+        """(requested mode, mode used by the last selection; -1 before any)."""
+        a, b = C.c_int(), C.c_int()
+        self._check(self.lib.abc_get_distance_mode(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
 

@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--no-abc", action="store_true", help="skip the plain vs screened ABC section")
     ap.add_argument("--dist-particles", type=int, default=5_000_000)
     ap.add_argument("--genes", type=int, default=2000)
+    ap.add_argument("--section", default="all", choices=["all", "distance"],
+                    help="'distance' runs only the P x G distance section and prints its object")
     return ap.parse_args()
 
 
@@ -289,6 +291,12 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
+    if args.section == "distance":
+        if rank == 0:
+            import __graft_entry__
+            __graft_entry__.build()
+            print(json.dumps(distance_bench(args.dist_particles, args.genes, 72, 0.001, 5, args.cpu_seconds)))
+        return
     dist = None
     if world > 1:
         import torch.distributed as dist
@@ -426,8 +434,11 @@ def main():
     if not args.no_abc:
         try:
             from abc_inference_transcription_gb300 import pipeline
-            line["abc_screened"] = pipeline.run(genes=(args.genes, 8), per_model_train=20000, per_model_plain=2000,
-                                                screen_factor=10, q=0.001, seed=1, epochs=40)
+            # accepted pairs per second, plain vs surrogate-screened, top 1 % per gene,
+            # for 8, 50 and the full gene set (the screen's gain falls with the
+            # number of genes a draw must be far from)
+            line["abc_screened"] = pipeline.run(genes=(8, 50, args.genes), per_model_train=20000,
+                                                per_model_plain=2000, screen_factor=10, q=0.01, seed=1, epochs=40)
         except Exception as exc:
             line["abc_screened"] = {"error": repr(exc)}
     print(json.dumps(line))

@@ -221,11 +221,32 @@ int abc_errors_select_device(abc_ctx* ctx, const double* data, const double* se,
 /* gene_offsets: G+1 entries; particle_idx: 1-based, n_accepted_total entries;
  * err: FP64 errors of the accepted pairs (may be NULL). */
 int abc_accept_fetch(abc_ctx* ctx, int64_t* gene_offsets, int64_t* particle_idx, double* err);
-/* Counters of the last selection: FP32 candidates rechecked in FP64. */
+/* Counters of the last selection: pairs emitted by the FP32 candidate
+ * pass(es), and pairs rechecked in FP64 (after the top-k refinement). */
 int abc_select_counters(const abc_ctx* ctx, int64_t* candidates, int64_t* rechecked);
-/* With abc_profile on: device milliseconds of the FP32 candidate-pass kernel
- * of the last selection, summed over its passes, and the number of passes. */
+/* With abc_profile on: device milliseconds of the candidate-pass kernel of
+ * the last selection, summed over its passes, and the number of passes. */
 int abc_select_profile_read(const abc_ctx* ctx, double* fast_ms, int* fast_passes);
+/* Candidate pass of the selections (the FP32 screen in front of the FP64
+ * recheck of scripts/compute_errors.jl:30-43; no reference counterpart, the
+ * reference evaluates every pair in FP64):
+ *   0  FP32 on the CUDA cores, 2 FMA per (particle, gene, statistic);
+ *   1  TF32 tensor cores, K err = c_g + [s | s^2] . [-2 w d | w], one term;
+ *   2  as 1 with hi/lo TF32 splits (three terms, ~FP32 products; default).
+ * Modes 1 and 2 fall back to 0 for a selection whose inputs hold an infinite
+ * value or could overflow FP32 in w s^2.  Accepted sets do not depend on the
+ * mode: every mode is followed by the same FP64 recheck. */
+int abc_set_distance_mode(abc_ctx* ctx, int mode);
+/* requested mode, and the mode the last selection used (-1 before any). */
+int abc_get_distance_mode(const abc_ctx* ctx, int* requested, int* used);
+/* Diagnostic: the candidate pass's FP32 error of every pair (row-major
+ * [P][G], P G <= 2^28; NaN where the pass yields NaN) with its error bound
+ * |err_out - err| <= b0_out[g] + b1_out err against the exact error of
+ * abc_errors (both clipped at 10), and the mode used.  b0_out, b1_out and
+ * mode_used may be NULL. */
+int abc_errors_candidate(abc_ctx* ctx, const double* data, const double* se, int64_t n_genes, int n_stats,
+                         int n_fam, const int32_t* fam, const double* stats, int64_t n_particles, float* err_out,
+                         double* b0_out, double* b1_out, int* mode_used);
 
 /* ------------------------------------------------------------------------
  * Learned pre-screen.  No reference counterpart: the reference simulates
