@@ -922,6 +922,14 @@ static int select_impl(abc_ctx* c, const double* data, const double* se, int64_t
       CK(launch_dist_fast(c->d_s32.p, c->d_sw.p, c->d_dw.p, P, G, K, nullptr, nullptr, nullptr, nullptr, 0,
                           c->d_esub.p, stride, n_sub, c->stream));
       CK(launch_dist_threshold(c->d_esub.p, n_sub, G, k_sub, c->d_b0.p, b1, c->d_X.p, c->stream));
+      if (dmode) {
+        // about k_sub of every n_sub particles per gene pass X: size the per-CTA
+        // segments for that (with room for imbalance) so one pass suffices
+        const int grid = tc_grid(P, G, c->sms);
+        const double est = (double)G * (double)k_sub * ((double)P / (double)n_sub);
+        const int64_t want = (int64_t)(1.5 * est / grid) + 4096;
+        c->seg_cap = std::max(c->seg_cap, std::min<int64_t>(want, kCandLimit / grid + 1));
+      }
       CK(cudaMemcpyAsync(hX.data(), c->d_X.p, sizeof(float) * G, cudaMemcpyDeviceToHost, c->stream));
     }
   }

@@ -11,11 +11,12 @@
 // Three-term mode splits each operand into TF32 hi + lo parts and accumulates
 // hi*hi + hi*lo + lo*hi, so every product is exact to ~2^-21.
 //
-// CTA: 6 warps, one persistent CTA per SM.  Warp 0 issues TMA loads of
+// CTA: 10 warps, one persistent CTA per SM.  Warp 0 issues TMA loads of
 // 128 x 32 (A) and 256 x 32 (B) FP32 boxes with the 128-byte swizzle into a
 // ring of shared-memory stages; warp 1 owns 512 tensor-memory columns (two
-// 128 x 256 FP32 accumulators) and issues the MMAs; warps 2-5 read the
-// finished accumulator (one TMEM lane quarter each), compare acc <= Y_g
+// 128 x 256 FP32 accumulators) and issues the MMAs; warps 2-9 read the
+// finished accumulator (two warps per TMEM lane quarter, half of the columns
+// each), compare acc <= Y_g
 // (Y_g = K X_g - c_g rounded up) and append candidates, with their FP32
 // error clipped at 10 like the reference's, to this CTA's own output segment
 // through a shared-memory counter.  The epilogue of one tile
@@ -38,7 +39,9 @@ namespace {
 constexpr int BM = 128;          // particles per tile = TMEM lanes
 constexpr int BN = 256;          // genes per tile = TMEM columns per accumulator
 constexpr int BK = 32;           // FP32 values per 128-byte swizzled row (one TMA box width)
-constexpr int kThreads = 192;
+constexpr int kEpiWarps = 8;                 // two per TMEM lane quarter, each half of the columns
+constexpr int kEpiThreads = 32 * kEpiWarps;
+constexpr int kThreads = 64 + kEpiThreads;
 constexpr uint32_t kTmemCols = 512;
 constexpr long long kWaitLimit = 1ll << 31;  // SM cycles (about one second) per wait
 constexpr uint32_t kABytes = BM * BK * 4;    // 16 KB
@@ -136,7 +139,7 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory"); }
 
 enum : int { kErrProducer = 1, kErrMma = 2, kErrEpilogue = 4, kErrDrain = 8 };
 
@@ -167,7 +170,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&tfull[b], 1);
-      mbar_init(&tempty[b], 128);
+      mbar_init(&tempty[b], kEpiThreads);
     }
     mbar_init(drain, 1);
     *s_count = 0;
@@ -275,16 +278,18 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (!mbar_wait(drain, 0)) atomicOr(a.err, kErrDrain);
     }
   } else {
-    // ---------------- epilogue: warps 2..5, TMEM lane quarter = warp % 4
+    // ---------------- epilogue: warps 2..9; TMEM lane quarter = warp % 4,
+    // columns [128 h, 128 h + 128) with h = (warp - 2) / 4
     const int et = threadIdx.x - 64;
     const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
     const float invK = 1.0f / (float)a.K;
     int acc = 0;
     uint32_t acc_phase = 0;
     for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
       const int m = t / a.nN, n = t - (t / a.nN) * a.nN;
       epi_bar();  // readers of the previous tile's Y / c are done
-      for (int j = et; j < BN; j += 128) {
+      for (int j = et; j < BN; j += kEpiThreads) {
         const int64_t g = (int64_t)n * BN + j;
         Ys[j] = g < a.G ? a.Y[g] : -INFINITY;
         Cs[j] = g < a.G ? a.cg[g] : 0.0f;
@@ -301,47 +306,57 @@ __global__ void __launch_bounds__(kThreads, 1)
       const bool valid = row < a.P;
       const uint32_t lane_addr = tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN);
 #pragma unroll 1
-      for (int cc = 0; cc < BN / 32; ++cc) {
+      for (int c4 = 0; c4 < BN / 64; ++c4) {
+        const int cc = half * (BN / 64) + c4;
         __syncwarp();
         uint32_t v[32];
         tmem_ld32(lane_addr + (uint32_t)(cc * 32), v);
-        uint32_t msk = 0;
+        // fast test: min_j (v_j - Y_j) <= 0 iff some v_j <= Y_j (NaN terms drop out)
         const float4* Y4 = reinterpret_cast<const float4*>(Ys + cc * 32);
+        float dm[8];
 #pragma unroll
         for (int j4 = 0; j4 < 8; ++j4) {
           const float4 y = Y4[j4];
-          msk |= (uint32_t)(__uint_as_float(v[4 * j4 + 0]) <= y.x) << (4 * j4 + 0);
-          msk |= (uint32_t)(__uint_as_float(v[4 * j4 + 1]) <= y.y) << (4 * j4 + 1);
-          msk |= (uint32_t)(__uint_as_float(v[4 * j4 + 2]) <= y.z) << (4 * j4 + 2);
-          msk |= (uint32_t)(__uint_as_float(v[4 * j4 + 3]) <= y.w) << (4 * j4 + 3);
+          dm[j4] = fminf(fminf(__uint_as_float(v[4 * j4 + 0]) - y.x, __uint_as_float(v[4 * j4 + 1]) - y.y),
+                         fminf(__uint_as_float(v[4 * j4 + 2]) - y.z, __uint_as_float(v[4 * j4 + 3]) - y.w));
         }
-        if (!valid) msk = 0;
-        if (__any_sync(0xffffffffu, msk != 0)) {
-          const uint32_t cnt = __popc(msk);
-          uint32_t incl = cnt;
+        const float dmin = fminf(fminf(fminf(dm[0], dm[1]), fminf(dm[2], dm[3])),
+                                 fminf(fminf(dm[4], dm[5]), fminf(dm[6], dm[7])));
+        const bool has = valid && dmin <= 0.0f;
+        if (__ballot_sync(0xffffffffu, has) == 0u) continue;
+        // exact test, one atomic per warp, then the candidates of this lane
+        uint32_t msk = 0;
+        if (has) {
 #pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
-          }
-          uint32_t base = 0;
-          if (lane == 31) base = atomicAdd(s_count, incl);
-          base = __shfl_sync(0xffffffffu, base, 31);
+          for (int j = 0; j < 32; ++j) msk |= (uint32_t)(__uint_as_float(v[j]) <= Ys[cc * 32 + j]) << j;
+        }
+        const uint32_t cnt = __popc(msk);
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += y;
+        }
+        uint32_t base = 0;
+        if (lane == 31) base = atomicAdd(s_count, incl);
+        base = __shfl_sync(0xffffffffu, base, 31);
+        if (msk) {
+          float vv[32];  // indexed by candidate column below
+#pragma unroll
+          for (int j = 0; j < 32; ++j) vv[j] = __uint_as_float(v[j]);
           uint32_t pos = base + incl - cnt;
-          // unrolled so that v[] stays in registers
-#pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            if (msk & (1u << j)) {
-              if ((int64_t)pos < a.seg_cap) {
-                const int64_t slot = (int64_t)blockIdx.x * a.seg_cap + pos;
-                Cand cd;
-                cd.p = (int32_t)row;
-                cd.g = (int32_t)((int64_t)n * BN + cc * 32 + j);
-                a.cand[slot] = cd;
-                a.cand_e[slot] = fminf((__uint_as_float(v[j]) + Cs[cc * 32 + j]) * invK, 10.0f);
-              }
-              ++pos;
+          while (msk) {
+            const int j = __ffs(msk) - 1;
+            msk &= msk - 1;
+            if ((int64_t)pos < a.seg_cap) {
+              const int64_t slot = (int64_t)blockIdx.x * a.seg_cap + pos;
+              Cand cd;
+              cd.p = (int32_t)row;
+              cd.g = (int32_t)((int64_t)n * BN + cc * 32 + j);
+              a.cand[slot] = cd;
+              a.cand_e[slot] = fminf((vv[j] + Cs[cc * 32 + j]) * invK, 10.0f);
             }
+            ++pos;
           }
         }
       }

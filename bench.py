@@ -202,22 +202,39 @@ def distance_bench(P: int, G: int, K: int, q: float, seed: int, cpu_seconds: flo
         dt = time.perf_counter() - t0
         fast_ms, passes = ctx.select_profile()
         cands, rechecked = ctx.select_counters()
+        mode_used = ctx.distance_mode()[1]
     finally:
         ctx.close()
         sh_keep = stats[:64].cpu().numpy()
         del stats, base, pick
         torch.cuda.empty_cache()
     k = int(np.ceil(q * P))
-    flops = 4.0 * P * G * K * passes
-    peak = SMS * 128 * 2 * 2070.0e6
     out = {"workload": f"P={P} particles x K={K} statistics x G={G} genes, top {q:g} per gene",
            "pairs_per_s": P * G / dt, "seconds": dt, "accepted": int(off[-1]), "accepted_expected": k * G,
            "candidates": cands, "fp64_rechecked": rechecked, "candidate_passes": passes,
-           "roofline": {"bound": "fp32", "achieved": flops / (fast_ms / 1e3) / 1e12, "peak": peak / 1e12,
-                        "unit": "TFLOP/s", "frac": flops / (fast_ms / 1e3) / peak, "traffic": None,
-                        "basis": "2 FMA per (p, g, k) in the candidate pass; peak = nominal FP32 (152 SMs x "
-                                 "128 lanes x 2 flop x 2,070 MHz), no measured FP32 peak available",
-                        "kernel_ms_per_pass": fast_ms / max(passes, 1)}}
+           "distance_mode": mode_used}
+    if mode_used in (1, 2):
+        # tcgen05 TF32 MMAs issued per pass: 128 x 256 tiles, depth KA per term, 1 or 3 terms
+        ka = -(-2 * K // 32) * 32
+        tiles = -(-P // 128) * -(-G // 256)
+        terms = 3 if mode_used == 2 else 1
+        flops = 2.0 * 128 * 256 * ka * terms * tiles * passes
+        pk, src = load_peaks()
+        peak = float(pk.get("bf16_tflops", 1900.0)) / 2.0 * 1e12
+        out["roofline"] = {"bound": "tensor", "achieved": flops / (fast_ms / 1e3) / 1e12, "peak": peak / 1e12,
+                           "unit": "TFLOP/s", "frac": flops / (fast_ms / 1e3) / peak, "traffic": None,
+                           "basis": f"TF32 MMA flops issued ({terms} term(s), 128 x 256 tiles, depth {ka}); "
+                                    f"peak = half the {src} dense BF16 GEMM rate (TF32 runs at half the BF16 rate)",
+                           "kernel_ms_per_pass": fast_ms / max(passes, 1),
+                           "useful_fp32_tflops": 4.0 * P * G * K * passes / (fast_ms / 1e3) / 1e12}
+    else:
+        flops = 4.0 * P * G * K * passes
+        peak = SMS * 128 * 2 * 2070.0e6
+        out["roofline"] = {"bound": "fp32", "achieved": flops / (fast_ms / 1e3) / 1e12, "peak": peak / 1e12,
+                           "unit": "TFLOP/s", "frac": flops / (fast_ms / 1e3) / peak, "traffic": None,
+                           "basis": "2 FMA per (p, g, k) in the candidate pass; peak = nominal FP32 (152 SMs x "
+                                    "128 lanes x 2 flop x 2,070 MHz), no measured FP32 peak available",
+                           "kernel_ms_per_pass": fast_ms / max(passes, 1)}
     if cpu_seconds > 0:
         try:
             from oracle import oracle as orc
