@@ -77,7 +77,7 @@ struct abc_ctx {
   size_t ev_used = 0;
   double phase_ms[3] = {0, 0, 0};
   // selection workspace and results
-  DBuf<double> d_data, d_se, d_sel_stats, d_e64, d_se64, d_out_err;
+  DBuf<double> d_data, d_se, d_sel_stats, d_e64, d_se64, d_out_err, d_den;
   DBuf<float> d_sw, d_dw, d_s32, d_X, d_esub;
   DBuf<Cand> d_cand;
   DBuf<float> d_cande;  // FP32 error of each candidate
@@ -213,7 +213,7 @@ int abc_destroy(abc_ctx* c) {
   c->d_data.release(); c->d_se.release(); c->d_sel_stats.release(); c->d_e64.release(); c->d_se64.release();
   c->d_out_err.release(); c->d_sw.release(); c->d_dw.release(); c->d_s32.release(); c->d_X.release();
   c->d_esub.release(); c->d_cand.release(); c->d_sp.release(); c->d_gcount.release(); c->d_goff.release();
-  c->d_cande.release(); c->d_tcA.release(); c->d_tcB.release(); c->d_cg32.release(); c->d_b0.release();
+  c->d_cande.release(); c->d_den.release(); c->d_tcA.release(); c->d_tcB.release(); c->d_cg32.release(); c->d_b0.release();
   c->d_Y.release(); c->d_Xt.release(); c->d_seg_e.release(); c->d_cg64.release(); c->d_tcflags.release();
   c->d_segcount.release(); c->d_hist.release(); c->d_tcerr.release(); c->d_seg.release(); c->d_cand2.release();
   c->d_alen.release(); c->d_aoff.release(); c->d_out_idx.release(); c->d_gcursor.release();
@@ -687,6 +687,9 @@ static int load_dist_inputs(abc_ctx* c, const double* data, const double* se, in
   CK(cudaMemcpyAsync(c->d_se.p, se, sizeof(double) * G * K, cudaMemcpyHostToDevice, c->stream));
   in.data = c->d_data.p;
   in.se = c->d_se.p;
+  CK(c->d_den.ensure((size_t)G * K));
+  CK(launch_dist_den(in, c->d_den.p, c->stream));
+  in.den = c->d_den.p;
   if (stats_on_device) {
     in.stats = stats;
   } else {
@@ -834,9 +837,7 @@ static int prepare_candidate_pass(abc_ctx* c, const DistInputs& in, int* dmode_o
   const int K = in.K;
   CK(c->d_sw.ensure((size_t)G * K));
   CK(c->d_dw.ensure((size_t)G * K));
-  CK(c->d_s32.ensure((size_t)P * K));
   CK(c->d_b0.ensure((size_t)G));
-  CK(launch_dist_prep(in, c->d_sw.p, c->d_dw.p, c->d_s32.p, c->stream));
   int dmode = c->dist_mode;
   float b1 = 0.0f;
   if (dmode) {
@@ -860,6 +861,10 @@ static int prepare_candidate_pass(abc_ctx* c, const DistInputs& in, int* dmode_o
     if (fl[0] || (double)maxw * (double)maxs2 * (4.0 * K) > 1e37) dmode = 0;
     else b1 = (float)(4.0 * beta);
   }
+  // FP32 statistics of every particle for the CUDA-core pass; the tensor-core
+  // pass needs them only for the threshold subsample (converted there)
+  if (dmode == 0) CK(c->d_s32.ensure((size_t)P * K));
+  CK(launch_dist_prep(in, c->d_sw.p, c->d_dw.p, dmode == 0 ? c->d_s32.p : nullptr, P, 1, c->stream));
   if (dmode == 0) {
     // 1.5 u (64 sqrt(e) + (K + 8) e) <= 48 u + 1.5 u (K + 40) e, u = 2^-24
     const double u = 5.9604644775390625e-08;
@@ -919,8 +924,15 @@ static int select_impl(abc_ctx* c, const double* data, const double* se, int64_t
       CK(cudaMemcpyAsync(c->d_X.p, hX.data(), sizeof(float) * G, cudaMemcpyHostToDevice, c->stream));
     } else {
       CK(c->d_esub.ensure((size_t)n_sub * G));
+      int64_t sub_stride = stride;
+      if (dmode) {
+        // the subsample rows, compacted
+        CK(c->d_s32.ensure((size_t)n_sub * K));
+        CK(launch_dist_prep(in, c->d_sw.p, c->d_dw.p, c->d_s32.p, n_sub, stride, c->stream));
+        sub_stride = 1;
+      }
       CK(launch_dist_fast(c->d_s32.p, c->d_sw.p, c->d_dw.p, P, G, K, nullptr, nullptr, nullptr, nullptr, 0,
-                          c->d_esub.p, stride, n_sub, c->stream));
+                          c->d_esub.p, sub_stride, n_sub, c->stream));
       CK(launch_dist_threshold(c->d_esub.p, n_sub, G, k_sub, c->d_b0.p, b1, c->d_X.p, c->stream));
       if (dmode) {
         // about k_sub of every n_sub particles per gene pass X: size the per-CTA

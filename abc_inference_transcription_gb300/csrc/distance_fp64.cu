@@ -8,9 +8,11 @@
 
 namespace abc {
 
-__global__ void dist_prep_kernel(DistInputs in, float* sw, float* dw, float* s32) {
+// sw, dw for every (g, k); s32[r][k] = stats[r * stride][k] for r < s32_rows.
+__global__ void dist_prep_kernel(DistInputs in, float* sw, float* dw, float* s32, int64_t s32_rows,
+                                 int64_t stride) {
   const int64_t n_gk = in.G * in.K;
-  const int64_t n_pk = in.P * in.K;
+  const int64_t n_pk = s32 ? s32_rows * in.K : 0;
   const double sig2 = 0.1 * 0.1;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_gk + n_pk;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -22,34 +24,58 @@ __global__ void dist_prep_kernel(DistInputs in, float* sw, float* dw, float* s32
       sw[i] = (float)a;
       dw[i] = (float)(a * d);
     } else {
-      s32[i - n_gk] = (float)in.stats[i - n_gk];
+      const int64_t j = i - n_gk;
+      const int64_t r = j / in.K, k = j - r * in.K;
+      s32[j] = (float)in.stats[(r * stride) * in.K + k];
     }
   }
 }
 
-cudaError_t launch_dist_prep(const DistInputs& in, float* sw, float* dw, float* s32, cudaStream_t s) {
-  const int64_t n = (in.G + in.P) * in.K;
+cudaError_t launch_dist_prep(const DistInputs& in, float* sw, float* dw, float* s32, int64_t s32_rows,
+                             int64_t stride, cudaStream_t s) {
+  const int64_t n = in.G * in.K + (s32 ? s32_rows * in.K : 0);
   if (n <= 0) return cudaSuccess;
   int blocks = (int)((n + 255) / 256 < 65536 ? (n + 255) / 256 : 65536);
-  dist_prep_kernel<<<blocks, 256, 0, s>>>(in, sw, dw, s32);
+  dist_prep_kernel<<<blocks, 256, 0, s>>>(in, sw, dw, s32, s32_rows, stride);
   return cudaGetLastError();
 }
 
-// err of one (p, g) pair exactly as compute_trunc_errors / nlsqerror_part.
+__device__ __forceinline__ double den_term(double d, double e) {
+  const double sig2 = 0.1 * 0.1;
+  const double eps = (e + d != 0.0) ? 0.0 : 0.0001;
+  return (e * e + sig2 * (d * d)) + eps;
+}
+
+__global__ void dist_den_kernel(DistInputs in, double* den) {
+  const int64_t n = in.G * in.K;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    den[i] = den_term(in.data[i], in.se[i]);
+}
+
+cudaError_t launch_dist_den(const DistInputs& in, double* den, cudaStream_t s) {
+  const int64_t n = in.G * in.K;
+  if (n <= 0) return cudaSuccess;
+  int blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+  dist_den_kernel<<<blocks, 256, 0, s>>>(in, den);
+  return cudaGetLastError();
+}
+
+// err of one (p, g) pair exactly as compute_trunc_errors / nlsqerror_part
+// (scripts/compute_errors.jl:30-43): per family, sum of diff^2 / den in
+// order, then part / K added to the total; clipped at 10.
 __device__ __forceinline__ double err_exact(const DistInputs& in, int64_t p, int64_t g) {
   const double* s = in.stats + p * in.K;
   const double* d = in.data + g * in.K;
   const double* e = in.se + g * in.K;
-  const double sig2 = 0.1 * 0.1;
+  const double* dn = in.den ? in.den + g * in.K : nullptr;
   const double nK = (double)in.K;
   double tot = 0.0;
   int k = 0;
   for (int f = 0; f < in.n_fam; ++f) {
     double part = 0.0;
     for (int q = 0; q < in.fam[f]; ++q, ++k) {
-      const double eps = (e[k] + d[k] != 0.0) ? 0.0 : 0.0001;
       const double diff = d[k] - s[k];
-      part = part + (diff * diff) / ((e[k] * e[k] + sig2 * (d[k] * d[k])) + eps);
+      part = part + (diff * diff) / (dn ? dn[k] : den_term(d[k], e[k]));
     }
     tot = tot + part / nK;
   }
@@ -141,7 +167,10 @@ __device__ __forceinline__ bool key_less(double ea, int32_t pa, double eb, int32
   return ea < eb || (ea == eb && pa < pb);
 }
 
+constexpr int kSortSmem = 8192;  // segments up to this size sort in shared memory
+
 __global__ void __launch_bounds__(1024) segsort_kernel(const int64_t* goff, int32_t* sp, double* se64) {
+  extern __shared__ double sort_smem[];
   const int64_t g = blockIdx.x;
   const int64_t base = goff[g];
   const int64_t n = goff[g + 1] - base;
@@ -150,6 +179,39 @@ __global__ void __launch_bounds__(1024) segsort_kernel(const int64_t* goff, int3
   double* E = se64 + base;
   int64_t n2 = 1;
   while (n2 < n) n2 <<= 1;
+  if (n2 <= kSortSmem) {
+    double* Es = sort_smem;
+    int32_t* Ps = reinterpret_cast<int32_t*>(sort_smem + kSortSmem);
+    const int m = (int)n;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+      Es[i] = E[i];
+      Ps[i] = P[i];
+    }
+    __syncthreads();
+    for (int k = 2; k <= (int)n2; k <<= 1) {
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        for (int i = threadIdx.x; i < (int)n2; i += blockDim.x) {
+          const int partner = (j == (k >> 1)) ? (i ^ (k - 1)) : (i ^ j);
+          if (partner > i && partner < m) {
+            const double ea = Es[i], eb = Es[partner];
+            const int32_t pa = Ps[i], pb = Ps[partner];
+            if (key_less(eb, pb, ea, pa)) {
+              Es[i] = eb;
+              Es[partner] = ea;
+              Ps[i] = pb;
+              Ps[partner] = pa;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    }
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+      E[i] = Es[i];
+      P[i] = Ps[i];
+    }
+    return;
+  }
   for (int64_t k = 2; k <= n2; k <<= 1) {
     for (int64_t j = k >> 1; j > 0; j >>= 1) {
       for (int64_t i = threadIdx.x; i < n2; i += blockDim.x) {
@@ -189,7 +251,14 @@ cudaError_t launch_dist_group_sort(const Cand* cand, const double* e64, int64_t 
   if (n > 0) {
     int blocks = (int)((n + 255) / 256 < 65536 ? (n + 255) / 256 : 65536);
     scatter_kernel<<<blocks, 256, 0, s>>>(cand, e64, n, goff, gcursor, sp, se64);
-    segsort_kernel<<<(unsigned)G, 1024, 0, s>>>(goff, sp, se64);
+    constexpr int smem = kSortSmem * (int)(sizeof(double) + sizeof(int32_t));
+    static bool attr = false;
+    if (!attr) {
+      err = cudaFuncSetAttribute(segsort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+      if (err) return err;
+      attr = true;
+    }
+    segsort_kernel<<<(unsigned)G, 1024, smem, s>>>(goff, sp, se64);
   }
   return cudaGetLastError();
 }

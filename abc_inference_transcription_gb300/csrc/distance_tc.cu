@@ -403,26 +403,50 @@ __device__ __forceinline__ void note_max(unsigned* slot, float v) {
   if (v == v) atomicMax(slot, __float_as_uint(fabsf(v)));
 }
 
-// A rows: [s (K) | s^2 (K) | 0 ...] per half.
+// hi/lo TF32 parts of an FP32 value: hi = tf32(x), lo = tf32(x - hi) (x - hi is exact)
+__device__ __forceinline__ void split_tf32f(float x, float& hi, float& lo) {
+  hi = tf32_rn(x);
+  lo = fabsf(hi) < INFINITY ? tf32_rn(x - hi) : 0.0f;
+}
+
+// A rows: [s (K) | s^2 (K) | 0 ...] per half, in FP32 (s rounded once from FP64,
+// s^2 = fl(s s): both within 2^-23 relative, inside the bound's rounding terms).
+// One warp per row, rows strided over the grid; the overflow monitors are
+// reduced per warp before one atomic each.
 __global__ void tc_prep_rows_kernel(const double* stats, int64_t P, int K, int KA, int NH, float* A,
                                     unsigned* flags) {
-  const int64_t n = P * (int64_t)KA;
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   const int64_t ld = (int64_t)NH * KA;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t p = i / KA;
-    const int k = (int)(i - p * KA);
-    double v = 0.0;
-    if (k < 2 * K) {
-      const double s = stats[p * K + (k < K ? k : k - K)];
-      v = k < K ? s : s * s;
-      const float f = (float)v;
-      if (fabsf(f) == INFINITY) atomicOr(&flags[0], 1u);
-      if (k >= K) note_max(&flags[2], f);
+  unsigned inf = 0, mx = 0;
+  for (int64_t p = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); p < P; p += warps) {
+    const double* srow = stats + p * K;
+    float* arow = A + p * ld;
+    for (int k = lane; k < K; k += 32) {
+      const float sv = (float)srow[k];
+      const float s2 = sv * sv;
+      float h1, l1, h2, l2;
+      split_tf32f(sv, h1, l1);
+      split_tf32f(s2, h2, l2);
+      arow[k] = h1;
+      arow[K + k] = h2;
+      if (NH == 2) {
+        arow[KA + k] = l1;
+        arow[KA + K + k] = l2;
+      }
+      if (fabsf(sv) == INFINITY || fabsf(s2) == INFINITY) inf = 1u;
+      if (s2 == s2) mx = max(mx, __float_as_uint(s2));
     }
-    float hi, lo;
-    split_tf32(v, hi, lo);
-    A[p * ld + k] = hi;
-    if (NH == 2) A[p * ld + KA + k] = lo;
+    for (int k = 2 * K + lane; k < KA; k += 32) {
+      arow[k] = 0.0f;
+      if (NH == 2) arow[KA + k] = 0.0f;
+    }
+  }
+  inf = __reduce_or_sync(0xffffffffu, inf);
+  mx = __reduce_max_sync(0xffffffffu, mx);
+  if (lane == 0) {
+    if (inf) atomicOr(&flags[0], 1u);
+    if (mx) atomicMax(&flags[2], mx);
   }
 }
 
@@ -554,9 +578,8 @@ cudaError_t launch_tc_prep(const DistInputs& in, int nh, double beta, float* A, 
                            float* b0, unsigned* flags, cudaStream_t s) {
   const int KA = tc_ka(in.K);
   if (in.P > 0) {
-    const int64_t n = in.P * (int64_t)KA;
-    int blocks = (int)((n + 255) / 256 < 65536 ? (n + 255) / 256 : 65536);
-    tc_prep_rows_kernel<<<blocks, 256, 0, s>>>(in.stats, in.P, in.K, KA, nh, A, flags);
+    const int64_t blocks = (in.P + 7) / 8 < 8192 ? (in.P + 7) / 8 : 8192;
+    tc_prep_rows_kernel<<<(unsigned)blocks, 256, 0, s>>>(in.stats, in.P, in.K, KA, nh, A, flags);
   }
   if (in.G > 0)
     tc_prep_genes_kernel<<<(unsigned)((in.G + 127) / 128), 128, 0, s>>>(in.data, in.se, in.G, in.K, KA, nh, beta,

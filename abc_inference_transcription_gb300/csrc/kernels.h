@@ -53,6 +53,7 @@ struct DistInputs {
   const double* data;   // [G][K]
   const double* se;     // [G][K]
   const double* stats;  // [P][K]
+  const double* den = nullptr;  // [G][K] (se^2 + 0.01 d^2) + eps, or null (computed per term)
   int64_t G, P;
   int K;
   int n_fam;
@@ -90,7 +91,9 @@ cudaError_t launch_tc_gather(const Cand* seg, const float* seg_e, const unsigned
                              Cand* out, float* out_e, cudaStream_t s);
 
 // per (g,k): sw = sqrt(w), dw = sqrt(w) d in FP32, w = 1/((se^2 + 0.01 d^2) + eps)
-cudaError_t launch_dist_prep(const DistInputs& in, float* sw, float* dw, float* s32, cudaStream_t s);
+// and s32[r][k] = stats[r stride][k] in FP32 for r < s32_rows (s32 may be null)
+cudaError_t launch_dist_prep(const DistInputs& in, float* sw, float* dw, float* s32, int64_t s32_rows,
+                             int64_t stride, cudaStream_t s);
 // FP32 direct distance: emit (p, g) with min(10, err32) <= X[g] (mode emit), or
 // write err32 of the particles p = row*stride into esub[row][g] (mode sample).
 cudaError_t launch_dist_fast(const float* s32, const float* sw, const float* dw, int64_t P, int64_t G, int K,
@@ -113,6 +116,9 @@ cudaError_t launch_x_from_thr(const double* thr, double eps, int64_t G, const fl
 cudaError_t launch_refine(const Cand* cand, const float* cand_e, int64_t n, int64_t G, int64_t k, const float* X,
                           const float* b0, float b1, unsigned int* hist, float* Xt, Cand* out,
                           unsigned long long* count, cudaStream_t s);
+// den[g][k] = (se^2 + 0.01 d^2) + eps_gk, the denominators of the error terms,
+// evaluated as in the per-term FP64 expression (bit-identical).
+cudaError_t launch_dist_den(const DistInputs& in, double* den, cudaStream_t s);
 // FP64 error of each candidate, in the reference's operation order.
 cudaError_t launch_dist_recheck(const DistInputs& in, const Cand* cand, int64_t n, double* e64, cudaStream_t s);
 // group candidates by gene and sort each gene's list by (err, p).

@@ -587,7 +587,7 @@ int abc_surrogate_screen_device(abc_surrogate* s, const double* d_theta, int ld_
   in.K = K;
   in.n_fam = 1;
   in.fam[0] = K;
-  SK(launch_dist_prep(in, s->sw.p, s->dw.p, nullptr, s->stream));
+  SK(launch_dist_prep(in, s->sw.p, s->dw.p, nullptr, 0, 1, s->stream));
   std::vector<float> hx((size_t)G);
   for (int64_t g = 0; g < G; ++g) hx[g] = (float)(thr[g] + margin);
   SK(cudaMemcpyAsync(s->X.p, hx.data(), sizeof(float) * G, cudaMemcpyHostToDevice, s->stream));
