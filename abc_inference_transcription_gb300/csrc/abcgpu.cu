@@ -77,7 +77,7 @@ struct abc_ctx {
   size_t ev_used = 0;
   double phase_ms[3] = {0, 0, 0};
   // selection workspace and results
-  DBuf<double> d_data, d_se, d_sel_stats, d_e64, d_se64, d_out_err, d_den;
+  DBuf<double> d_data, d_se, d_sel_stats, d_e64, d_se64, d_out_err, d_den, d_rden;
   DBuf<float> d_sw, d_dw, d_s32, d_X, d_esub;
   DBuf<Cand> d_cand;
   DBuf<float> d_cande;  // FP32 error of each candidate
@@ -213,7 +213,7 @@ int abc_destroy(abc_ctx* c) {
   c->d_data.release(); c->d_se.release(); c->d_sel_stats.release(); c->d_e64.release(); c->d_se64.release();
   c->d_out_err.release(); c->d_sw.release(); c->d_dw.release(); c->d_s32.release(); c->d_X.release();
   c->d_esub.release(); c->d_cand.release(); c->d_sp.release(); c->d_gcount.release(); c->d_goff.release();
-  c->d_cande.release(); c->d_den.release(); c->d_tcA.release(); c->d_tcB.release(); c->d_cg32.release(); c->d_b0.release();
+  c->d_cande.release(); c->d_den.release(); c->d_rden.release(); c->d_tcA.release(); c->d_tcB.release(); c->d_cg32.release(); c->d_b0.release();
   c->d_Y.release(); c->d_Xt.release(); c->d_seg_e.release(); c->d_cg64.release(); c->d_tcflags.release();
   c->d_segcount.release(); c->d_hist.release(); c->d_tcerr.release(); c->d_seg.release(); c->d_cand2.release();
   c->d_alen.release(); c->d_aoff.release(); c->d_out_idx.release(); c->d_gcursor.release();
@@ -688,8 +688,10 @@ static int load_dist_inputs(abc_ctx* c, const double* data, const double* se, in
   in.data = c->d_data.p;
   in.se = c->d_se.p;
   CK(c->d_den.ensure((size_t)G * K));
-  CK(launch_dist_den(in, c->d_den.p, c->stream));
+  CK(c->d_rden.ensure((size_t)G * K));
+  CK(launch_dist_den(in, c->d_den.p, c->d_rden.p, c->stream));
   in.den = c->d_den.p;
+  in.rden = c->d_rden.p;
   if (stats_on_device) {
     in.stats = stats;
   } else {

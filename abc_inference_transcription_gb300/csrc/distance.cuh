@@ -29,6 +29,26 @@ ABC_HDF float dist_bound_f(float e, int K) {
   return 1.5f * u * (64.0f * sqrtf(e) + (float)(K + 8) * e) + 1e-30f;
 }
 
+#if defined(__CUDACC__)
+// Correctly rounded a / b (round to nearest) from y = RN(1/b), in three FP64
+// operations instead of a full division: q0 = RN(a y) is within one ulp of
+// a / b, the remainder r = a - b q0 is exact (one FMA), and RN(q0 + r y) =
+// RN(a / b) (Markstein's theorem: P. Markstein, IBM J. Res. Dev. 34(1), 1990;
+// J.-M. Muller et al., Handbook of Floating-Point Arithmetic, ch. 4).  The
+// theorem needs a, b and the quotient away from underflow and overflow; outside
+// [2^-900, 2^900] x [2^-400, 2^400] (and for zero, NaN, infinity) the IEEE
+// division is used.
+__device__ __forceinline__ double div_rn(double a, double b, double y) {
+  const double fa = fabs(a), fb = fabs(b);
+  if (fa >= 0x1p-900 && fa <= 0x1p+900 && fb >= 0x1p-400 && fb <= 0x1p+400) {
+    const double q0 = a * y;
+    const double r = fma(-q0, b, a);
+    return fma(r, y, q0);
+  }
+  return a / b;
+}
+#endif
+
 constexpr int kDistTile = 128;  // particles and genes per CTA tile
 constexpr int kDistKc = 16;     // statistics per shared-memory stage
 constexpr int kHistBins = 4096; // threshold histogram bins (sqrt scale on [0, 10])

@@ -46,17 +46,20 @@ __device__ __forceinline__ double den_term(double d, double e) {
   return (e * e + sig2 * (d * d)) + eps;
 }
 
-__global__ void dist_den_kernel(DistInputs in, double* den) {
+__global__ void dist_den_kernel(DistInputs in, double* den, double* rden) {
   const int64_t n = in.G * in.K;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    den[i] = den_term(in.data[i], in.se[i]);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double b = den_term(in.data[i], in.se[i]);
+    den[i] = b;
+    rden[i] = 1.0 / b;
+  }
 }
 
-cudaError_t launch_dist_den(const DistInputs& in, double* den, cudaStream_t s) {
+cudaError_t launch_dist_den(const DistInputs& in, double* den, double* rden, cudaStream_t s) {
   const int64_t n = in.G * in.K;
   if (n <= 0) return cudaSuccess;
   int blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
-  dist_den_kernel<<<blocks, 256, 0, s>>>(in, den);
+  dist_den_kernel<<<blocks, 256, 0, s>>>(in, den, rden);
   return cudaGetLastError();
 }
 
@@ -67,17 +70,30 @@ __device__ __forceinline__ double err_exact(const DistInputs& in, int64_t p, int
   const double* s = in.stats + p * in.K;
   const double* d = in.data + g * in.K;
   const double* e = in.se + g * in.K;
-  const double* dn = in.den ? in.den + g * in.K : nullptr;
   const double nK = (double)in.K;
   double tot = 0.0;
   int k = 0;
-  for (int f = 0; f < in.n_fam; ++f) {
-    double part = 0.0;
-    for (int q = 0; q < in.fam[f]; ++q, ++k) {
-      const double diff = d[k] - s[k];
-      part = part + (diff * diff) / (dn ? dn[k] : den_term(d[k], e[k]));
+  if (in.den) {
+    const double* dn = in.den + g * in.K;
+    const double* ry = in.rden + g * in.K;
+    const double rK = 1.0 / nK;
+    for (int f = 0; f < in.n_fam; ++f) {
+      double part = 0.0;
+      for (int q = 0; q < in.fam[f]; ++q, ++k) {
+        const double diff = d[k] - s[k];
+        part = part + div_rn(diff * diff, dn[k], ry[k]);
+      }
+      tot = tot + div_rn(part, nK, rK);
     }
-    tot = tot + part / nK;
+  } else {
+    for (int f = 0; f < in.n_fam; ++f) {
+      double part = 0.0;
+      for (int q = 0; q < in.fam[f]; ++q, ++k) {
+        const double diff = d[k] - s[k];
+        part = part + (diff * diff) / den_term(d[k], e[k]);
+      }
+      tot = tot + part / nK;
+    }
   }
   if (tot > 10.0) tot = 10.0;
   return tot;

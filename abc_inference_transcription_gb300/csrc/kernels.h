@@ -53,7 +53,8 @@ struct DistInputs {
   const double* data;   // [G][K]
   const double* se;     // [G][K]
   const double* stats;  // [P][K]
-  const double* den = nullptr;  // [G][K] (se^2 + 0.01 d^2) + eps, or null (computed per term)
+  const double* den = nullptr;   // [G][K] (se^2 + 0.01 d^2) + eps, or null (computed per term)
+  const double* rden = nullptr;  // [G][K] RN(1 / den) (with den)
   int64_t G, P;
   int K;
   int n_fam;
@@ -117,8 +118,8 @@ cudaError_t launch_refine(const Cand* cand, const float* cand_e, int64_t n, int6
                           const float* b0, float b1, unsigned int* hist, float* Xt, Cand* out,
                           unsigned long long* count, cudaStream_t s);
 // den[g][k] = (se^2 + 0.01 d^2) + eps_gk, the denominators of the error terms,
-// evaluated as in the per-term FP64 expression (bit-identical).
-cudaError_t launch_dist_den(const DistInputs& in, double* den, cudaStream_t s);
+// evaluated as in the per-term FP64 expression (bit-identical), and rden = 1/den.
+cudaError_t launch_dist_den(const DistInputs& in, double* den, double* rden, cudaStream_t s);
 // FP64 error of each candidate, in the reference's operation order.
 cudaError_t launch_dist_recheck(const DistInputs& in, const Cand* cand, int64_t n, double* e64, cudaStream_t s);
 // group candidates by gene and sort each gene's list by (err, p).

@@ -5,6 +5,10 @@ expanded as K err = c_g + [s | s^2] . [-2 w d | w]).
 Every candidate error lies within the stated bound of the exact FP64 error,
 and the accepted sets after the FP64 recheck are identical to the oracle's in
 every mode (eps, top-q and per-gene thresholds)."""
+import ctypes as C
+import os
+import subprocess
+
 import numpy as np
 import pytest
 
@@ -124,3 +128,21 @@ def test_many_tiles_topq_and_segment_growth(Ctx, orc, mode):
         e32, b0, b1, _ = ctx.errors_candidate(data[:300], se[:300], stats[:40000])
     E = np.minimum(_exact_unclipped(data[:300], se[:300], stats[:40000]), 10.0)
     assert (np.abs(e32 - E) <= b0[None, :] + b1 * E).all()
+
+
+def test_markstein_division_matches_ieee(tmp_path):
+    """The FP64 recheck divides through div_rn (three operations from RN(1/b));
+    it must equal the IEEE quotient bit for bit, here on 2^30 operand pairs
+    including all-ones significands, powers of two, squares, exact quotients
+    and the fallback range."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    so = tmp_path / "libdivrn.so"
+    subprocess.run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-fmad=false",
+                    "-shared", "-Xcompiler", "-fPIC", os.path.join(root, "tests", "gpu_helpers", "div_rn.cu"),
+                    "-o", str(so)], check=True)
+    lib = C.CDLL(str(so))
+    for seed in (1, 0xABCDEF):
+        bad = C.c_ulonglong(0)
+        first = (C.c_double * 4)()
+        assert lib.div_rn_check(C.c_ulonglong(1 << 30), C.c_ulonglong(seed), C.byref(bad), first) == 0
+        assert bad.value == 0, list(first)
