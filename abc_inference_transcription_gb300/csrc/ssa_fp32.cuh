@@ -137,10 +137,21 @@ __global__ void __launch_bounds__(128, MINB) ssa_kernel_f32(SsaArgs A) {
   StepRates q;
   float koff = 0.f, lam = 0.f, beta = 0.f, scal = 0.f;
   bool active = false, done = false;
+  // Random words: each iteration consumes two words of the lane's stream
+  // (blocks 1, 2, ... of its (cell, particle) counter, in order).  cur holds
+  // the block being read (half: its z, w next), nxt the following one.  New
+  // blocks are computed on even warp iterations only, by every lane whose nxt
+  // is empty, so the Philox rounds run for the whole warp every other
+  // iteration; two words per iteration and four per refill keep cur + nxt
+  // from running dry whatever the iteration at which an item starts.
+  U4 cur = {0u, 0u, 0u, 0u}, nxt = {0u, 0u, 0u, 0u};
+  bool half = false, has_nxt = false;
+  uint32_t it = 0;
   unsigned long long tot_ev = 0, tot_rej = 0;
   int err = 0;
   s.plocal = 0;
   while (true) {
+    ++it;
     const bool need = !active && !done;
     const unsigned mask = __ballot_sync(FULL, need);
     if (mask) {
@@ -175,6 +186,10 @@ __global__ void __launch_bounds__(128, MINB) ssa_kernel_f32(SsaArgs A) {
           s.block = 0;
           const U4 w = main_block(s, A.rk);
           s.block = 1;
+          cur = main_block(s, A.rk);
+          s.block = 2;
+          half = false;
+          has_nxt = false;
           s.G = ((double)w.x * ABC_TWO_M32 < R.g0) ? 1 : 0;
           s.uu = floorf((float)R.u0 + 0.5f);
           s.us = SPLICE ? floorf((float)R.s0 + 0.5f) : 0.0f;
@@ -211,9 +226,23 @@ __global__ void __launch_bounds__(128, MINB) ssa_kernel_f32(SsaArgs A) {
       c6 = fmaf(q.gam, s.us, c5);
       a0 = c6 + a_last;
     }
-    const U4 w = main_block(s, A.rk);
-    s.block++;
-    const float U1 = 1.0f - u23(w.x);  // (0, 1]
+    if ((it & 1u) == 0u && !has_nxt) {
+      nxt = main_block(s, A.rk);
+      s.block++;
+      has_nxt = true;
+    }
+    const uint32_t wt = half ? cur.z : cur.x;  // waiting time (top 23 bits)
+    const uint32_t wc = half ? cur.w : cur.y;  // channel (top 23 bits)
+    if (half) {
+      if (!has_nxt) {  // not reached by the refill schedule; keeps the stream order regardless
+        nxt = main_block(s, A.rk);
+        s.block++;
+      }
+      cur = nxt;
+      has_nxt = false;
+    }
+    half = !half;
+    const float U1 = 1.0f - u23(wt);  // (0, 1]
     const float tau = __fdividef(-__logf(U1), a0);
     const float y = tau - s.comp;
     const float tt = s.el + y;
@@ -262,13 +291,15 @@ __global__ void __launch_bounds__(128, MINB) ssa_kernel_f32(SsaArgs A) {
     // ---- event: predicated channel update
     s.el = tt;
     s.comp = nc;
-    const float r = u23(w.y) * a0;
+    const float r = u23(wc) * a0;
     const bool b1 = r >= c1, b2 = r >= c2, b3 = r >= c3, b4 = r >= c4;
     const float size = fmaf(s.ph0 + (s.el - s.comp), invT, 1.0f);
     const float sz_lin = fmaf(scal, size - 1.0f, 1.0f);          // exact for s in {0, 1}
     const float sz_pow = exp2f(scal * __log2f(size));
     const float at = q.alp * ((scal == 0.0f || scal == 1.0f) ? sz_lin : sz_pow);
-    const float v = u23(w.z) * q.amax;  // thinning uniform x bound
+    // thinning uniform from the 9 low bits of both words (18 bits), x bound
+    const uint32_t th = ((wt & 0x1FFu) << 9) | (wc & 0x1FFu);
+    const float v = (__uint_as_float(0x3F800000u | (th << 5)) - 1.0f) * q.amax;
     const bool tx = b2 && !b3;
     const bool acc = tx && (v < at);
     const bool lab = acc && (v < at * s.lam_cur);
