@@ -29,6 +29,7 @@ UNITS = {
     "distance_fp64.cu": ["-fmad=false"],
     "distance_fp32.cu": [],
     "distance_tc.cu": [],
+    "posterior.cu": ["-fmad=false"],
     "noalloc.cu": [],
     "mlp.cu": [],
     "surrogate.cu": [],

@@ -99,7 +99,7 @@ struct abc_ctx {
   double sel_fast_ms = 0.0;  // candidate-pass kernel time of the last selection (abc_profile)
   int sel_fast_passes = 0;
   int64_t cand_cap = int64_t(1) << 22;
-  int64_t sel_G = 0, sel_total = 0, sel_cands = 0, sel_rechecked = 0, sel_cands_emitted = 0;
+  int64_t sel_G = 0, sel_P = 0, sel_total = 0, sel_cands = 0, sel_rechecked = 0, sel_cands_emitted = 0;
   bool sel_ready = false;
 };
 
@@ -1007,6 +1007,7 @@ static int select_impl(abc_ctx* c, const double* data, const double* se, int64_t
                          c->stream));
   CK(cudaStreamSynchronize(c->stream));
   c->sel_G = G;
+  c->sel_P = P;
   c->sel_total = total;
   c->sel_cands = c->sel_cands_emitted;
   c->sel_ready = true;
@@ -1089,6 +1090,77 @@ int abc_select_profile_read(const abc_ctx* c, double* fast_ms, int* fast_passes)
   if (!c) return ABC_ERR_INVALID;
   if (fast_ms) *fast_ms = c->sel_fast_ms;
   if (fast_passes) *fast_passes = c->sel_fast_passes;
+  return ABC_OK;
+}
+
+int abc_model_probs(abc_ctx* c, const int64_t* counts, int64_t G, int M, int n_boot, double alpha, uint64_t seed,
+                    double* prob, double* lb, double* ub) {
+  if (!c) return ABC_ERR_INVALID;
+  if (!counts || !prob || !lb || !ub || G < 0 || M < 1 || M > 64 || n_boot < 1 || n_boot > 100000 ||
+      !(alpha > 0.0 && alpha < 1.0))
+    return fail(c, ABC_ERR_INVALID, "abc_model_probs: bad arguments");
+  for (int64_t i = 0; i < G * M; ++i)
+    if (counts[i] < 0) return fail(c, ABC_ERR_INVALID, "abc_model_probs: negative count");
+  if (G == 0) return ABC_OK;
+  DBuf<int64_t> d_counts;
+  DBuf<double> d_out, d_boot;
+  cudaError_t e = d_counts.ensure((size_t)G * M);
+  if (e == cudaSuccess) e = d_out.ensure((size_t)3 * G * M);
+  if (e == cudaSuccess) e = d_boot.ensure((size_t)G * M * n_boot);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_counts.p, counts, sizeof(int64_t) * G * M, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess)
+    e = launch_model_probs(d_counts.p, G, M, n_boot, alpha, seed, d_out.p, d_out.p + G * M, d_out.p + 2 * G * M,
+                           d_boot.p, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(prob, d_out.p, sizeof(double) * G * M, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(lb, d_out.p + G * M, sizeof(double) * G * M, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(ub, d_out.p + 2 * G * M, sizeof(double) * G * M, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  d_counts.release();
+  d_out.release();
+  d_boot.release();
+  if (e != cudaSuccess) return cuda_fail(c, e, "abc_model_probs");
+  return ABC_OK;
+}
+
+int abc_posterior_summary(abc_ctx* c, const double* theta, int64_t ld, int npar, int theta_on_device, double q,
+                          double* map, double* mean, double* lb, double* ub, int64_t* n_particles) {
+  if (!c) return ABC_ERR_INVALID;
+  if (!c->sel_ready) return fail(c, ABC_ERR_STATE, "no selection result: call abc_errors_select first");
+  if (!theta || !map || !mean || !lb || !ub || npar < 1 || ld < npar || !(q > 0.0 && q < 1.0))
+    return fail(c, ABC_ERR_INVALID, "abc_posterior_summary: bad arguments");
+  const int64_t G = c->sel_G, P = c->sel_P, total = c->sel_total;
+  DBuf<double> d_theta, d_scr, d_out;
+  DBuf<int64_t> d_n;
+  const double* th = theta;
+  cudaError_t e = cudaSuccess;
+  if (!theta_on_device) {
+    e = d_theta.ensure((size_t)P * ld);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_theta.p, theta, sizeof(double) * P * ld, cudaMemcpyHostToDevice, c->stream);
+    th = d_theta.p;
+  }
+  if (e == cudaSuccess) e = d_scr.ensure((size_t)std::max<int64_t>(total, 1) * npar);
+  if (e == cudaSuccess) e = d_out.ensure((size_t)4 * G * npar);
+  if (e == cudaSuccess) e = d_n.ensure((size_t)G);
+  if (e == cudaSuccess)
+    e = launch_posterior_summary(c->d_aoff.p, c->d_out_idx.p, G, total, th, ld, npar, q, d_scr.p, d_out.p,
+                                 d_out.p + G * npar, d_out.p + 2 * G * npar, d_out.p + 3 * G * npar, d_n.p,
+                                 c->stream);
+  double* outs[4] = {map, mean, lb, ub};
+  for (int i = 0; i < 4 && e == cudaSuccess; ++i)
+    e = cudaMemcpyAsync(outs[i], d_out.p + (size_t)i * G * npar, sizeof(double) * G * npar, cudaMemcpyDeviceToHost,
+                        c->stream);
+  if (e == cudaSuccess && n_particles)
+    e = cudaMemcpyAsync(n_particles, d_n.p, sizeof(int64_t) * G, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  d_theta.release();
+  d_scr.release();
+  d_out.release();
+  d_n.release();
+  if (e != cudaSuccess) return cuda_fail(c, e, "abc_posterior_summary");
   return ABC_OK;
 }
 

@@ -139,6 +139,14 @@ cudaError_t launch_scan(const int64_t* cnt, int64_t G, int64_t* off, cudaStream_
 // full FP64 error matrix [P][G]
 cudaError_t launch_dist_full(const DistInputs& in, double* err, cudaStream_t s);
 
+// model probabilities with bootstrap intervals and per-gene posterior summaries (posterior.cu)
+cudaError_t launch_model_probs(const int64_t* counts, int64_t G, int M, int n_boot, double alpha, uint64_t seed,
+                               double* prob, double* lb, double* ub, double* boot, cudaStream_t s);
+cudaError_t launch_posterior_summary(const int64_t* aoff, const int64_t* idx, int64_t G, int64_t total,
+                                     const double* theta, int64_t ld, int npar, double q, double* scratch,
+                                     double* map, double* mean, double* lb, double* ub, int64_t* n_out,
+                                     cudaStream_t s);
+
 cudaError_t launch_prior(const PriorArgs& a, cudaStream_t s);
 cudaError_t launch_setup(const SetupArgs& a, cudaStream_t s);
 cudaError_t launch_ssa_fp64(const SsaArgs& a, int grid, cudaStream_t s);

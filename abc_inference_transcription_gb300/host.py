@@ -207,13 +207,10 @@ class Context:
         tot = C.c_int64()
         self._check(self.lib.abc_errors_select(self.h, ptr(d), ptr(e), G, K, nf, ptr(f, C.c_int32), ptr(s),
                                                s.shape[0], mode, float(eps_or_q), C.byref(tot)))
-        off = np.zeros(G + 1, np.int64)
-        idx = np.zeros(max(tot.value, 1), np.int64)
-        err = np.zeros(max(tot.value, 1))
-        self._check(self.lib.abc_accept_fetch(self.h, ptr(off, C.c_int64), ptr(idx, C.c_int64), ptr(err)))
-        return off, idx[:tot.value], err[:tot.value]
+        return self._fetch(G, tot.value)
 
     def _fetch(self, G: int, total: int):
+        self._sel_G = G
         off = np.zeros(G + 1, np.int64)
         idx = np.zeros(max(total, 1), np.int64)
         err = np.zeros(max(total, 1))
@@ -259,6 +256,34 @@ class Context:
         self._check(self.lib.abc_select_counters(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
+    def model_probs(self, counts: np.ndarray, n_boot: int = 100, alpha: float = 0.95, seed: int = 1):
+        """(prob, lower, upper) [G, M] from accepted counts [G, M] (scripts/model_probs.jl)."""
+        cnt = np.ascontiguousarray(counts, np.int64)
+        G, M = cnt.shape
+        out = [np.zeros((G, M)) for _ in range(3)]
+        self._check(self.lib.abc_model_probs(self.h, ptr(cnt, C.c_int64), G, M, int(n_boot), float(alpha),
+                                             C.c_uint64(seed), *[ptr(o) for o in out]))
+        return tuple(out)
+
+    def posterior_summary(self, theta, npar: int | None = None, q: float = 0.95, on_device: bool = False,
+                          ld: int | None = None) -> dict:
+        """MAP, mean, quantile bounds [G, npar] and particle counts [G] of the last
+        selection (scripts/posterior_kinetics.jl:1-33).  theta: host array [P, ld]
+        or, with on_device, a device pointer (then pass npar and ld)."""
+        if on_device:
+            tp, ld_ = C.c_void_p(theta), int(ld)
+        else:
+            th = np.ascontiguousarray(theta, np.float64)
+            tp, ld_ = ptr(th), th.shape[1]
+            npar = npar or ld_
+        G = int(self._sel_G)
+        outs = [np.zeros((G, npar)) for _ in range(4)]
+        n = np.zeros(G, np.int64)
+        self._check(self.lib.abc_posterior_summary(self.h, C.cast(tp, C.POINTER(C.c_double)), ld_, npar,
+                                                   1 if on_device else 0, float(q), *[ptr(o) for o in outs],
+                                                   ptr(n, C.c_int64)))
+        return {"map": outs[0], "mean": outs[1], "lower": outs[2], "upper": outs[3], "n_particles": n}
+
     def set_distance_mode(self, mode: int) -> None:
         """Candidate pass: 0 FP32 CUDA cores, 1 TF32 tensor cores (one term),
         2 TF32 tensor cores with hi/lo splits (default)."""
@@ -269,6 +294,40 @@ class Context:
         a, b = C.c_int(), C.c_int()
         self._check(self.lib.abc_get_distance_mode(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+
+# ---------------------------------------------------------------------------
+# Downstream of the acceptance, with the reference's names
+# (scripts/model_probs.jl, scripts/posterior_kinetics.jl).
+# ---------------------------------------------------------------------------
+def get_model_probs(ctx: Context, counts: np.ndarray, alpha: float = 0.95, n_bootstraps: int = 100,
+                    seed: int = 1):
+    """Model probabilities with bootstrap bounds per gene (model_probs.jl:1-28
+    and the per-gene cases :41-48).  counts[g, m]: accepted particles of model
+    group m (the reference groups constant + constant-non-scaling against the
+    three varying models)."""
+    return ctx.model_probs(counts, n_boot=n_bootstraps, alpha=alpha, seed=seed)
+
+
+def get_n_particles(offsets: np.ndarray) -> np.ndarray:
+    """Accepted particles per gene (posterior_kinetics.jl:1-8; an empty list is 0)."""
+    return np.diff(np.asarray(offsets, np.int64))
+
+
+def get_burst_kinetics(sets: np.ndarray, model: int, n_steps: int = 5) -> np.ndarray:
+    """log10 [burst frequency, burst size, synthesis rate, decay rate]
+    (posterior_kinetics.jl:50-55): columns kon, alpha - koff, alpha, gamma with
+    the varying rate's columns kept (vary map of model.jl:30-43)."""
+    sets = np.asarray(sets, np.float64)
+    nv = n_steps if model >= 3 else 1
+    w = {1: 0, 2: 0, 3: 1, 4: 3, 5: 4}[model]   # index of the varying rate among kon, koff, alpha, gamma (+1)
+    cols, c = [], 0
+    for r in range(4):                            # kon, koff, alpha, gamma
+        n = nv if (w and r == w - 1) else 1
+        cols.append(list(range(c, c + n)))
+        c += n
+    kon, koff, alpha, gamma = (sets[:, cc] for cc in cols)
+    return np.hstack([kon, alpha - koff, alpha, gamma])
 
 
 # ---------------------------------------------------------------------------

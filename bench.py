@@ -191,6 +191,7 @@ def distance_bench(P: int, G: int, K: int, q: float, seed: int, cpu_seconds: flo
     b = base.cpu().numpy()
     data = b[rng.integers(0, NB, G)] * (1.0 + 0.05 * rng.normal(size=(G, K)))
     se = 0.1 * np.abs(data) * rng.lognormal(0.0, 0.5, (G, K))
+    k = int(np.ceil(q * P))
     ctx = Context(make_config("hour"), None)
     try:
         ctx.profile(True)
@@ -203,16 +204,45 @@ def distance_bench(P: int, G: int, K: int, q: float, seed: int, cpu_seconds: flo
         fast_ms, passes = ctx.select_profile()
         cands, rechecked = ctx.select_counters()
         mode_used = ctx.distance_mode()[1]
+        # downstream of the acceptance: posterior summaries of the 10^7 accepted
+        # pairs (theta on the device) and model probabilities for the genes
+        theta = torch.randn((P, 9), device="cuda", dtype=torch.float64, generator=g)
+        ctx.posterior_summary(theta.data_ptr(), npar=9, on_device=True, ld=9)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.posterior_summary(theta.data_ptr(), npar=9, on_device=True, ld=9)
+        t_post = time.perf_counter() - t0
+        mp_counts = np.stack([np.diff(off), np.random.default_rng(seed).integers(0, 3 * k, G)], 1)
+        ctx.model_probs(mp_counts)
+        t0 = time.perf_counter()
+        ctx.model_probs(mp_counts)
+        t_mp = time.perf_counter() - t0
+        down = {"posterior_summary_s": t_post, "model_probs_s": t_mp,
+                "workload": f"posterior MAP/mean/95 % bounds of 9 parameters over {int(off[-1])} accepted pairs "
+                            f"in {G} genes; model probabilities of {G} genes x 2 groups, 100 bootstraps"}
+        if cpu_seconds > 0:
+            from oracle import oracle as orc
+            orc.build()
+            gs = min(G, 100)
+            th_h = theta.cpu().numpy()
+            t0 = time.perf_counter()
+            orc.posterior_summary(th_h, off[:gs + 1], idx[:off[gs]], 0.95)
+            down["cpu_posterior_summary_s_scaled"] = (time.perf_counter() - t0) * G / gs
+            t0 = time.perf_counter()
+            orc.model_probs(mp_counts)
+            down["cpu_model_probs_s"] = time.perf_counter() - t0
+            down["cpu_sample"] = f"posterior summary of the first {gs} genes scaled to {G}, one core (oracle)"
+            del th_h
+        del theta
     finally:
         ctx.close()
         sh_keep = stats[:64].cpu().numpy()
         del stats, base, pick
         torch.cuda.empty_cache()
-    k = int(np.ceil(q * P))
     out = {"workload": f"P={P} particles x K={K} statistics x G={G} genes, top {q:g} per gene",
            "pairs_per_s": P * G / dt, "seconds": dt, "accepted": int(off[-1]), "accepted_expected": k * G,
            "candidates": cands, "fp64_rechecked": rechecked, "candidate_passes": passes,
-           "distance_mode": mode_used}
+           "distance_mode": mode_used, "downstream": down}
     if mode_used in (1, 2):
         # tcgen05 TF32 MMAs issued per pass: 128 x 256 tiles, depth KA per term, 1 or 3 terms
         ka = -(-2 * K // 32) * 32

@@ -249,6 +249,30 @@ int abc_errors_candidate(abc_ctx* ctx, const double* data, const double* se, int
                          double* b0_out, double* b1_out, int* mode_used);
 
 /* ------------------------------------------------------------------------
+ * Downstream of the acceptance.
+ *
+ * Model probabilities (scripts/model_probs.jl:1-28, per-gene driver :37-62):
+ * counts[g][m] = accepted particles of model group m for gene g.  No
+ * acceptance: zeros; one group: that group's probability and bounds 1;
+ * otherwise counts / sum and the quantiles 1 - alpha and alpha (Julia's
+ * default quantile) of n_boot bootstrap resamples of the accepted model
+ * labels (the reference uses n_boot = 100, alpha = 0.95).  The resamples come
+ * from a Philox stream keyed by (seed, bootstrap, gene), not from Julia's RNG.
+ * Outputs [G][M]. */
+int abc_model_probs(abc_ctx* ctx, const int64_t* counts, int64_t n_genes, int n_groups, int n_boot, double alpha,
+                    uint64_t seed, double* prob, double* lower, double* upper);
+/* Posterior summaries of the last selection (scripts/posterior_kinetics.jl:
+ * 1-33, get_n_particles, get_posterior_estimate "map"/"mean",
+ * get_posterior_ci): per gene and parameter column the parameters of the
+ * first accepted particle (lowest error), the mean over the accepted
+ * particles (summed in list order), and the quantiles 1 - q and q; NaN for a
+ * gene without acceptance.  theta: [P][ld] with the selection's particle
+ * order, on the host or (theta_on_device) the device.  Outputs [G][npar],
+ * n_particles[G] (may be NULL). */
+int abc_posterior_summary(abc_ctx* ctx, const double* theta, int64_t ld, int npar, int theta_on_device, double q,
+                          double* map, double* mean, double* lower, double* upper, int64_t* n_particles);
+
+/* ------------------------------------------------------------------------
  * Learned pre-screen.  No reference counterpart: the reference simulates
  * every prior draw.  An ensemble of MLPs (log-parameters -> means and
  * log-variances of the statistics; 3 x 256 SiLU hidden layers; FP32 master

@@ -1103,3 +1103,97 @@ int64_t orc_accept(const double* err, int64_t P, int64_t G, int mode, double eps
   free(buf);
   return total;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Downstream of the acceptance: model probabilities with bootstrap bounds    */
+/* (model_probs.jl:1-28, per-gene cases :41-48) and posterior summaries       */
+/* (posterior_kinetics.jl:1-33).  Julia's default quantile (alpha = beta = 1).*/
+/* ------------------------------------------------------------------------- */
+static double quantile_sorted(const double* v, int64_t n, double p) {
+  double m = 1.0 + p * ((1.0 - 1.0) - 1.0);
+  double aleph = (double)n * p + m;
+  int64_t j = (int64_t)aleph;
+  if (j > n - 1) j = n - 1;
+  if (j < 1 && n > 1) j = 1;
+  double g = aleph - (double)j;
+  g = g < 0.0 ? 0.0 : (g > 1.0 ? 1.0 : g);
+  double a = n == 1 ? v[0] : v[j - 1], b = n == 1 ? v[0] : v[j];
+  if (isfinite(a) && isfinite(b)) return a + g * (b - a);
+  return (1.0 - g) * a + g * b;
+}
+
+static int cmp_dbl(const void* x, const void* y) {
+  double a = *(const double*)x, b = *(const double*)y;
+  return (a > b) - (a < b);
+}
+
+int orc_model_probs(const int64_t* counts, int64_t G, int M, int n_boot, double alpha, uint64_t seed,
+                    double* prob, double* lb, double* ub) {
+  double* bv = (double*)malloc(sizeof(double) * (size_t)M * n_boot);
+  if (!bv) return ABC_ERR_NOMEM;
+  for (int64_t g = 0; g < G; ++g) {
+    const int64_t* l = counts + g * M;
+    double *P = prob + g * M, *LB = lb + g * M, *UB = ub + g * M;
+    int64_t L = 0;
+    int nz = 0, which = -1;
+    for (int m = 0; m < M; ++m) {
+      L += l[m];
+      if (l[m] > 0) { nz++; which = m; }
+      P[m] = LB[m] = UB[m] = 0.0;
+    }
+    if (L == 0) continue;
+    if (nz == 1) { P[which] = LB[which] = UB[which] = 1.0; continue; }
+    for (int m = 0; m < M; ++m) P[m] = (double)l[m] / (double)L;
+    for (int b = 0; b < n_boot; ++b) {
+      orc_rng r;
+      rng_init(&r, seed, 3u, (uint32_t)b, (uint32_t)g);
+      int64_t nrem = L, lrem = L;
+      for (int m = 0; m < M; ++m) {
+        int64_t x;
+        if (m == M - 1 || lrem == l[m]) x = nrem;
+        else if (l[m] == 0 || nrem == 0) x = 0;
+        else x = binomial(&r, nrem, (double)l[m] / (double)lrem);
+        nrem -= x;
+        lrem -= l[m];
+        bv[(int64_t)m * n_boot + b] = (double)x / (double)L;
+      }
+    }
+    for (int m = 0; m < M; ++m) {
+      qsort(bv + (int64_t)m * n_boot, (size_t)n_boot, sizeof(double), cmp_dbl);
+      LB[m] = quantile_sorted(bv + (int64_t)m * n_boot, n_boot, 1.0 - alpha);
+      UB[m] = quantile_sorted(bv + (int64_t)m * n_boot, n_boot, alpha);
+    }
+  }
+  free(bv);
+  return ABC_OK;
+}
+
+int orc_posterior_summary(const double* theta, int64_t ld, int npar, const int64_t* off, const int64_t* idx,
+                          int64_t G, double q, double* map, double* mean, double* lb, double* ub,
+                          int64_t* n_out) {
+  int64_t maxn = 1;
+  for (int64_t g = 0; g < G; ++g)
+    if (off[g + 1] - off[g] > maxn) maxn = off[g + 1] - off[g];
+  double* v = (double*)malloc(sizeof(double) * (size_t)maxn);
+  if (!v) return ABC_ERR_NOMEM;
+  for (int64_t g = 0; g < G; ++g) {
+    const int64_t o = off[g], n = off[g + 1] - off[g];
+    if (n_out) n_out[g] = n;
+    for (int c = 0; c < npar; ++c) {
+      const int64_t t = g * npar + c;
+      if (n == 0) { map[t] = mean[t] = lb[t] = ub[t] = NAN; continue; }
+      map[t] = theta[(idx[o] - 1) * ld + c];
+      double s = 0.0;
+      for (int64_t i = 0; i < n; ++i) {
+        v[i] = theta[(idx[o + i] - 1) * ld + c];
+        s = s + v[i];
+      }
+      mean[t] = s / (double)n;
+      qsort(v, (size_t)n, sizeof(double), cmp_dbl);
+      lb[t] = quantile_sorted(v, n, 1.0 - q);
+      ub[t] = quantile_sorted(v, n, q);
+    }
+  }
+  free(v);
+  return ABC_OK;
+}

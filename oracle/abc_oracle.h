@@ -75,6 +75,11 @@ int orc_errors(const double* data, const double* se, int64_t G, int K, int n_fam
 int64_t orc_accept(const double* err, int64_t P, int64_t G, int mode, double eps_or_q,
                    int64_t* offsets, int64_t* idx, int64_t cap);
 
+int orc_model_probs(const int64_t* counts, int64_t G, int M, int n_boot, double alpha, uint64_t seed,
+                    double* prob, double* lb, double* ub);
+int orc_posterior_summary(const double* theta, int64_t ld, int npar, const int64_t* off, const int64_t* idx,
+                          int64_t G, double q, double* map, double* mean, double* lb, double* ub,
+                          int64_t* n_out);
 #ifdef __cplusplus
 }
 #endif

@@ -57,6 +57,11 @@ def lib() -> C.CDLL:
         L.orc_errors.argtypes = [dp, dp, C.c_int64, C.c_int, C.c_int, i32p, dp, C.c_int64, C.c_int, dp]
         L.orc_accept.argtypes = [dp, C.c_int64, C.c_int64, C.c_int, C.c_double, i64p, i64p, C.c_int64]
         L.orc_accept.restype = C.c_int64
+        L.orc_model_probs.argtypes = [i64p, C.c_int64, C.c_int, C.c_int, C.c_double, C.c_uint64, dp, dp, dp]
+        L.orc_model_probs.restype = C.c_int
+        L.orc_posterior_summary.argtypes = [dp, C.c_int64, C.c_int, i64p, i64p, C.c_int64, C.c_double, dp, dp,
+                                            dp, dp, i64p]
+        L.orc_posterior_summary.restype = C.c_int
         _lib = L
     return _lib
 
@@ -188,3 +193,27 @@ def accept(err: np.ndarray, mode: int, eps_or_q: float):
     idx = np.zeros(max(n, 1), np.int64)
     lib().orc_accept(ptr(e), P, G, mode, eps_or_q, ptr(offsets, C.c_int64), ptr(idx, C.c_int64), n)
     return offsets, idx[:n]
+
+
+def model_probs(counts: np.ndarray, n_boot: int = 100, alpha: float = 0.95, seed: int = 1):
+    """model_probs.jl:1-28 with the per-gene cases of :41-48 (bootstrap from Philox)."""
+    cnt = np.ascontiguousarray(counts, np.int64)
+    G, M = cnt.shape
+    out = [np.zeros((G, M)) for _ in range(3)]
+    _check(lib().orc_model_probs(ptr(cnt, C.c_int64), G, M, n_boot, alpha, seed, *[ptr(o) for o in out]),
+           "orc_model_probs")
+    return tuple(out)
+
+
+def posterior_summary(theta: np.ndarray, offsets: np.ndarray, idx: np.ndarray, q: float = 0.95) -> dict:
+    """posterior_kinetics.jl:1-33: MAP, mean, quantile bounds and counts per gene."""
+    th = np.ascontiguousarray(theta, np.float64)
+    off = np.ascontiguousarray(offsets, np.int64)
+    ix = np.ascontiguousarray(idx if len(idx) else np.zeros(1, np.int64), np.int64)
+    G = off.shape[0] - 1
+    npar = th.shape[1]
+    outs = [np.zeros((G, npar)) for _ in range(4)]
+    n = np.zeros(G, np.int64)
+    _check(lib().orc_posterior_summary(ptr(th), npar, npar, ptr(off, C.c_int64), ptr(ix, C.c_int64), G, q,
+                                       *[ptr(o) for o in outs], ptr(n, C.c_int64)), "orc_posterior_summary")
+    return {"map": outs[0], "mean": outs[1], "lower": outs[2], "upper": outs[3], "n_particles": n}
