@@ -30,6 +30,8 @@ UNITS = {
     "distance_fp32.cu": [],
     "distance_tc.cu": [],
     "posterior.cu": ["-fmad=false"],
+    "moment.cu": ["-fmad=false"],
+    "moment_fp32.cu": [],
     "noalloc.cu": [],
     "mlp.cu": [],
     "surrogate.cu": [],

@@ -1093,6 +1093,98 @@ int abc_select_profile_read(const abc_ctx* c, double* fast_ms, int* fast_passes)
   return ABC_OK;
 }
 
+static bool grid_ok(double x, double h) {
+  const double q = x / h;
+  return std::fabs(q - std::nearbyint(q)) < 1e-7 * (1.0 + std::fabs(q));
+}
+
+int abc_moment_simulate(abc_ctx* c, int model, const double* theta, int64_t P, const double* iv, double h_max,
+                        const double* beta_mom, int n_pulse_conds, const double* age_dist, double* stats_out,
+                        double* moments_out, int32_t* iters_out) {
+  if (!c) return ABC_ERR_INVALID;
+  const int npar = npar_of(&c->cfg, model);
+  if (npar < 0) return fail(c, ABC_ERR_INVALID, "model must be 1..5");
+  if (c->cfg.splicing) return fail(c, ABC_ERR_INVALID, "the moment model has no splicing");
+  if (!theta || !iv || !beta_mom || !age_dist || !stats_out || P < 0)
+    return fail(c, ABC_ERR_INVALID, "abc_moment_simulate: bad arguments");
+  if (P == 0) return ABC_OK;
+  const abc_config& cf = c->cfg;
+  const double T = cf.cycle;
+  const int S = cf.n_steps, A = cf.n_ages, J = cf.n_conds, K = 4 * A + 3 * J;
+  const double t0 = -(double)cf.n_burn_cycles * T;
+  // substep grid: the coarsest h <= h_max dividing every breakpoint (oracle's rule);
+  // default cycle / 400 (FP64, the oracle's) or cycle / 80 (FP32 production mode)
+  if (!(h_max > 0.0)) h_max = cf.precision == ABC_FP32 ? T / 80.0 : T / 400.0;
+  int per_step = (int)std::ceil((T / (double)S) / h_max);
+  double h = 0.0;
+  for (; per_step < 200000; ++per_step) {
+    h = T / (double)(S * per_step);
+    bool ok = grid_ok(t0, h);
+    for (int a = 0; a < A && ok; ++a) ok = grid_ok(cf.ages[a], h);
+    for (int j = 0; j < J && ok; ++j) ok = grid_ok(cf.pulse[j], h) && grid_ok(cf.chase[j], h);
+    if (ok) break;
+  }
+  if (per_step >= 200000 || (int64_t)S * per_step > 20000)
+    return fail(c, ABC_ERR_INVALID, "no substep grid aligned with the breakpoints");
+  MomArgs a;
+  memset(&a, 0, sizeof(a));
+  a.cfg = c->dcfg;
+  a.ld = npar;
+  a.P = P;
+  a.model = model;
+  for (int i = 0; i < 9; ++i) a.iv[i] = iv[i];
+  a.h = h;
+  a.per_step = per_step;
+  a.nsub = S * per_step;
+  a.n_pulse_conds = n_pulse_conds;
+  const bool f32 = cf.precision == ABC_FP32;
+  const int grid = (int)std::min<int64_t>(P, (int64_t)c->sms * (f32 ? 16 : 8));
+  const size_t scr_doubles = f32 ? (moment_f32_scratch_per_cta(a.nsub) + 7) / 8 : (size_t)2 * a.nsub * 100;
+  DBuf<double> d_theta, d_bm, d_ad, d_stats, d_mom, d_scr;
+  DBuf<int> d_it;
+  CK(d_theta.ensure((size_t)P * npar));
+  CK(d_bm.ensure((size_t)2 * A * 3));
+  CK(d_ad.ensure((size_t)A * J));
+  CK(d_stats.ensure((size_t)P * K));
+  CK(d_scr.ensure((size_t)grid * scr_doubles));
+  if (moments_out) CK(d_mom.ensure((size_t)P * J * A * 5));
+  if (iters_out) CK(d_it.ensure((size_t)P));
+  CK(cudaMemcpyAsync(d_theta.p, theta, sizeof(double) * P * npar, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(d_bm.p, beta_mom, sizeof(double) * 2 * A * 3, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(d_ad.p, age_dist, sizeof(double) * A * J, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemsetAsync(c->d_status.p, 0, sizeof(int), c->stream));
+  a.theta = d_theta.p;
+  a.beta_mom = d_bm.p;
+  a.age_dist = d_ad.p;
+  a.stats = d_stats.p;
+  a.moments = moments_out ? d_mom.p : nullptr;
+  a.iters = iters_out ? d_it.p : nullptr;
+  a.scratch = d_scr.p;
+  a.status = c->d_status.p;
+  if (c->prof && !c->sel_ev[0]) {
+    CK(cudaEventCreate(&c->sel_ev[0]));
+    CK(cudaEventCreate(&c->sel_ev[1]));
+  }
+  if (c->prof) CK(cudaEventRecord(c->sel_ev[0], c->stream));
+  CK(f32 ? launch_moment_f32(a, grid, c->stream) : launch_moment(a, grid, c->stream));
+  if (c->prof) CK(cudaEventRecord(c->sel_ev[1], c->stream));
+  CK(cudaMemcpyAsync(stats_out, d_stats.p, sizeof(double) * P * K, cudaMemcpyDeviceToHost, c->stream));
+  if (moments_out)
+    CK(cudaMemcpyAsync(moments_out, d_mom.p, sizeof(double) * P * J * A * 5, cudaMemcpyDeviceToHost, c->stream));
+  if (iters_out) CK(cudaMemcpyAsync(iters_out, d_it.p, sizeof(int) * P, cudaMemcpyDeviceToHost, c->stream));
+  int hst = 0;
+  CK(cudaMemcpyAsync(&hst, c->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (c->prof) {
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, c->sel_ev[0], c->sel_ev[1]));
+    c->sel_fast_ms = ms;
+    c->sel_fast_passes = 1;
+  }
+  if (hst) return fail(c, ABC_ERR_NONFINITE, "abc_moment_simulate: non-finite rates for some particles (NaN rows)");
+  return ABC_OK;
+}
+
 int abc_model_probs(abc_ctx* c, const int64_t* counts, int64_t G, int M, int n_boot, double alpha, uint64_t seed,
                     double* prob, double* lb, double* ub) {
   if (!c) return ABC_ERR_INVALID;

@@ -139,6 +139,29 @@ cudaError_t launch_scan(const int64_t* cnt, int64_t G, int64_t* off, cudaStream_
 // full FP64 error matrix [P][G]
 cudaError_t launch_dist_full(const DistInputs& in, double* err, cudaStream_t s);
 
+// moment ODE (moment.cu)
+struct MomArgs {
+  DevCfg cfg;
+  const double* theta;  // [P][ld]
+  int64_t ld, P;
+  int model;
+  double iv[9];
+  double h;             // substep (T / (n_steps per_step)), aligned with every breakpoint
+  int per_step, nsub;   // substeps per age step and per cycle
+  const double* beta_mom;  // [2][A][3]: capture mean, mean of squares, sample variance (pulse, chase cells)
+  int n_pulse_conds;
+  const double* age_dist;  // [A][J]
+  double* stats;           // [P][K]
+  double* moments;         // [P][J][A][5] or null
+  int* iters;              // [P] transient cycles or null
+  double* scratch;         // [grid][2][nsub][100]
+  int* status;
+};
+cudaError_t launch_moment(const MomArgs& a, int grid, cudaStream_t s);
+// FP32 production mode (moment_fp32.cu); scratch: moment_f32_scratch_per_cta(nsub) bytes per CTA
+size_t moment_f32_scratch_per_cta(int nsub);
+cudaError_t launch_moment_f32(const MomArgs& a, int grid, cudaStream_t s);
+
 // model probabilities with bootstrap intervals and per-gene posterior summaries (posterior.cu)
 cudaError_t launch_model_probs(const int64_t* counts, int64_t G, int M, int n_boot, double alpha, uint64_t seed,
                                double* prob, double* lb, double* ub, double* boot, cudaStream_t s);

@@ -105,7 +105,8 @@ ABC_HD void initial_means(const DevCfg& cfg, PRec& R) {
 }
 
 // theta -> record; returns 0 or a negative abc_status.
-ABC_HD int parse_theta(const DevCfg& cfg, int model, const double* th, PRec& R) {
+// with_ic: also the SSA initial state and work estimate (not needed by the moment ODE)
+ABC_HD int parse_theta(const DevCfg& cfg, int model, const double* th, PRec& R, bool with_ic = true) {
   const int S = cfg.n_steps;
   int i = 0;
   double lk[kMaxSteps], la[kMaxSteps], lg[kMaxSteps];
@@ -143,6 +144,7 @@ ABC_HD int parse_theta(const DevCfg& cfg, int model, const double* th, PRec& R) 
   for (int k = 0; k < S; ++k)
     if (!(R.kon[k] < INFINITY) || !(R.alp[k] < INFINITY) || !(R.gam[k] < INFINITY)) return -5;
   if (!(R.koff < INFINITY) || R.lam != R.lam || R.scal != R.scal || R.scal < 0.0) return -5;
+  if (!with_ic) return 0;
   initial_means(cfg, R);
   // work estimate: switching + transcription + decay events over the horizon
   double horizon = (double)(cfg.ages[0] - cfg.t0);

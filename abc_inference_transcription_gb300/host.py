@@ -256,6 +256,25 @@ class Context:
         self._check(self.lib.abc_select_counters(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
+    def moment_simulate(self, model: int, theta: np.ndarray, iv, beta_mom: np.ndarray, age_dist: np.ndarray,
+                        n_pulse_conds: int = 6, h_max: float = 0.0, moments: bool = False) -> dict:
+        """Deterministic statistics of every particle from the moment ODE
+        (the reference's abc_sim); {"stats", "moments" (optional), "transient_iters"}."""
+        th = np.ascontiguousarray(theta, np.float64)
+        P = th.shape[0]
+        A, J = self.cfg.n_ages, self.cfg.n_conds
+        st = np.zeros((P, nstats(A, J)))
+        mo = np.zeros((P, J, A, 5)) if moments else None
+        it = np.zeros(P, np.int32)
+        self._check(self.lib.abc_moment_simulate(self.h, model, ptr(th), P, ptr(np.ascontiguousarray(iv, np.float64)),
+                                                 float(h_max), ptr(np.ascontiguousarray(beta_mom, np.float64)),
+                                                 n_pulse_conds, ptr(np.ascontiguousarray(age_dist, np.float64)),
+                                                 ptr(st), ptr(mo), ptr(it, C.c_int32)))
+        out = {"stats": st, "transient_iters": it}
+        if moments:
+            out["moments"] = mo
+        return out
+
     def model_probs(self, counts: np.ndarray, n_boot: int = 100, alpha: float = 0.95, seed: int = 1):
         """(prob, lower, upper) [G, M] from accepted counts [G, M] (scripts/model_probs.jl)."""
         cnt = np.ascontiguousarray(counts, np.int64)

@@ -249,6 +249,26 @@ int abc_errors_candidate(abc_ctx* ctx, const double* data, const double* se, int
                          double* b0_out, double* b1_out, int* mode_used);
 
 /* ------------------------------------------------------------------------
+ * Deterministic simulation (the reference's own): the 9-moment ODE of the
+ * model (scripts/model.jl:67-96), its periodic steady state by the 1 %
+ * transient rule from iv (:114-142, iv as in abc_simulation.jl:70-71), the
+ * multi-cycle trajectories with division for every (condition, age)
+ * (:98-111, :146-199), the capture moment transform with the per-cluster
+ * capture moments beta_mom[2][A][3] = {mean, mean of squares, sample
+ * variance} of the pulse and the chase cells (:221-239), and the statistics
+ * of abc_simulation.jl:13-62 with age_dist[A][J].  Exponential midpoint rule
+ * on a substep grid h <= h_max aligned with every breakpoint (h_max <= 0:
+ * cycle / 400 in FP64, cycle / 80 in FP32).  stats_out [P][K]; moments_out [P][J][A][5] (E u, E l, Var u,
+ * Cov ul, Var l before capture) and iters_out [P] (transient cycles) may be
+ * NULL.  No splicing.  Replaces the CVODE-based abc_sim path.  Precision of
+ * the context: ABC_FP64 = the oracle's arithmetic, bit for bit; ABC_FP32 =
+ * production mode (FP32 propagators and states on the triangular form of the
+ * moment matrix, FP64 rates and statistics). */
+int abc_moment_simulate(abc_ctx* ctx, int model, const double* theta, int64_t n_particles, const double* iv,
+                        double h_max, const double* beta_mom, int n_pulse_conds, const double* age_dist,
+                        double* stats_out, double* moments_out, int32_t* iters_out);
+
+/* ------------------------------------------------------------------------
  * Downstream of the acceptance.
  *
  * Model probabilities (scripts/model_probs.jl:1-28, per-gene driver :37-62):

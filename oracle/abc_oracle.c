@@ -857,7 +857,7 @@ static const double* propagator(mctx_t* M, int idx, int lab) {
     const rec_t* R = M->R;
     int k = idx / M->per_step;
     double ph = ((double)idx + 0.5) * M->h;
-    double al = R->alp[k] * pow(1.0 + ph / M->cfg->cycle, R->scal);
+    double al = R->alp[k] * xpow(1.0 + ph / M->cfg->cycle, R->scal);
     double A[NAUG * NAUG];
     build_A(A, R->kon[k], R->koff, al, R->gam[k], lab ? R->lam : 0.0, M->h);
     expm(A, P);
