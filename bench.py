@@ -53,10 +53,11 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-distance", action="store_true", help="skip the P x G distance section")
     ap.add_argument("--no-abc", action="store_true", help="skip the plain vs screened ABC section")
+    ap.add_argument("--no-moment", action="store_true", help="skip the moment-ODE section")
     ap.add_argument("--dist-particles", type=int, default=5_000_000)
     ap.add_argument("--genes", type=int, default=2000)
-    ap.add_argument("--section", default="all", choices=["all", "distance"],
-                    help="'distance' runs only the P x G distance section and prints its object")
+    ap.add_argument("--section", default="all", choices=["all", "distance", "moment"],
+                    help="'distance' / 'moment' run only that section and print its object")
     return ap.parse_args()
 
 
@@ -281,6 +282,49 @@ def distance_bench(P: int, G: int, K: int, q: float, seed: int, cpu_seconds: flo
     return out
 
 
+def moment_bench(P: int, cpu_seconds: float):
+    """The reference's deterministic simulation (moment ODE, all 53 statistics)
+    for P particles of the five models (factor prior, reference time grid):
+    FP32 production mode (substep cycle / 80) and the oracle-exact FP64 mode,
+    beside the FP64 C oracle on all host cores at both grids."""
+    import numpy as np
+    from abc_inference_transcription_gb300 import FP32, FP64, factor_prior, make_config, synthetic_cells
+    from abc_inference_transcription_gb300.config import beta_moments
+    from abc_inference_transcription_gb300.host import Context
+    cells = synthetic_cells(seed=1)
+    bm = beta_moments(cells, 5)
+    iv = np.zeros(9)
+    iv[1] = 0.5
+    out = {"workload": f"moment ODE statistics of {P} particles per model x 5 models, reference time grid (h), "
+                       "factor prior, 2,000-cell capture moments", "unit": "particles/s"}
+    thetas = {}
+    for prec, name, n in ((FP32, "fp32_production", P), (FP64, "fp64_exact", max(P // 50, 200))):
+        with Context(make_config("hour", precision=prec), cells) as ctx:
+            tot, dt = 0, 0.0
+            for m in range(1, 6):
+                th = ctx.sample_prior(m, n, 100 + m, factor_prior())
+                thetas[m] = th
+                ctx.moment_simulate(m, th[:64], iv, bm, cells.age_dist)   # warm-up
+                t0 = time.perf_counter()
+                ctx.moment_simulate(m, th, iv, bm, cells.age_dist)
+                dt += time.perf_counter() - t0
+                tot += n
+            out[name] = {"value": tot / dt, "particles": tot, "seconds": dt}
+    if cpu_seconds > 0:
+        from oracle import oracle as orc
+        orc.build()
+        cfg = make_config("hour", precision=FP64)
+        for h_max, name in ((20.0 / 400, "cpu_h_cycle_over_400"), (20.0 / 80, "cpu_h_cycle_over_80")):
+            n = 64
+            t0 = time.perf_counter()
+            for m in range(1, 6):
+                orc.moment_batch(cfg, m, thetas[m][:n], iv, bm, cells.age_dist, n_threads=os.cpu_count() or 1,
+                                 h_max=h_max)
+            out[name] = {"value": 5 * n / (time.perf_counter() - t0), "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"{n} particles per model, FP64 oracle"}
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -338,11 +382,14 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    if args.section == "distance":
+    if args.section in ("distance", "moment"):
         if rank == 0:
             import __graft_entry__
             __graft_entry__.build()
-            print(json.dumps(distance_bench(args.dist_particles, args.genes, 72, 0.001, 5, args.cpu_seconds)))
+            if args.section == "distance":
+                print(json.dumps(distance_bench(args.dist_particles, args.genes, 72, 0.001, 5, args.cpu_seconds)))
+            else:
+                print(json.dumps(moment_bench(40000, args.cpu_seconds)))
         return
     dist = None
     if world > 1:
@@ -478,6 +525,11 @@ def main():
             line["distance"] = distance_bench(args.dist_particles, args.genes, 72, 0.001, 5, args.cpu_seconds)
         except Exception as exc:
             line["distance"] = {"error": repr(exc)}
+    if not args.no_moment:
+        try:
+            line["moment_ode"] = moment_bench(40000, args.cpu_seconds)
+        except Exception as exc:
+            line["moment_ode"] = {"error": repr(exc)}
     if not args.no_abc:
         try:
             from abc_inference_transcription_gb300 import pipeline
