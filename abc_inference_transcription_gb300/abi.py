@@ -158,6 +158,8 @@ def _declare(lib: C.CDLL) -> None:
         "abc_set_distance_mode": (C.c_int, [vp, C.c_int]),
         "abc_moment_simulate": (C.c_int, [vp, C.c_int, dp, C.c_int64, dp, C.c_double, dp, C.c_int, dp, dp, dp,
                                           C.POINTER(C.c_int32)]),
+        "abc_data_stats": (C.c_int, [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int64, C.c_int,
+                                     C.c_uint64, dp, dp]),
         "abc_model_probs": (C.c_int, [vp, i64p, C.c_int64, C.c_int, C.c_int, C.c_double, C.c_uint64, dp, dp, dp]),
         "abc_posterior_summary": (C.c_int, [vp, dp, C.c_int64, C.c_int, C.c_int, C.c_double, dp, dp, dp, dp,
                                             i64p]),
@@ -198,7 +200,7 @@ ABI_SYMBOLS = [
     "abc_errors_select", "abc_errors_select_thr", "abc_errors_select_device", "abc_accept_fetch",
     "abc_select_counters", "abc_select_profile_read", "abc_set_distance_mode", "abc_get_distance_mode",
     "abc_errors_candidate", "abc_model_probs", "abc_posterior_summary",
-    "abc_moment_simulate",
+    "abc_moment_simulate", "abc_data_stats",
     "abc_surrogate_create", "abc_surrogate_destroy", "abc_surrogate_last_error", "abc_surrogate_num_params",
     "abc_surrogate_train", "abc_surrogate_gradients", "abc_surrogate_get_params", "abc_surrogate_set_params",
     "abc_surrogate_get_norm", "abc_surrogate_set_norm", "abc_surrogate_predict", "abc_surrogate_predict_device",

@@ -32,6 +32,7 @@ UNITS = {
     "posterior.cu": ["-fmad=false"],
     "moment.cu": ["-fmad=false"],
     "moment_fp32.cu": [],
+    "datastats.cu": ["-fmad=false"],
     "noalloc.cu": [],
     "mlp.cu": [],
     "surrogate.cu": [],

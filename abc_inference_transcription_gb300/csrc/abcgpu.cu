@@ -1185,6 +1185,61 @@ int abc_moment_simulate(abc_ctx* c, int model, const double* theta, int64_t P, c
   return ABC_OK;
 }
 
+int abc_data_stats(abc_ctx* c, const int32_t* u, const int32_t* l, int64_t G, int n_boot, uint64_t seed,
+                   double* stats_out, double* se_out) {
+  if (!c) return ABC_ERR_INVALID;
+  if (!c->cells_set) return fail(c, ABC_ERR_STATE, "abc_data_stats: call abc_set_cells first");
+  if (!u || !l || !stats_out || G < 0 || n_boot < 0 || n_boot > 10000 || (se_out && n_boot < 2))
+    return fail(c, ABC_ERR_INVALID, "abc_data_stats: bad arguments (standard errors need n_boot >= 2)");
+  const int64_t C = c->C;
+  for (int64_t i = 0; i < G * C; ++i)
+    if (u[i] < 0 || l[i] < 0 || u[i] > (1 << 20) || l[i] > (1 << 20))
+      return fail(c, ABC_ERR_INVALID, "abc_data_stats: counts must lie in [0, 2^20]");
+  if (G == 0) return ABC_OK;
+  const int K = 4 * c->cfg.n_ages + 3 * c->cfg.n_conds;
+  DBuf<int32_t> du, dl;
+  DBuf<double> dout, dse;
+  CK(du.ensure((size_t)G * C));
+  CK(dl.ensure((size_t)G * C));
+  CK(dout.ensure((size_t)G * (n_boot + 1) * K));
+  if (se_out) CK(dse.ensure((size_t)G * K));
+  CK(cudaMemcpyAsync(du.p, u, sizeof(int32_t) * G * C, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(dl.p, l, sizeof(int32_t) * G * C, cudaMemcpyHostToDevice, c->stream));
+  DataStatsArgs a;
+  a.cfg = c->dcfg;
+  a.u = du.p;
+  a.l = dl.p;
+  a.G = G;
+  a.C = C;
+  a.cell_cond = c->d_cond.p;
+  a.cell_age = c->d_age.p;
+  a.cell_id = c->d_id.p;
+  a.gstart = c->d_gstart.p;
+  a.age_dist = c->d_age_dist.p;
+  a.n_boot = n_boot;
+  a.seed = seed;
+  a.out = dout.p;
+  if (c->prof && !c->sel_ev[0]) {
+    CK(cudaEventCreate(&c->sel_ev[0]));
+    CK(cudaEventCreate(&c->sel_ev[1]));
+  }
+  if (c->prof) CK(cudaEventRecord(c->sel_ev[0], c->stream));
+  CK(launch_data_stats(a, se_out ? dse.p : nullptr, c->stream));
+  if (c->prof) CK(cudaEventRecord(c->sel_ev[1], c->stream));
+  // the estimate is resample 0 of each gene
+  CK(cudaMemcpy2DAsync(stats_out, sizeof(double) * K, dout.p, sizeof(double) * K * (n_boot + 1), sizeof(double) * K,
+                       (size_t)G, cudaMemcpyDeviceToHost, c->stream));
+  if (se_out) CK(cudaMemcpyAsync(se_out, dse.p, sizeof(double) * G * K, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (c->prof) {
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, c->sel_ev[0], c->sel_ev[1]));
+    c->sel_fast_ms = ms;
+    c->sel_fast_passes = 1;
+  }
+  return ABC_OK;
+}
+
 int abc_model_probs(abc_ctx* c, const int64_t* counts, int64_t G, int M, int n_boot, double alpha, uint64_t seed,
                     double* prob, double* lb, double* ub) {
   if (!c) return ABC_ERR_INVALID;

@@ -162,6 +162,23 @@ cudaError_t launch_moment(const MomArgs& a, int grid, cudaStream_t s);
 size_t moment_f32_scratch_per_cta(int nsub);
 cudaError_t launch_moment_f32(const MomArgs& a, int grid, cudaStream_t s);
 
+// data-side statistics and bootstrap standard errors (datastats.cu)
+struct DataStatsArgs {
+  DevCfg cfg;
+  const int32_t* u;  // [G][C] counts, caller's cell order
+  const int32_t* l;
+  int64_t G, C;
+  const int32_t* cell_cond;   // group-sorted cell table (abc_set_cells)
+  const int32_t* cell_age;
+  const uint32_t* cell_id;    // caller's index of each sorted cell
+  const int32_t* gstart;      // [J A + 1] group starts
+  const double* age_dist;     // [A][J]
+  int n_boot;
+  uint64_t seed;
+  double* out;                // [G][n_boot + 1][K]
+};
+cudaError_t launch_data_stats(const DataStatsArgs& a, double* se, cudaStream_t s);
+
 // model probabilities with bootstrap intervals and per-gene posterior summaries (posterior.cu)
 cudaError_t launch_model_probs(const int64_t* counts, int64_t G, int M, int n_boot, double alpha, uint64_t seed,
                                double* prob, double* lb, double* ub, double* boot, cudaStream_t s);

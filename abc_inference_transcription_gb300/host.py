@@ -275,6 +275,19 @@ class Context:
             out["moments"] = mo
         return out
 
+    def data_stats(self, u: np.ndarray, l: np.ndarray, n_boot: int = 100, seed: int = 1):
+        """(statistics [G, K], bootstrap standard errors [G, K] or None) of the
+        observed counts u, l [G, C] (data_summary_statistics.jl)."""
+        uu = np.ascontiguousarray(u, np.int32)
+        ll = np.ascontiguousarray(l, np.int32)
+        G = uu.shape[0]
+        K = nstats(self.cfg.n_ages, self.cfg.n_conds)
+        st = np.zeros((G, K))
+        se = np.zeros((G, K)) if n_boot >= 2 else None
+        self._check(self.lib.abc_data_stats(self.h, ptr(uu, C.c_int32), ptr(ll, C.c_int32), G, int(n_boot),
+                                            C.c_uint64(seed), ptr(st), ptr(se)))
+        return st, se
+
     def model_probs(self, counts: np.ndarray, n_boot: int = 100, alpha: float = 0.95, seed: int = 1):
         """(prob, lower, upper) [G, M] from accepted counts [G, M] (scripts/model_probs.jl)."""
         cnt = np.ascontiguousarray(counts, np.int64)

@@ -218,9 +218,22 @@ def distance_bench(P: int, G: int, K: int, q: float, seed: int, cpu_seconds: flo
         t0 = time.perf_counter()
         ctx.model_probs(mp_counts)
         t_mp = time.perf_counter() - t0
-        down = {"posterior_summary_s": t_post, "model_probs_s": t_mp,
+        # data side: statistics + 100 bootstrap SEs of G genes' observed counts
+        from abc_inference_transcription_gb300 import synthetic_cells
+        cells_d = synthetic_cells(seed=1)
+        rng_d = np.random.default_rng(seed)
+        lam = rng_d.gamma(2.0, 3.0, (G, 1)) * cells_d.beta[None, :] * 5
+        u_d = rng_d.poisson(lam, (G, cells_d.cond.shape[0])).astype(np.int32)
+        l_d = rng_d.poisson(0.4 * lam, (G, cells_d.cond.shape[0])).astype(np.int32)
+        with Context(make_config("hour"), cells_d) as dctx:
+            dctx.data_stats(u_d[:8], l_d[:8], n_boot=100)
+            t0 = time.perf_counter()
+            dctx.data_stats(u_d, l_d, n_boot=100)
+            t_ds = time.perf_counter() - t0
+        down = {"posterior_summary_s": t_post, "model_probs_s": t_mp, "data_stats_s": t_ds,
                 "workload": f"posterior MAP/mean/95 % bounds of 9 parameters over {int(off[-1])} accepted pairs "
-                            f"in {G} genes; model probabilities of {G} genes x 2 groups, 100 bootstraps"}
+                            f"in {G} genes; model probabilities of {G} genes x 2 groups, 100 bootstraps; data "
+                            f"statistics + 100-resample SEs of {G} genes x 2,000 cells"}
         if cpu_seconds > 0:
             from oracle import oracle as orc
             orc.build()
@@ -232,7 +245,11 @@ def distance_bench(P: int, G: int, K: int, q: float, seed: int, cpu_seconds: flo
             t0 = time.perf_counter()
             orc.model_probs(mp_counts)
             down["cpu_model_probs_s"] = time.perf_counter() - t0
-            down["cpu_sample"] = f"posterior summary of the first {gs} genes scaled to {G}, one core (oracle)"
+            t0 = time.perf_counter()
+            orc.data_stats(make_config("hour"), cells_d, u_d[:20], l_d[:20], n_boot=100)
+            down["cpu_data_stats_s_scaled"] = (time.perf_counter() - t0) * G / 20
+            down["cpu_sample"] = (f"posterior summary of the first {gs} genes and data statistics of the first 20 "
+                                  f"genes, scaled to {G}, one core (oracle)")
             del th_h
         del theta
     finally:

@@ -268,6 +268,19 @@ int abc_moment_simulate(abc_ctx* ctx, int model, const double* theta, int64_t n_
                         double h_max, const double* beta_mom, int n_pulse_conds, const double* age_dist,
                         double* stats_out, double* moments_out, int32_t* iters_out);
 
+/* Data side (scripts/data_summary_statistics.jl:1-216): the statistics of
+ * observed counts, u[g][c] and l[g][c] (non-negative integers <= 2^20, cells
+ * in the order given to abc_set_cells), per gene in the simulated layout
+ * (pulse mean and FF of u + l per age over the pulse-statistic cells, chase
+ * likewise, per-condition ratio of means, mean_corr and corr_mean with the
+ * context's age weights), and, if se_out is not NULL, their bootstrap
+ * standard errors over n_boot >= 2 resamples of the cells (per family, as the
+ * reference's get_*_se; the correlation resamples re-weight the ages by their
+ * resampled fractions within each condition).  Resamples come from a Philox
+ * stream keyed by (seed, family, resample, gene).  stats_out, se_out [G][K]. */
+int abc_data_stats(abc_ctx* ctx, const int32_t* u_counts, const int32_t* l_counts, int64_t n_genes, int n_boot,
+                   uint64_t seed, double* stats_out, double* se_out);
+
 /* ------------------------------------------------------------------------
  * Downstream of the acceptance.
  *

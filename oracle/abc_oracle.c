@@ -1197,3 +1197,148 @@ int orc_posterior_summary(const double* theta, int64_t ld, int npar, const int64
   free(v);
   return ABC_OK;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Data-side statistics and bootstrap standard errors                         */
+/* (data_summary_statistics.jl:1-216).  Cells in the stable (condition, age)  */
+/* order; draw i of (seed, family, resample, gene) from its own Philox        */
+/* counter; statistics from exact integer sums.                              */
+/* ------------------------------------------------------------------------- */
+static int64_t draw_pos(uint64_t seed, int fam, int b, int64_t g, int64_t i, int64_t n) {
+  uint32_t c[4] = {(uint32_t)(i >> 1), ((uint32_t)((uint64_t)i >> 33) & 0x3fffffffu) | (3u << 30),
+                   (uint32_t)b | ((uint32_t)(fam + 1) << 24), (uint32_t)g};
+  uint32_t k[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)}, o[4];
+  orc_philox4x32_10(c, k, o);
+  double u = (i & 1) ? u52(o[2], o[3]) : u52(o[0], o[1]);
+  int64_t p = (int64_t)(u * (double)n);
+  return p < n ? p : n - 1;
+}
+
+static double sample_cov(unsigned long long n, unsigned long long sx, unsigned long long sy, unsigned long long sxy) {
+  __int128 num = (__int128)n * (__int128)sxy - (__int128)sx * (__int128)sy;
+  return i128_to_double(num) / ((double)n * (double)(n - 1));
+}
+
+static void data_one(const abc_config* cfg, int64_t C, const int32_t* cond_s, const int32_t* age_s,
+                     const int64_t* id_s, const int64_t* gs, const double* age_dist, const int32_t* u,
+                     const int32_t* l, int64_t g, int b, uint64_t seed, double* st) {
+  const int A = cfg->n_ages, J = cfg->n_conds;
+  unsigned long long Sp[2][ABC_MAX_AGES][3];
+  unsigned long long Sg[ABC_MAX_CONDS * ABC_MAX_AGES][6];
+  memset(Sp, 0, sizeof(Sp));
+  memset(Sg, 0, sizeof(Sg));
+  for (int f = 0; f < 2; ++f) {
+    int cond = f == 0 ? cfg->pulse_stat_cond : cfg->chase_stat_cond;
+    int64_t base = gs[cond * A], n = gs[(cond + 1) * A] - base;
+    for (int64_t i = 0; i < n; ++i) {
+      int64_t cell = base + (b == 0 ? i : draw_pos(seed, f, b, g, i, n));
+      int64_t id = id_s[cell];
+      unsigned long long x = (unsigned long long)u[id] + (unsigned long long)l[id];
+      int ag = age_s[cell];
+      Sp[f][ag][0] += 1ull;
+      Sp[f][ag][1] += x;
+      Sp[f][ag][2] += x * x;
+    }
+  }
+  for (int64_t i = 0; i < C; ++i) {
+    int64_t cell = b == 0 ? i : draw_pos(seed, 2, b, g, i, C);
+    int64_t id = id_s[cell];
+    unsigned long long uu = (unsigned long long)u[id], ll = (unsigned long long)l[id];
+    unsigned long long* S = Sg[cond_s[cell] * A + age_s[cell]];
+    S[0] += 1ull; S[1] += uu; S[2] += ll; S[3] += uu * uu; S[4] += ll * ll; S[5] += uu * ll;
+  }
+  for (int f = 0; f < 2; ++f) {
+    int off = f == 0 ? 0 : 2 * A;
+    for (int ag = 0; ag < A; ++ag) {
+      unsigned long long n = Sp[f][ag][0];
+      double m = 0.0, ff = 0.0;
+      if (n > 0) {
+        m = (double)Sp[f][ag][1] / (double)n;
+        double v = sample_cov(n, Sp[f][ag][1], Sp[f][ag][1], Sp[f][ag][2]);
+        double eps = (m == 0.0) ? 0.0001 : 0.0;
+        ff = v / (m + eps);
+      }
+      st[off + ag] = m;
+      st[off + A + ag] = ff;
+    }
+  }
+  for (int j = 0; j < J; ++j) {
+    double m1[ABC_MAX_AGES] = {0}, m2[ABC_MAX_AGES] = {0}, v1[ABC_MAX_AGES] = {0}, v2[ABC_MAX_AGES] = {0};
+    double c12[ABC_MAX_AGES] = {0}, w[ABC_MAX_AGES] = {0};
+    unsigned long long nj = 0, suj = 0, slj = 0;
+    for (int ag = 0; ag < A; ++ag) {
+      unsigned long long* S = Sg[j * A + ag];
+      nj += S[0]; suj += S[1]; slj += S[2];
+      if (S[0] == 0) {
+        m1[ag] = m2[ag] = v1[ag] = v2[ag] = c12[ag] = 0.0;
+      } else {
+        m1[ag] = (double)S[1] / (double)S[0];
+        m2[ag] = (double)S[2] / (double)S[0];
+        v1[ag] = sample_cov(S[0], S[1], S[1], S[3]);
+        v2[ag] = sample_cov(S[0], S[2], S[2], S[4]);
+        c12[ag] = sample_cov(S[0], S[1], S[2], S[5]);
+      }
+    }
+    double mu = (double)suj / (double)nj, ml = (double)slj / (double)nj;
+    st[4 * A + j] = (mu + ml > 0.0) ? ml / (mu + ml) : 0.0;
+    for (int ag = 0; ag < A; ++ag) {
+      if (b == 0) {
+        w[ag] = age_dist[ag * J + j];
+      } else {
+        double x = (double)Sg[j * A + ag][0] / (double)nj;
+        w[ag] = x == x ? x : 0.0;
+      }
+    }
+    double tv1 = wsum(w, v1, A) + wcov(m1, m1, w, A);
+    double tv2 = wsum(w, v2, A) + wcov(m2, m2, w, A);
+    int any_cov = 0;
+    for (int ag = 0; ag < A; ++ag) any_cov = any_cov || (c12[ag] != 0.0);
+    int tv_ok = tv1 != 0.0 && tv2 != 0.0;
+    st[4 * A + J + j] = (any_cov && tv_ok) ? wsum(w, c12, A) / sqrt(fabs(tv1 * tv2)) : 0.0;
+    st[4 * A + 2 * J + j] = tv_ok ? wcov(m1, m2, w, A) / sqrt(fabs(tv1 * tv2)) : 0.0;
+  }
+}
+
+int orc_data_stats(const abc_config* cfg, int64_t C, const int32_t* cell_cond, const int32_t* cell_age,
+                   const double* age_dist, const int32_t* u, const int32_t* l, int64_t G, int n_boot,
+                   uint64_t seed, double* stats, double* se) {
+  const int A = cfg->n_ages, J = cfg->n_conds, K = 4 * A + 3 * J, NG = A * J;
+  int32_t* cond_s = (int32_t*)malloc(sizeof(int32_t) * (size_t)C);
+  int32_t* age_s = (int32_t*)malloc(sizeof(int32_t) * (size_t)C);
+  int64_t* id_s = (int64_t*)malloc(sizeof(int64_t) * (size_t)C);
+  int64_t gs[ABC_MAX_CONDS * ABC_MAX_AGES + 1];
+  double* boot = (double*)malloc(sizeof(double) * (size_t)(n_boot + 1) * K);
+  if (!cond_s || !age_s || !id_s || !boot) return ABC_ERR_NOMEM;
+  /* stable counting sort by group = condition * A + age */
+  memset(gs, 0, sizeof(gs));
+  for (int64_t i = 0; i < C; ++i) gs[cell_cond[i] * A + cell_age[i] + 1]++;
+  for (int q = 0; q < NG; ++q) gs[q + 1] += gs[q];
+  int64_t cur[ABC_MAX_CONDS * ABC_MAX_AGES];
+  for (int q = 0; q < NG; ++q) cur[q] = gs[q];
+  for (int64_t i = 0; i < C; ++i) {
+    int q = cell_cond[i] * A + cell_age[i];
+    int64_t pos = cur[q]++;
+    cond_s[pos] = cell_cond[i];
+    age_s[pos] = cell_age[i];
+    id_s[pos] = i;
+  }
+  for (int64_t g = 0; g < G; ++g) {
+    for (int b = 0; b <= n_boot; ++b)
+      data_one(cfg, C, cond_s, age_s, id_s, gs, age_dist, u + g * C, l + g * C, g, b, seed, boot + (size_t)b * K);
+    memcpy(stats + g * K, boot, sizeof(double) * K);
+    if (se && n_boot >= 2) {
+      for (int k = 0; k < K; ++k) {
+        double s = 0.0;
+        for (int b = 1; b <= n_boot; ++b) s = s + boot[(size_t)b * K + k];
+        double m = s / (double)n_boot, q = 0.0;
+        for (int b = 1; b <= n_boot; ++b) {
+          double d = boot[(size_t)b * K + k] - m;
+          q = q + d * d;
+        }
+        se[g * K + k] = sqrt((1.0 / (double)(n_boot - 1)) * q);
+      }
+    }
+  }
+  free(cond_s); free(age_s); free(id_s); free(boot);
+  return ABC_OK;
+}

@@ -80,6 +80,9 @@ int orc_model_probs(const int64_t* counts, int64_t G, int M, int n_boot, double 
 int orc_posterior_summary(const double* theta, int64_t ld, int npar, const int64_t* off, const int64_t* idx,
                           int64_t G, double q, double* map, double* mean, double* lb, double* ub,
                           int64_t* n_out);
+int orc_data_stats(const abc_config* cfg, int64_t C, const int32_t* cell_cond, const int32_t* cell_age,
+                   const double* age_dist, const int32_t* u, const int32_t* l, int64_t G, int n_boot,
+                   uint64_t seed, double* stats, double* se);
 #ifdef __cplusplus
 }
 #endif

@@ -57,6 +57,10 @@ def lib() -> C.CDLL:
         L.orc_errors.argtypes = [dp, dp, C.c_int64, C.c_int, C.c_int, i32p, dp, C.c_int64, C.c_int, dp]
         L.orc_accept.argtypes = [dp, C.c_int64, C.c_int64, C.c_int, C.c_double, i64p, i64p, C.c_int64]
         L.orc_accept.restype = C.c_int64
+        L.orc_data_stats.argtypes = [C.POINTER(AbcConfig), C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32), dp,
+                                     C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int64, C.c_int, C.c_uint64,
+                                     dp, dp]
+        L.orc_data_stats.restype = C.c_int
         L.orc_model_probs.argtypes = [i64p, C.c_int64, C.c_int, C.c_int, C.c_double, C.c_uint64, dp, dp, dp]
         L.orc_model_probs.restype = C.c_int
         L.orc_posterior_summary.argtypes = [dp, C.c_int64, C.c_int, i64p, i64p, C.c_int64, C.c_double, dp, dp,
@@ -217,3 +221,19 @@ def posterior_summary(theta: np.ndarray, offsets: np.ndarray, idx: np.ndarray, q
     _check(lib().orc_posterior_summary(ptr(th), npar, npar, ptr(off, C.c_int64), ptr(ix, C.c_int64), G, q,
                                        *[ptr(o) for o in outs], ptr(n, C.c_int64)), "orc_posterior_summary")
     return {"map": outs[0], "mean": outs[1], "lower": outs[2], "upper": outs[3], "n_particles": n}
+
+
+def data_stats(cfg: AbcConfig, cells, u: np.ndarray, l: np.ndarray, n_boot: int = 100, seed: int = 1):
+    """data_summary_statistics.jl: statistics [G, K] of observed counts u, l [G, C]
+    and bootstrap standard errors (None for n_boot < 2)."""
+    uu = np.ascontiguousarray(u, np.int32)
+    ll = np.ascontiguousarray(l, np.int32)
+    G, Cn = uu.shape
+    K = nstats(cfg.n_ages, cfg.n_conds)
+    st = np.zeros((G, K))
+    se = np.zeros((G, K)) if n_boot >= 2 else None
+    _check(lib().orc_data_stats(C.byref(cfg), Cn, ptr(np.ascontiguousarray(cells.cond, np.int32), C.c_int32),
+                                ptr(np.ascontiguousarray(cells.age, np.int32), C.c_int32),
+                                ptr(np.ascontiguousarray(cells.age_dist, np.float64)), ptr(uu, C.c_int32),
+                                ptr(ll, C.c_int32), G, n_boot, seed, ptr(st), ptr(se)), "orc_data_stats")
+    return st, se
