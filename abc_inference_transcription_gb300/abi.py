@@ -156,6 +156,8 @@ def _declare(lib: C.CDLL) -> None:
         "abc_select_counters": (C.c_int, [vp, i64p, i64p]),
         "abc_select_profile_read": (C.c_int, [vp, dp, C.POINTER(C.c_int)]),
         "abc_set_distance_mode": (C.c_int, [vp, C.c_int]),
+        "abc_set_graph": (C.c_int, [vp, C.c_int]),
+        "abc_graph_counters": (C.c_int, [vp, i64p, i64p]),
         "abc_moment_simulate": (C.c_int, [vp, C.c_int, dp, C.c_int64, dp, C.c_double, dp, C.c_int, dp, dp, dp,
                                           C.POINTER(C.c_int32)]),
         "abc_data_stats": (C.c_int, [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int64, C.c_int,
@@ -200,7 +202,7 @@ ABI_SYMBOLS = [
     "abc_errors_select", "abc_errors_select_thr", "abc_errors_select_device", "abc_accept_fetch",
     "abc_select_counters", "abc_select_profile_read", "abc_set_distance_mode", "abc_get_distance_mode",
     "abc_errors_candidate", "abc_model_probs", "abc_posterior_summary",
-    "abc_moment_simulate", "abc_data_stats",
+    "abc_moment_simulate", "abc_data_stats", "abc_set_graph", "abc_graph_counters",
     "abc_surrogate_create", "abc_surrogate_destroy", "abc_surrogate_last_error", "abc_surrogate_num_params",
     "abc_surrogate_train", "abc_surrogate_gradients", "abc_surrogate_get_params", "abc_surrogate_set_params",
     "abc_surrogate_get_norm", "abc_surrogate_set_norm", "abc_surrogate_predict", "abc_surrogate_predict_device",

@@ -71,6 +71,9 @@ struct abc_ctx {
   DBuf<int> d_status;
   int64_t last_events = 0, last_rej = 0;
   int variant = 0;  // production SSA kernel variant chosen by abc_autotune
+  bool graph_mode = false;           // simulate chain as a CUDA graph (abc_set_graph)
+  cudaGraphExec_t gexec = nullptr;
+  int64_t graph_instantiations = 0, graph_updates = 0;
   // per-phase device timing (abc_profile): 4 events per chunk
   bool prof = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -206,6 +209,7 @@ int abc_create(abc_ctx** out, const abc_config* cfg) {
 int abc_destroy(abc_ctx* c) {
   if (!c) return ABC_OK;
   cudaStreamSynchronize(c->stream);
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
   c->d_cond.release(); c->d_age.release(); c->d_gstart.release(); c->d_id.release();
   c->d_beta.release(); c->d_age_dist.release(); c->d_theta.release(); c->d_stats.release();
   c->d_models.release(); c->d_order.release(); c->d_ohist.release(); c->d_rec.release(); c->d_recf.release(); c->d_counts.release(); c->d_captured.release();
@@ -361,10 +365,9 @@ static cudaError_t prof_mark(abc_ctx* c) {
   return cudaEventRecord(c->ev_pool[c->ev_used++], c->stream);
 }
 
-static int enqueue_simulate(abc_ctx* c, int model, const int32_t* d_models, const double* d_theta, int64_t ld,
-                            int64_t P, uint64_t seed, int64_t p_offset, double* d_stats, bool want_cells) {
-  const int npar = d_models ? npar_max(&c->cfg) : npar_of(&c->cfg, model);
-  const int K = ABC_NSTATS(c->cfg.n_ages, c->cfg.n_conds);
+// device workspace of a simulation of P particles, processed in chunks that
+// keep the per-cell count buffer under kChunkBytes
+static int prepare_simulate(abc_ctx* c, int64_t P, bool want_cells, int64_t* chunk_out) {
   const int64_t C = c->C;
   int64_t chunk = std::max<int64_t>(1, (int64_t)(kChunkBytes / (sizeof(int2) * (size_t)C)));
   if (want_cells) chunk = P;  // per-cell outputs are requested for small P only
@@ -379,6 +382,18 @@ static int enqueue_simulate(abc_ctx* c, int model, const int32_t* d_models, cons
     CK(c->d_events.ensure((size_t)chunk * C));
     CK(c->d_hash.ensure((size_t)chunk * C));
   }
+  *chunk_out = chunk;
+  return ABC_OK;
+}
+
+static int enqueue_simulate(abc_ctx* c, int model, const int32_t* d_models, const double* d_theta, int64_t ld,
+                            int64_t P, uint64_t seed, int64_t p_offset, double* d_stats, bool want_cells) {
+  const int npar = d_models ? npar_max(&c->cfg) : npar_of(&c->cfg, model);
+  const int K = ABC_NSTATS(c->cfg.n_ages, c->cfg.n_conds);
+  const int64_t C = c->C;
+  int64_t chunk = 0;
+  int pst = prepare_simulate(c, P, want_cells, &chunk);
+  if (pst) return pst;
   CK(cudaMemsetAsync(c->d_misc.p, 0, sizeof(unsigned long long) * 4, c->stream));
   CK(cudaMemsetAsync(c->d_status.p, 0, sizeof(int), c->stream));
   c->ev_used = 0;
@@ -480,6 +495,71 @@ static int finish_status(abc_ctx* c) {
   return ABC_OK;
 }
 
+// The simulate -> capture -> statistics chain, as one CUDA graph when graph
+// mode is on: the chain is captured on the context's stream, the instantiated
+// graph is updated in place (new seed, pointers) when its topology is
+// unchanged, re-instantiated otherwise, and launched once.  Workspace is
+// grown before the capture (no allocation inside it); profiling events are
+// not recorded inside the graph.
+static int enqueue_chain(abc_ctx* c, int model, const int32_t* d_models, const double* d_theta, int64_t ld, int64_t P,
+                         uint64_t seed, int64_t p_offset, double* d_stats) {
+  if (!c->graph_mode) return enqueue_simulate(c, model, d_models, d_theta, ld, P, seed, p_offset, d_stats, false);
+  int64_t chunk = 0;
+  int st = prepare_simulate(c, P, false, &chunk);
+  if (st) return st;
+  const bool prof = c->prof;
+  c->prof = false;
+  cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    c->prof = prof;
+    return cuda_fail(c, e, "cudaStreamBeginCapture");
+  }
+  st = enqueue_simulate(c, model, d_models, d_theta, ld, P, seed, p_offset, d_stats, false);
+  cudaGraph_t g = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(c->stream, &g);
+  c->prof = prof;
+  if (st || ec != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return st ? st : cuda_fail(c, ec, "cudaStreamEndCapture");
+  }
+  if (c->gexec) {
+    cudaGraphExecUpdateResultInfo info;
+    if (cudaGraphExecUpdate(c->gexec, g, &info) != cudaSuccess) {
+      (void)cudaGetLastError();
+      cudaGraphExecDestroy(c->gexec);
+      c->gexec = nullptr;
+    } else {
+      c->graph_updates++;
+    }
+  }
+  if (!c->gexec) {
+    e = cudaGraphInstantiate(&c->gexec, g, 0);
+    if (e != cudaSuccess) {
+      c->gexec = nullptr;
+      cudaGraphDestroy(g);
+      return cuda_fail(c, e, "cudaGraphInstantiate");
+    }
+    c->graph_instantiations++;
+  }
+  e = cudaGraphLaunch(c->gexec, c->stream);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphLaunch");
+  return ABC_OK;
+}
+
+int abc_set_graph(abc_ctx* c, int enable) {
+  if (!c) return ABC_ERR_INVALID;
+  c->graph_mode = enable != 0;
+  return ABC_OK;
+}
+
+int abc_graph_counters(const abc_ctx* c, int64_t* instantiations, int64_t* updates) {
+  if (!c) return ABC_ERR_INVALID;
+  if (instantiations) *instantiations = c->graph_instantiations;
+  if (updates) *updates = c->graph_updates;
+  return ABC_OK;
+}
+
 int abc_simulate_device(abc_ctx* c, int model, const double* d_theta, int64_t P, uint64_t seed,
                         int64_t particle_offset, double* d_stats) {
   if (!c) return ABC_ERR_INVALID;
@@ -487,8 +567,7 @@ int abc_simulate_device(abc_ctx* c, int model, const double* d_theta, int64_t P,
   if (st) return st;
   if (P == 0) return ABC_OK;
   if (!d_theta || !d_stats) return fail(c, ABC_ERR_INVALID, "null device pointer");
-  return enqueue_simulate(c, model, nullptr, d_theta, npar_of(&c->cfg, model), P, seed, particle_offset, d_stats,
-                          false);
+  return enqueue_chain(c, model, nullptr, d_theta, npar_of(&c->cfg, model), P, seed, particle_offset, d_stats);
 }
 
 int abc_simulate_batch_device(abc_ctx* c, const int32_t* d_models, const double* d_theta, int64_t ld_theta,
@@ -499,7 +578,7 @@ int abc_simulate_batch_device(abc_ctx* c, const int32_t* d_models, const double*
   if (P == 0) return ABC_OK;
   if (!d_models || !d_theta || !d_stats) return fail(c, ABC_ERR_INVALID, "null device pointer");
   if (ld_theta < npar_max(&c->cfg)) return fail(c, ABC_ERR_INVALID, "ld_theta below the largest npar");
-  return enqueue_simulate(c, 0, d_models, d_theta, ld_theta, P, seed, particle_offset, d_stats, false);
+  return enqueue_chain(c, 0, d_models, d_theta, ld_theta, P, seed, particle_offset, d_stats);
 }
 
 int abc_simulate_batch(abc_ctx* c, const int32_t* models, const double* theta, int64_t ld_theta, int64_t P,
@@ -518,7 +597,7 @@ int abc_simulate_batch(abc_ctx* c, const int32_t* models, const double* theta, i
   CK(c->d_stats.ensure((size_t)P * K));
   CK(cudaMemcpyAsync(c->d_models.p, models, sizeof(int32_t) * P, cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(c->d_theta.p, theta, sizeof(double) * P * ld_theta, cudaMemcpyHostToDevice, c->stream));
-  st = enqueue_simulate(c, 0, c->d_models.p, c->d_theta.p, ld_theta, P, seed, particle_offset, c->d_stats.p, false);
+  st = enqueue_chain(c, 0, c->d_models.p, c->d_theta.p, ld_theta, P, seed, particle_offset, c->d_stats.p);
   if (st) return st;
   CK(cudaMemcpyAsync(stats_out, c->d_stats.p, sizeof(double) * P * K, cudaMemcpyDeviceToHost, c->stream));
   return finish_status(c);

@@ -316,6 +316,15 @@ class Context:
                                                    ptr(n, C.c_int64)))
         return {"map": outs[0], "mean": outs[1], "lower": outs[2], "upper": outs[3], "n_particles": n}
 
+    def set_graph(self, enable: bool = True) -> None:
+        """Run the simulation chain as one CUDA graph (captured, updated in place, launched)."""
+        self._check(self.lib.abc_set_graph(self.h, 1 if enable else 0))
+
+    def graph_counters(self) -> tuple[int, int]:
+        a, b = C.c_int64(), C.c_int64()
+        self._check(self.lib.abc_graph_counters(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def set_distance_mode(self, mode: int) -> None:
         """Candidate pass: 0 FP32 CUDA cores, 1 TF32 tensor cores (one term),
         2 TF32 tensor cores with hi/lo splits (default)."""

@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--no-distance", action="store_true", help="skip the P x G distance section")
     ap.add_argument("--no-abc", action="store_true", help="skip the plain vs screened ABC section")
     ap.add_argument("--no-moment", action="store_true", help="skip the moment-ODE section")
+    ap.add_argument("--no-graph", action="store_true", help="skip the CUDA-graph timing of the step")
     ap.add_argument("--dist-particles", type=int, default=5_000_000)
     ap.add_argument("--genes", type=int, default=2000)
     ap.add_argument("--section", default="all", choices=["all", "distance", "moment"],
@@ -470,6 +471,27 @@ def main():
         tot_ev_all = float(tot_ev)
     value = tot_ev_all / (t_ms / 1e3)
 
+    # the same steps with the chain (setup -> work order -> SSA -> capture +
+    # statistics) as one CUDA graph, updated in place per seed
+    graph = None
+    if not args.no_graph:
+        ctx.profile(False)
+        ctx.set_graph(True)
+        step(700)
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        g0.record(stream)
+        ng = min(args.steps, 3)
+        for k in range(ng):
+            step(1000 + k)
+        g1.record(stream)
+        torch.cuda.synchronize()
+        gi, gu = ctx.graph_counters()
+        graph = {"ms_per_step": g0.elapsed_time(g1) / ng, "plain_ms_per_step": t_ms / args.steps,
+                 "instantiations": gi, "in_place_updates": gu, "steps": ng}
+        ctx.set_graph(False)
+        ctx.profile(True)
+
     # e2e through the host API
     e2e = None
     if not args.no_e2e:
@@ -535,6 +557,7 @@ def main():
         "e2e": e2e,
         "gpu_launches": 5 * args.steps,  # setup, 2 work-order kernels, SSA, capture+statistics
         "autotune": {"chosen_variant": variant, "ssa_ms_per_variant": tune_ms, "sample": f"{n_tune} particles"},
+        "cuda_graph": graph,
         "clocks": clocks,
     }
     if not args.no_distance:

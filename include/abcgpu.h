@@ -221,6 +221,15 @@ int abc_errors_select_device(abc_ctx* ctx, const double* data, const double* se,
 /* gene_offsets: G+1 entries; particle_idx: 1-based, n_accepted_total entries;
  * err: FP64 errors of the accepted pairs (may be NULL). */
 int abc_accept_fetch(abc_ctx* ctx, int64_t* gene_offsets, int64_t* particle_idx, double* err);
+/* CUDA graph mode for the simulation chain (setup -> work order -> SSA ->
+ * capture + statistics) of abc_simulate_device, abc_simulate_batch_device
+ * and abc_simulate_batch: each call captures the chain on the context's
+ * stream and updates one instantiated graph in place (re-instantiating only
+ * when the chain's shape changes), then launches it.  Results are identical
+ * to the plain launches.  No reference counterpart. */
+int abc_set_graph(abc_ctx* ctx, int enable);
+/* graph instantiations and in-place updates so far */
+int abc_graph_counters(const abc_ctx* ctx, int64_t* instantiations, int64_t* updates);
 /* Counters of the last selection: pairs emitted by the FP32 candidate
  * pass(es), and pairs rechecked in FP64 (after the top-k refinement). */
 int abc_select_counters(const abc_ctx* ctx, int64_t* candidates, int64_t* rechecked);
