@@ -148,6 +148,8 @@ __global__ void __launch_bounds__(128, MINB) ssa_kernel_f32(SsaArgs A) {
   bool half = false, has_nxt = false;
   uint32_t it = 0;
   unsigned long long tot_ev = 0, tot_rej = 0;
+  unsigned rej32 = 0;  // rejections since the lane's last item boundary (folded into tot_rej there)
+  bool scal01 = true;
   int err = 0;
   s.plocal = 0;
   while (true) {
@@ -179,6 +181,7 @@ __global__ void __launch_bounds__(128, MINB) ssa_kernel_f32(SsaArgs A) {
           lam = F.lam;
           beta = F.beta;
           scal = F.scal;
+          scal01 = scal == 0.0f || scal == 1.0f;
           s.k = 0;
           s.cyc = 0;
           s.lab = 0;
@@ -284,6 +287,8 @@ __global__ void __launch_bounds__(128, MINB) ssa_kernel_f32(SsaArgs A) {
         A.counts[s.out] = make_int2((int)(s.uu + s.us), (int)(s.lu + s.ls));
         if (A.events) A.events[s.out] = s.ev;
         tot_ev += (unsigned long long)s.ev;
+        tot_rej += rej32;
+        rej32 = 0;
         active = false;
       }
       continue;
@@ -294,9 +299,11 @@ __global__ void __launch_bounds__(128, MINB) ssa_kernel_f32(SsaArgs A) {
     const float r = u23(wc) * a0;
     const bool b1 = r >= c1, b2 = r >= c2, b3 = r >= c3, b4 = r >= c4;
     const float size = fmaf(s.ph0 + (s.el - s.comp), invT, 1.0f);
-    const float sz_lin = fmaf(scal, size - 1.0f, 1.0f);          // exact for s in {0, 1}
-    const float sz_pow = exp2f(scal * __log2f(size));
-    const float at = q.alp * ((scal == 0.0f || scal == 1.0f) ? sz_lin : sz_pow);
+    // size^s: linear (exact) for s in {0, 1}, the general power only for lanes
+    // with another exponent (a warp-uniform skip for the reference's models)
+    float sz = fmaf(scal, size - 1.0f, 1.0f);
+    if (!scal01) sz = exp2f(scal * __log2f(size));
+    const float at = q.alp * sz;
     // thinning uniform from the 9 low bits of both words (18 bits), x bound
     const uint32_t th = ((wt & 0x1FFu) << 9) | (wc & 0x1FFu);
     const float v = (__uint_as_float(0x3F800000u | (th << 5)) - 1.0f) * q.amax;
@@ -320,12 +327,14 @@ __global__ void __launch_bounds__(128, MINB) ssa_kernel_f32(SsaArgs A) {
       fired = (!tx || acc) && (!b6 || dl);
     }
     s.ev += fired ? 1 : 0;
-    tot_rej += (tx && !acc) ? 1ull : 0ull;
+    rej32 += (tx && !acc) ? 1u : 0u;
     if (s.ev > cap) {
       err |= STF_EVENT_CAP;
       A.counts[s.out] = make_int2((int)(s.uu + s.us), (int)(s.lu + s.ls));
       if (A.events) A.events[s.out] = s.ev;
       tot_ev += (unsigned long long)s.ev;
+      tot_rej += rej32;
+      rej32 = 0;
       active = false;
     }
   }
