@@ -35,6 +35,7 @@ UNITS = {
     "datastats.cu": ["-fmad=false"],
     "noalloc.cu": [],
     "mlp.cu": [],
+    "mlp_tc.cu": [],
     "surrogate.cu": [],
 }
 

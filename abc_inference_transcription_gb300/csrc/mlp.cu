@@ -1,120 +1,17 @@
-// mlp.cu — forward, backward and Adam kernels of the surrogate ensemble.
-// GEMMs use BF16 tensor-core tiles (16x16x16 fragments, FP32 accumulation);
-// the ensemble member is blockIdx.z.  See mlp.cuh for the layout.
+// mlp.cu — forward, backward and Adam of the surrogate ensemble.  Every GEMM
+// runs on the tcgen05 tensor cores (mlp_tc.cu) with both operands K-major, so
+// the passes keep transposed BF16 copies where the backward pass reduces over
+// the batch: W^T for the forward GEMMs, and X0^T, A_l^T, dY^T, dZ_l^T
+// ([features][batch]) for the weight gradients.  See mlp.cuh for the layout.
 #include <cuda_bf16.h>
-#include <mma.h>
+
+#include <algorithm>
 
 #include "common.cuh"
 #include "kernels.h"
 #include "mlp.cuh"
 
 namespace abc {
-
-using namespace nvcuda;
-
-constexpr int GBM = 64, GBN = 64, GBK = 32;
-
-__device__ __forceinline__ float sigmoidf_fast(float z) { return 1.0f / (1.0f + __expf(-z)); }
-
-template <bool TA, bool TB, int EPI>
-__global__ void __launch_bounds__(128) mlp_gemm_kernel(GemmArgs g) {
-  __shared__ __align__(128) __nv_bfloat16 As[GBM][GBK + 8];
-  __shared__ __align__(128) __nv_bfloat16 Bs[GBK][GBN + 8];
-  __shared__ __align__(128) float Cs[GBM][GBN + 4];
-  const int z = blockIdx.z;
-  const __nv_bfloat16* A = g.A + z * g.sA;
-  const __nv_bfloat16* B = g.B + z * g.sB;
-  const int n_mt = (g.M + GBM - 1) / GBM;
-  const int mt = blockIdx.y % n_mt;
-  const int split = blockIdx.y / n_mt;
-  const int m0 = mt * GBM, n0 = blockIdx.x * GBN;
-  int kbeg = 0, kend = g.K;
-  if (EPI == EPI_ATOMIC) {
-    const int per = (((g.K + g.k_split - 1) / g.k_split) + GBK - 1) / GBK * GBK;
-    kbeg = split * per;
-    kend = min(g.K, kbeg + per);
-  }
-  const int warp = threadIdx.x >> 5;
-  const int wm = warp >> 1, wn = warp & 1;
-  wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc[2][2];
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 2; ++j) wmma::fill_fragment(acc[i][j], 0.0f);
-  const __nv_bfloat16 zero = __float2bfloat16(0.0f);
-  for (int k0 = kbeg; k0 < kend; k0 += GBK) {
-    for (int idx = threadIdx.x; idx < GBM * GBK; idx += 128) {
-      int r, c;
-      if (TA) { c = idx / GBM; r = idx - c * GBM; }  // consecutive threads along m (contiguous in A)
-      else { r = idx / GBK; c = idx - r * GBK; }     // consecutive threads along k
-      const int m = m0 + r, k = k0 + c;
-      __nv_bfloat16 v = zero;
-      if (m < g.M && k < kend) v = TA ? A[(int64_t)k * g.lda + m] : A[(int64_t)m * g.lda + k];
-      As[r][c] = v;
-    }
-    for (int idx = threadIdx.x; idx < GBK * GBN; idx += 128) {
-      int r, c;
-      if (TB) { r = idx % GBK; c = idx / GBK; }      // consecutive threads along k (contiguous in B)
-      else { r = idx / GBN; c = idx - r * GBN; }     // consecutive threads along n
-      const int k = k0 + r, n = n0 + c;
-      __nv_bfloat16 v = zero;
-      if (n < g.N && k < kend) v = TB ? B[(int64_t)n * g.ldb + k] : B[(int64_t)k * g.ldb + n];
-      Bs[r][c] = v;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < GBK; kk += 16) {
-      wmma::fragment<wmma::matrix_a, 16, 16, 16, __nv_bfloat16, wmma::row_major> fa[2];
-      wmma::fragment<wmma::matrix_b, 16, 16, 16, __nv_bfloat16, wmma::row_major> fb[2];
-#pragma unroll
-      for (int i = 0; i < 2; ++i) wmma::load_matrix_sync(fa[i], &As[wm * 32 + i * 16][kk], GBK + 8);
-#pragma unroll
-      for (int j = 0; j < 2; ++j) wmma::load_matrix_sync(fb[j], &Bs[kk][wn * 32 + j * 16], GBN + 8);
-#pragma unroll
-      for (int i = 0; i < 2; ++i)
-#pragma unroll
-        for (int j = 0; j < 2; ++j) wmma::mma_sync(acc[i][j], fa[i], fb[j], acc[i][j]);
-    }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 2; ++j)
-      wmma::store_matrix_sync(&Cs[wm * 32 + i * 16][wn * 32 + j * 16], acc[i][j], GBN + 4, wmma::mem_row_major);
-  __syncthreads();
-  const float* bias = g.bias ? g.bias + z * g.sBias : nullptr;
-  for (int idx = threadIdx.x; idx < GBM * GBN; idx += 128) {
-    const int r = idx / GBN, c = idx - r * GBN;
-    const int m = m0 + r, n = n0 + c;
-    if (m >= g.M || n >= g.N) continue;
-    const float v = Cs[r][c];
-    const int64_t o = (int64_t)m * g.ldo + n;
-    if (EPI == EPI_HIDDEN) {
-      const float zz = v + (bias ? bias[n] : 0.0f);
-      if (g.outf) g.outf[z * g.sOut + o] = zz;
-      g.outh[z * g.sOut + o] = __float2bfloat16(zz * sigmoidf_fast(zz));
-    } else if (EPI == EPI_LINEAR) {
-      g.outf[z * g.sOut + o] = v + (bias ? bias[n] : 0.0f);
-    } else if (EPI == EPI_ATOMIC) {
-      atomicAdd(&g.outf[z * g.sOut + o], v);
-    } else {
-      const float zp = g.zprev[z * g.sZ + o];
-      const float s = sigmoidf_fast(zp);
-      g.outh[z * g.sOut + o] = __float2bfloat16(v * (s * (1.0f + zp * (1.0f - s))));
-    }
-  }
-}
-
-template <bool TA, bool TB, int EPI>
-static cudaError_t gemm(const GemmArgs& g, int members, int splits, cudaStream_t s) {
-  const int n_mt = (g.M + GBM - 1) / GBM;
-  dim3 grid((g.N + GBN - 1) / GBN, n_mt * splits, members);
-  GemmArgs a = g;
-  a.k_split = splits;
-  mlp_gemm_kernel<TA, TB, EPI><<<grid, 128, 0, s>>>(a);
-  return cudaGetLastError();
-}
 
 // ---------------------------------------------------------------------------
 // elementwise kernels
@@ -160,17 +57,41 @@ __global__ void mlp_to_bf16_kernel(const float* src, __nv_bfloat16* dst, int64_t
     dst[i] = __float2bfloat16(src[i]);
 }
 
+// BF16 transposed weights: W_l [R][C] at off_w -> W_l^T [C][R] at the same
+// offset (biases copied), for the K-major forward GEMMs.
+__global__ void mlp_weights_t_kernel(const float* P, MlpDims d, int members, __nv_bfloat16* PT) {
+  const int64_t n = d.n_params * members;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = i / d.n_params, q = i - e * d.n_params;
+    int64_t off = -1, R = 0, Cc = 0;
+    if (q >= d.off_w1 && q < d.off_b1) { off = d.off_w1; R = d.in_pad; Cc = d.H; }
+    else if (q >= d.off_w2 && q < d.off_b2) { off = d.off_w2; R = d.H; Cc = d.H; }
+    else if (q >= d.off_w3 && q < d.off_b3) { off = d.off_w3; R = d.H; Cc = d.H; }
+    else if (q >= d.off_w4 && q < d.off_b4) { off = d.off_w4; R = d.H; Cc = d.out_pad; }
+    if (off < 0) {
+      PT[i] = __float2bfloat16(P[i]);
+    } else {
+      const int64_t t = q - off, r = t / Cc, c = t - r * Cc;   // source element (r, c)
+      PT[e * d.n_params + off + c * R + r] = __float2bfloat16(P[i]);
+    }
+  }
+}
+
 // rows of the batch for member e: idx = (a_e * (base + i) + b_e) mod N
 __global__ void mlp_gather_kernel(const float* xn, const float* yn, int64_t N, int in_pad, int K, int B, int64_t base,
-                                  const uint64_t* perm_ab, __nv_bfloat16* X0, float* T, int64_t sX, int64_t sT) {
+                                  const uint64_t* perm_ab, __nv_bfloat16* X0, __nv_bfloat16* X0T, int ldT, float* T,
+                                  int64_t sX, int64_t sT) {
   const int e = blockIdx.y;
   const uint64_t a = perm_ab[2 * e], b = perm_ab[2 * e + 1];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B; i += gridDim.x * blockDim.x) {
     const int64_t pos = base + i;
     const bool ok = pos < N;
     const int64_t r = ok ? (int64_t)((a * (uint64_t)pos + b) % (uint64_t)N) : 0;
-    for (int c = 0; c < in_pad; ++c)
-      X0[e * sX + (int64_t)i * in_pad + c] = __float2bfloat16(ok ? xn[r * in_pad + c] : 0.0f);
+    for (int c = 0; c < in_pad; ++c) {
+      const __nv_bfloat16 x = __float2bfloat16(ok ? xn[r * in_pad + c] : 0.0f);
+      X0[e * sX + (int64_t)i * in_pad + c] = x;
+      if (X0T) X0T[(int64_t)e * in_pad * ldT + (int64_t)c * ldT + i] = x;
+    }
     for (int k = 0; k < K; ++k) T[e * sT + (int64_t)i * K + k] = ok ? yn[r * K + k] : __int_as_float(0x7fc00000);
   }
 }
@@ -179,7 +100,7 @@ __global__ void mlp_gather_kernel(const float* xn, const float* yn, int64_t N, i
 constexpr float kLvMin = -9.0f, kLvMax = 9.0f;
 
 __global__ void mlp_loss_kernel(const float* Y, const float* T, int B, int K, int out_pad, float inv_count,
-                                __nv_bfloat16* dY, float* loss, int64_t sY, int64_t sT) {
+                                __nv_bfloat16* dY, __nv_bfloat16* dYT, int ldT, float* loss, int64_t sY, int64_t sT) {
   const int e = blockIdx.y;
   float local = 0.0f;
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < B * out_pad; idx += gridDim.x * blockDim.x) {
@@ -207,7 +128,9 @@ __global__ void mlp_loss_kernel(const float* Y, const float* T, int B, int K, in
         grad = inside ? 0.5f * (1.0f - r * r * __expf(-lv)) * inv_count : 0.0f;
       }
     }
-    dY[e * sY + idx] = __float2bfloat16(grad);
+    const __nv_bfloat16 gb = __float2bfloat16(grad);
+    dY[e * sY + idx] = gb;
+    dYT[(int64_t)e * out_pad * ldT + (int64_t)c * ldT + i] = gb;
   }
   for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
   if ((threadIdx.x & 31) == 0) atomicAdd(&loss[e], local * inv_count);
@@ -282,121 +205,160 @@ __global__ void mlp_combine_kernel(const float* Y, int N, int K, int out_pad, in
 // ---------------------------------------------------------------------------
 static int blocks_for(int64_t n, int t) { return (int)std::min<int64_t>((n + t - 1) / t, 65536); }
 
-cudaError_t mlp_init(const MlpDims& d, int members, uint64_t seed, float* P, __nv_bfloat16* Ph, cudaStream_t s) {
+// BF16 copies of the parameters: as stored (for dX = dZ W^T) and transposed
+// (for the forward GEMMs)
+cudaError_t mlp_refresh_bf16(const MlpDims& d, int members, const float* P, __nv_bfloat16* Ph, __nv_bfloat16* PhT,
+                             cudaStream_t s) {
   const int64_t n = d.n_params * members;
-  mlp_init_kernel<<<blocks_for(n, 256), 256, 0, s>>>(d, members, seed, P);
   mlp_to_bf16_kernel<<<blocks_for(n, 256), 256, 0, s>>>(P, Ph, n);
+  mlp_weights_t_kernel<<<blocks_for(n, 256), 256, 0, s>>>(P, d, members, PhT);
   return cudaGetLastError();
 }
 
-cudaError_t mlp_to_bf16(const float* src, __nv_bfloat16* dst, int64_t n, cudaStream_t s) {
-  mlp_to_bf16_kernel<<<blocks_for(n, 256), 256, 0, s>>>(src, dst, n);
-  return cudaGetLastError();
+cudaError_t mlp_init(const MlpDims& d, int members, uint64_t seed, float* P, __nv_bfloat16* Ph, __nv_bfloat16* PhT,
+                     cudaStream_t s) {
+  const int64_t n = d.n_params * members;
+  mlp_init_kernel<<<blocks_for(n, 256), 256, 0, s>>>(d, members, seed, P);
+  return mlp_refresh_bf16(d, members, P, Ph, PhT, s);
 }
 
 cudaError_t mlp_gather(const float* xn, const float* yn, int64_t N, const MlpDims& d, int B, int64_t base,
-                       const uint64_t* perm_ab, int members, __nv_bfloat16* X0, float* T, cudaStream_t s) {
+                       const uint64_t* perm_ab, int members, __nv_bfloat16* X0, __nv_bfloat16* X0T, int ldT, float* T,
+                       cudaStream_t s) {
   dim3 grid((B + 255) / 256, members);
-  mlp_gather_kernel<<<grid, 256, 0, s>>>(xn, yn, N, d.in_pad, d.K, B, base, perm_ab, X0, T, (int64_t)B * d.in_pad,
-                                          (int64_t)B * d.K);
+  mlp_gather_kernel<<<grid, 256, 0, s>>>(xn, yn, N, d.in_pad, d.K, B, base, perm_ab, X0, X0T, ldT, T,
+                                          (int64_t)B * d.in_pad, (int64_t)B * d.K);
   return cudaGetLastError();
 }
 
-// Forward pass of all members for a batch of B rows.  X0: [members or 1][B][in_pad]
-// (sX = 0 shares one input).  Z: [members][3][B][H] fp32 (may be null),
-// Ah: [members][3][B][H] bf16, Y: [members][B][out_pad].
+// Forward pass of all members for B rows.  X0: [members or 1][B][in_pad] (sX = 0:
+// one input for every member).  Z: [members][3][B][H] fp32 (may be null), Ah:
+// [members][3][B][H] bf16, AhT: [members][3][H][ldT] (transposed activations
+// for the weight gradients; null for inference), Y: [members][B][out_pad].
 cudaError_t mlp_forward(const MlpDims& d, int members, int B, const __nv_bfloat16* X0, int64_t sX,
-                        const __nv_bfloat16* Wh, const float* Pf, float* Z, __nv_bfloat16* Ah, float* Y,
-                        cudaStream_t s) {
+                        const __nv_bfloat16* WhT, const float* Pf, float* Z, __nv_bfloat16* Ah, __nv_bfloat16* AhT,
+                        int ldT, float* Y, int* err, cudaStream_t s) {
   const int H = d.H;
-  const int64_t sZ = 3 * (int64_t)B * H, sL = (int64_t)B * H;
-  cudaError_t err;
-  for (int layer = 0; layer < 3; ++layer) {
-    GemmArgs g{};
-    g.A = layer == 0 ? X0 : Ah + (layer - 1) * sL;
-    g.sA = layer == 0 ? sX : sZ;
-    g.B = Wh + (layer == 0 ? d.off_w1 : layer == 1 ? d.off_w2 : d.off_w3);
-    g.sB = d.n_params;
-    g.bias = Pf + (layer == 0 ? d.off_b1 : layer == 1 ? d.off_b2 : d.off_b3);
-    g.sBias = d.n_params;
-    g.outf = Z ? Z + layer * sL : nullptr;
-    g.outh = Ah + layer * sL;
-    g.sOut = sZ;
+  const int64_t sZ = 3 * (int64_t)B * H, sL = (int64_t)B * H, sLT = (int64_t)H * ldT;
+  const int64_t w_off[4] = {d.off_w1, d.off_w2, d.off_w3, d.off_w4};
+  const int64_t b_off[4] = {d.off_b1, d.off_b2, d.off_b3, d.off_b4};
+  cudaError_t e;
+  for (int layer = 0; layer < 4; ++layer) {
+    const int K = layer == 0 ? d.in_pad : H;
+    const int N = layer == 3 ? d.out_pad : H;
+    TcOperand A, Bw;
+    A.ptr = layer == 0 ? X0 : Ah + (layer - 1) * sL;
+    A.ld = K;
+    A.rows = B;
+    A.member_stride = layer == 0 ? sX : sZ;
+    Bw.ptr = WhT + w_off[layer];   // W^T [N][K]
+    Bw.ld = K;
+    Bw.rows = N;
+    Bw.member_stride = d.n_params;
+    TcGemm g{};
     g.M = B;
-    g.N = H;
-    g.K = layer == 0 ? d.in_pad : H;
-    g.lda = g.K;
-    g.ldb = H;
-    g.ldo = H;
-    err = gemm<false, false, EPI_HIDDEN>(g, members, 1, s);
-    if (err) return err;
+    g.N = N;
+    g.K = K;
+    g.k_split = 1;
+    g.a_shared = (layer == 0 && sX == 0) ? 1 : 0;
+    g.bias = Pf + b_off[layer];
+    g.sBias = d.n_params;
+    g.err = err;
+    if (layer < 3) {
+      g.outf = Z ? Z + layer * sL : nullptr;
+      g.sOutf = sZ;
+      g.ldf = H;
+      g.outh = Ah + layer * sL;
+      g.sOuth = sZ;
+      g.ldh = H;
+      g.outhT = AhT ? AhT + layer * sLT : nullptr;
+      g.sOuthT = 3 * sLT;
+      g.ldhT = ldT;
+      e = mlp_tc_gemm(EPI_HIDDEN, A, Bw, g, members, s);
+    } else {
+      g.outf = Y;
+      g.sOutf = (int64_t)B * d.out_pad;
+      g.ldf = d.out_pad;
+      e = mlp_tc_gemm(EPI_LINEAR, A, Bw, g, members, s);
+    }
+    if (e != cudaSuccess) return e;
   }
-  GemmArgs g{};
-  g.A = Ah + 2 * sL;
-  g.sA = sZ;
-  g.B = Wh + d.off_w4;
-  g.sB = d.n_params;
-  g.bias = Pf + d.off_b4;
-  g.sBias = d.n_params;
-  g.outf = Y;
-  g.sOut = (int64_t)B * d.out_pad;
-  g.M = B;
-  g.N = d.out_pad;
-  g.K = H;
-  g.lda = H;
-  g.ldb = d.out_pad;
-  g.ldo = d.out_pad;
-  return gemm<false, false, EPI_LINEAR>(g, members, 1, s);
+  return cudaSuccess;
 }
 
-// Backward pass: loss gradient dY (bf16 [members][B][out_pad]) -> parameter
-// gradients Gf (fp32, zeroed here).  dA, dZ: [members][B][H] bf16 scratch.
-cudaError_t mlp_backward(const MlpDims& d, int members, int B, const __nv_bfloat16* X0, int64_t sX,
-                         const __nv_bfloat16* Wh, const float* Z, const __nv_bfloat16* Ah, const __nv_bfloat16* dY,
-                         __nv_bfloat16* dZa, __nv_bfloat16* dZb, float* Gf, cudaStream_t s) {
+// Backward pass: dY (bf16 [members][B][out_pad]) and dY^T ([members][out_pad][ldT])
+// -> parameter gradients Gf (fp32, zeroed here).  dW_l = A_{l-1}^T dZ_l from the
+// transposed copies (reduction over the batch split across CTAs, atomically
+// accumulated); dZ_l = (dZ_{l+1} W_{l+1}^T) silu'(Z_l) with its transposed copy.
+cudaError_t mlp_backward(const MlpDims& d, int members, int B, const __nv_bfloat16* X0T, const __nv_bfloat16* Wh,
+                         const float* Z, const __nv_bfloat16* AhT, const __nv_bfloat16* dY, const __nv_bfloat16* dYT,
+                         __nv_bfloat16* dZa, __nv_bfloat16* dZb, __nv_bfloat16* dZTa, __nv_bfloat16* dZTb, int ldT,
+                         float* Gf, int* err, cudaStream_t s) {
   const int H = d.H;
-  const int64_t sZ = 3 * (int64_t)B * H, sL = (int64_t)B * H, sP = d.n_params;
-  const int splits = std::max(1, std::min(32, B / 256));
-  cudaError_t err = cudaMemsetAsync(Gf, 0, sizeof(float) * d.n_params * members, s);
-  if (err) return err;
-  // layer 4: dW4 = A3^T dY, db4 = colsum(dY)
+  const int64_t sZ = 3 * (int64_t)B * H, sL = (int64_t)B * H, sLT = (int64_t)H * ldT, sP = d.n_params;
+  const int splits = std::max(1, std::min(16, B / 128));
+  cudaError_t e = cudaMemsetAsync(Gf, 0, sizeof(float) * d.n_params * members, s);
+  if (e) return e;
+  auto wgrad = [&](const TcOperand& A, const TcOperand& Bg, int M, int N, int64_t off) {
+    TcGemm g{};
+    g.M = M;
+    g.N = N;
+    g.K = B;
+    g.k_split = splits;
+    g.outf = Gf + off;
+    g.sOutf = sP;
+    g.ldf = N;
+    g.err = err;
+    return mlp_tc_gemm(EPI_ATOMIC, A, Bg, g, members, s);
+  };
+  // layer 4: dW4 = A3^T dY (M = H, N = out_pad), db4 = colsum(dY)
   {
-    GemmArgs g{};
-    g.A = Ah + 2 * sL; g.sA = sZ; g.lda = H;                 // A3 stored [B][H] -> op = A3^T (M=H, K=B)
-    g.B = dY; g.sB = (int64_t)B * d.out_pad; g.ldb = d.out_pad;
-    g.outf = Gf + d.off_w4; g.sOut = sP; g.ldo = d.out_pad;
-    g.M = H; g.N = d.out_pad; g.K = B;
-    if ((err = gemm<true, false, EPI_ATOMIC>(g, members, splits, s))) return err;
+    TcOperand A{AhT + 2 * sLT, ldT, H, 3 * sLT};
+    TcOperand Bg{dYT, ldT, d.out_pad, (int64_t)d.out_pad * ldT};
+    if ((e = wgrad(A, Bg, H, d.out_pad, d.off_w4))) return e;
     mlp_colsum_kernel<<<dim3((d.out_pad + 127) / 128, members), 128, 0, s>>>(dY, B, d.out_pad, (int64_t)B * d.out_pad,
                                                                              Gf + d.off_b4, sP);
   }
-  // dZ3 = (dY W4^T) * silu'(Z3)
   const __nv_bfloat16* grad_in = dY;
   int64_t s_gin = (int64_t)B * d.out_pad;
   int ld_gin = d.out_pad;
-  int64_t w_off[3] = {d.off_w2, d.off_w3, d.off_w4};
-  int64_t b_off[3] = {d.off_b1, d.off_b2, d.off_b3};
-  int64_t wgrad_off[3] = {d.off_w1, d.off_w2, d.off_w3};
+  const int64_t w_next[3] = {d.off_w2, d.off_w3, d.off_w4};
+  const int64_t b_off[3] = {d.off_b1, d.off_b2, d.off_b3};
+  const int64_t w_off[3] = {d.off_w1, d.off_w2, d.off_w3};
   __nv_bfloat16* bufs[2] = {dZa, dZb};
+  __nv_bfloat16* bufsT[2] = {dZTa, dZTb};
   for (int layer = 2; layer >= 0; --layer) {
     __nv_bfloat16* dZ = bufs[layer & 1];
+    __nv_bfloat16* dZT = bufsT[layer & 1];
     {
-      GemmArgs g{};
-      g.A = grad_in; g.sA = s_gin; g.lda = ld_gin;
-      g.B = Wh + w_off[layer]; g.sB = sP; g.ldb = (layer == 2) ? d.out_pad : H;   // W_{l+1} stored [H][out]
-      g.zprev = Z + layer * sL; g.sZ = sZ;
-      g.outh = dZ; g.sOut = sL; g.ldo = H;
-      g.M = B; g.N = H; g.K = (layer == 2) ? d.out_pad : H;
-      if ((err = gemm<false, true, EPI_DSILU>(g, members, 1, s))) return err;
+      // dZ_l = (grad_in W_{l+1}^T) silu'(Z_l): W_{l+1} stored [H][out] is the K-major [N = H][K = out] operand
+      const int Kn = layer == 2 ? d.out_pad : H;
+      TcOperand A{grad_in, ld_gin, B, s_gin};
+      TcOperand Bw{Wh + w_next[layer], Kn, H, sP};
+      TcGemm g{};
+      g.M = B;
+      g.N = H;
+      g.K = Kn;
+      g.k_split = 1;
+      g.zprev = Z + layer * sL;
+      g.sZ = sZ;
+      g.ldz = H;
+      g.outh = dZ;
+      g.sOuth = sL;
+      g.ldh = H;
+      g.outhT = dZT;
+      g.sOuthT = sLT;
+      g.ldhT = ldT;
+      g.err = err;
+      if ((e = mlp_tc_gemm(EPI_DSILU, A, Bw, g, members, s))) return e;
     }
     {
-      GemmArgs g{};
-      const __nv_bfloat16* in = layer == 0 ? X0 : Ah + (layer - 1) * sL;
-      g.A = in; g.sA = layer == 0 ? sX : sZ; g.lda = layer == 0 ? d.in_pad : H;
-      g.B = dZ; g.sB = sL; g.ldb = H;
-      g.outf = Gf + wgrad_off[layer]; g.sOut = sP; g.ldo = H;
-      g.M = layer == 0 ? d.in_pad : H; g.N = H; g.K = B;
-      if ((err = gemm<true, false, EPI_ATOMIC>(g, members, splits, s))) return err;
+      // dW_l = A_{l-1}^T dZ_l (M = in_l, N = H), db_l = colsum(dZ_l)
+      const int Min = layer == 0 ? d.in_pad : H;
+      TcOperand A = layer == 0 ? TcOperand{X0T, ldT, d.in_pad, (int64_t)d.in_pad * ldT}
+                               : TcOperand{AhT + (layer - 1) * sLT, ldT, H, 3 * sLT};
+      TcOperand Bg{dZT, ldT, H, sLT};
+      if ((e = wgrad(A, Bg, Min, H, w_off[layer]))) return e;
       mlp_colsum_kernel<<<dim3((H + 127) / 128, members), 128, 0, s>>>(dZ, B, H, sL, Gf + b_off[layer], sP);
     }
     grad_in = dZ;
@@ -407,21 +369,22 @@ cudaError_t mlp_backward(const MlpDims& d, int members, int B, const __nv_bfloat
 }
 
 cudaError_t mlp_loss(const MlpDims& d, int members, int B, int valid_rows, const float* Y, const float* T,
-                     __nv_bfloat16* dY, float* loss, cudaStream_t s) {
+                     __nv_bfloat16* dY, __nv_bfloat16* dYT, int ldT, float* loss, cudaStream_t s) {
   const float inv = 1.0f / (float)(std::max(1, valid_rows) * d.K);
   dim3 grid(std::min(1024, (B * d.out_pad + 255) / 256), members);
-  mlp_loss_kernel<<<grid, 256, 0, s>>>(Y, T, B, d.K, d.out_pad, inv, dY, loss, (int64_t)B * d.out_pad,
+  mlp_loss_kernel<<<grid, 256, 0, s>>>(Y, T, B, d.K, d.out_pad, inv, dY, dYT, ldT, loss, (int64_t)B * d.out_pad,
                                        (int64_t)B * d.K);
   return cudaGetLastError();
 }
 
 cudaError_t mlp_adam(const MlpDims& d, int members, float* P, const float* G, float* m, float* v,
-                     __nv_bfloat16* Ph, float lr, int step, cudaStream_t s) {
+                     __nv_bfloat16* Ph, __nv_bfloat16* PhT, float lr, int step, cudaStream_t s) {
   const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
   const float c1 = 1.0f / (1.0f - powf(b1, (float)step));
   const float c2 = 1.0f / (1.0f - powf(b2, (float)step));
   const int64_t n = d.n_params * members;
   mlp_adam_kernel<<<blocks_for(n, 256), 256, 0, s>>>(P, G, m, v, Ph, n, lr, b1, b2, eps, c1, c2);
+  mlp_weights_t_kernel<<<blocks_for(n, 256), 256, 0, s>>>(P, d, members, PhT);
   return cudaGetLastError();
 }
 

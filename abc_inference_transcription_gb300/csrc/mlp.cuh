@@ -8,6 +8,7 @@
 // Output columns: [0, K) means, [K, 2K) log-variances, the rest zero padding.
 #pragma once
 #include <cuda_bf16.h>
+#include <cuda_runtime.h>
 #include <stdint.h>
 
 namespace abc {
@@ -40,9 +41,7 @@ inline MlpDims mlp_dims(int in_dim, int K) {
   return d;
 }
 
-// C[M][N] = op(A) op(B) (+ bias), BF16 operands, FP32 accumulation.
-// TA: A is stored K x M (use A^T); TB: B is stored N x K (use B^T).
-// Epilogues.
+// GEMM epilogues.
 enum MlpEpi : int {
   EPI_HIDDEN = 0,    // z = C + bias -> Zf32 (optional), act = silu(z) -> bf16 out
   EPI_LINEAR = 1,    // C + bias -> fp32 out
@@ -50,17 +49,38 @@ enum MlpEpi : int {
   EPI_DSILU = 3      // bf16 out = C * silu'(Zprev)
 };
 
-struct GemmArgs {
-  const __nv_bfloat16* A;
-  const __nv_bfloat16* B;
-  const float* bias;
-  const float* zprev;   // EPI_DSILU: pre-activation of the layer
-  float* outf;
-  __nv_bfloat16* outh;
-  int M, N, K;
-  int lda, ldb, ldo;
-  int64_t sA, sB, sBias, sZ, sOut;  // per-member strides (blockIdx.z)
-  int k_split;                       // EPI_ATOMIC: K range per blockIdx.y slice... (split count)
+// Tensor-core GEMM C[M][N] = sum_k A[m][k] B[n][k] (mlp_tc.cu): both operands
+// K-major BF16 ([rows][ld], K contiguous; ld * 2 bytes a multiple of 16), one
+// operand set per ensemble member.
+struct TcOperand {
+  const __nv_bfloat16* ptr;
+  int64_t ld;             // elements between rows
+  int64_t rows;           // M for A, N for B
+  int64_t member_stride;  // elements between members
 };
+
+struct TcGemm {
+  int M, N, K;
+  int k_split;   // reduction split over blockIdx.y (EPI_ATOMIC)
+  int a_shared;  // one A for every member
+  const float* bias;
+  int64_t sBias;
+  const float* zprev;  // EPI_DSILU: pre-activation [M][ldz]
+  int64_t sZ;
+  int ldz;
+  float* outf;         // EPI_HIDDEN (optional), EPI_LINEAR, EPI_ATOMIC: [M][ldf]
+  int64_t sOutf;
+  int ldf;
+  __nv_bfloat16* outh;   // EPI_HIDDEN, EPI_DSILU: [M][ldh]
+  int64_t sOuth;
+  int ldh;
+  __nv_bfloat16* outhT;  // optional transposed copy [N][ldhT]
+  int64_t sOuthT;
+  int ldhT;
+  int* err;              // nonzero: a bounded wait ran out
+};
+
+cudaError_t mlp_tc_gemm(int epi, const TcOperand& A, const TcOperand& B, const TcGemm& g, int members,
+                        cudaStream_t s);
 
 }  // namespace abc

@@ -18,20 +18,24 @@
 #include "mlp.cuh"
 
 namespace abc {
-cudaError_t mlp_init(const MlpDims& d, int members, uint64_t seed, float* P, __nv_bfloat16* Ph, cudaStream_t s);
-cudaError_t mlp_to_bf16(const float* src, __nv_bfloat16* dst, int64_t n, cudaStream_t s);
+cudaError_t mlp_init(const MlpDims& d, int members, uint64_t seed, float* P, __nv_bfloat16* Ph, __nv_bfloat16* PhT,
+                     cudaStream_t s);
+cudaError_t mlp_refresh_bf16(const MlpDims& d, int members, const float* P, __nv_bfloat16* Ph, __nv_bfloat16* PhT,
+                             cudaStream_t s);
 cudaError_t mlp_gather(const float* xn, const float* yn, int64_t N, const MlpDims& d, int B, int64_t base,
-                       const uint64_t* perm_ab, int members, __nv_bfloat16* X0, float* T, cudaStream_t s);
+                       const uint64_t* perm_ab, int members, __nv_bfloat16* X0, __nv_bfloat16* X0T, int ldT, float* T,
+                       cudaStream_t s);
 cudaError_t mlp_forward(const MlpDims& d, int members, int B, const __nv_bfloat16* X0, int64_t sX,
-                        const __nv_bfloat16* Wh, const float* Pf, float* Z, __nv_bfloat16* Ah, float* Y,
-                        cudaStream_t s);
-cudaError_t mlp_backward(const MlpDims& d, int members, int B, const __nv_bfloat16* X0, int64_t sX,
-                         const __nv_bfloat16* Wh, const float* Z, const __nv_bfloat16* Ah, const __nv_bfloat16* dY,
-                         __nv_bfloat16* dZa, __nv_bfloat16* dZb, float* Gf, cudaStream_t s);
+                        const __nv_bfloat16* WhT, const float* Pf, float* Z, __nv_bfloat16* Ah, __nv_bfloat16* AhT,
+                        int ldT, float* Y, int* err, cudaStream_t s);
+cudaError_t mlp_backward(const MlpDims& d, int members, int B, const __nv_bfloat16* X0T, const __nv_bfloat16* Wh,
+                         const float* Z, const __nv_bfloat16* AhT, const __nv_bfloat16* dY, const __nv_bfloat16* dYT,
+                         __nv_bfloat16* dZa, __nv_bfloat16* dZb, __nv_bfloat16* dZTa, __nv_bfloat16* dZTb, int ldT,
+                         float* Gf, int* err, cudaStream_t s);
 cudaError_t mlp_loss(const MlpDims& d, int members, int B, int valid_rows, const float* Y, const float* T,
-                     __nv_bfloat16* dY, float* loss, cudaStream_t s);
+                     __nv_bfloat16* dY, __nv_bfloat16* dYT, int ldT, float* loss, cudaStream_t s);
 cudaError_t mlp_adam(const MlpDims& d, int members, float* P, const float* G, float* m, float* v,
-                     __nv_bfloat16* Ph, float lr, int step, cudaStream_t s);
+                     __nv_bfloat16* Ph, __nv_bfloat16* PhT, float lr, int step, cudaStream_t s);
 cudaError_t mlp_combine(const MlpDims& d, int members, int N, const float* Y, const float* ymean, const float* ystd,
                         const float* yscale, double* mean_out, double* var_out, double* disagree, int aleatoric_only,
                         cudaStream_t s);
@@ -256,12 +260,15 @@ struct abc_surrogate {
   int step = 0;
   bool normed = false;
   Buf<float> P, G, Am, Av, ymf, ysf, yscf;  // yscf: asinh scale per statistic (0: identity)
-  Buf<__nv_bfloat16> Ph;
+  Buf<__nv_bfloat16> Ph, PhT;   // BF16 weights as stored and transposed
+  Buf<int> tcerr;                // tensor-core GEMM error word
   Buf<double> xm, xs, ym, ys;
   // training / batch scratch
   Buf<double> th64, st64;
   Buf<float> xn, yn, T, Z, Y;
   Buf<__nv_bfloat16> X0, Ah, dY, dZa, dZb;
+  Buf<__nv_bfloat16> X0T, AhT, dYT, dZTa, dZTb;  // [features][ldT] copies for the weight gradients
+  int ldT = 0;
   Buf<float> loss;
   Buf<uint64_t> perm;
   // prediction scratch
@@ -295,8 +302,39 @@ static int ensure_batch(abc_surrogate* s, int B) {
   SK(s->dY.ensure(E * B * d.out_pad));
   SK(s->dZa.ensure(E * B * d.H));
   SK(s->dZb.ensure(E * B * d.H));
+  s->ldT = (B + 7) / 8 * 8;   // 16-byte rows for the tensor maps
+  const size_t lt = (size_t)s->ldT;
+  SK(s->X0T.ensure(E * d.in_pad * lt));
+  SK(s->AhT.ensure(E * 3 * d.H * lt));
+  SK(s->dYT.ensure(E * d.out_pad * lt));
+  SK(s->dZTa.ensure(E * d.H * lt));
+  SK(s->dZTb.ensure(E * d.H * lt));
   SK(s->loss.ensure(E));
   SK(s->perm.ensure(2 * E));
+  return ABC_OK;
+}
+
+// the tensor-core GEMMs report a bounded wait that ran out in tcerr
+static int check_tc(abc_surrogate* s) {
+  int h = 0;
+  SK(cudaMemcpy(&h, s->tcerr.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h) {
+    SK(cudaMemset(s->tcerr.p, 0, sizeof(int)));
+    return sfail(s, ABC_ERR_CUDA, "tensor-core GEMM: a bounded wait ran out (code " + std::to_string(h) + ")");
+  }
+  return ABC_OK;
+}
+
+// gather a batch, forward, loss and backward (gradients in s->G)
+static int train_step(abc_surrogate* s, int B, int64_t base, int valid, int64_t N) {
+  const MlpDims& d = s->d;
+  const int E = s->members;
+  SK(mlp_gather(s->xn.p, s->yn.p, N, d, B, base, s->perm.p, E, s->X0.p, s->X0T.p, s->ldT, s->T.p, s->stream));
+  SK(mlp_forward(d, E, B, s->X0.p, (int64_t)B * d.in_pad, s->PhT.p, s->P.p, s->Z.p, s->Ah.p, s->AhT.p, s->ldT,
+                 s->Y.p, s->tcerr.p, s->stream));
+  SK(mlp_loss(d, E, B, valid, s->Y.p, s->T.p, s->dY.p, s->dYT.p, s->ldT, s->loss.p, s->stream));
+  SK(mlp_backward(d, E, B, s->X0T.p, s->Ph.p, s->Z.p, s->AhT.p, s->dY.p, s->dYT.p, s->dZa.p, s->dZb.p, s->dZTa.p,
+                  s->dZTb.p, s->ldT, s->G.p, s->tcerr.p, s->stream));
   return ABC_OK;
 }
 
@@ -317,6 +355,7 @@ int abc_surrogate_create(abc_surrogate** out, int in_dim, int n_stats, int ensem
   }
   const size_t n = (size_t)s->d.n_params * ensemble;
   if (s->P.ensure(n) || s->G.ensure(n) || s->Am.ensure(n) || s->Av.ensure(n) || s->Ph.ensure(n) ||
+      s->PhT.ensure(n) || s->tcerr.ensure(1) || cudaMemset(s->tcerr.p, 0, sizeof(int)) != cudaSuccess ||
       s->xm.ensure(kMlpInPad) || s->xs.ensure(kMlpInPad) || s->ym.ensure(n_stats) || s->ys.ensure(n_stats) ||
       s->ymf.ensure(n_stats) || s->ysf.ensure(n_stats) || s->yscf.ensure(n_stats) || s->cnt.ensure(1) ||
       cudaMemset(s->yscf.p, 0, sizeof(float) * n_stats) != cudaSuccess) {
@@ -324,7 +363,7 @@ int abc_surrogate_create(abc_surrogate** out, int in_dim, int n_stats, int ensem
     delete s;
     return ABC_ERR_NOMEM;
   }
-  if (mlp_init(s->d, ensemble, seed, s->P.p, s->Ph.p, s->stream) != cudaSuccess ||
+  if (mlp_init(s->d, ensemble, seed, s->P.p, s->Ph.p, s->PhT.p, s->stream) != cudaSuccess ||
       cudaMemsetAsync(s->Am.p, 0, n * sizeof(float), s->stream) != cudaSuccess ||
       cudaMemsetAsync(s->Av.p, 0, n * sizeof(float), s->stream) != cudaSuccess ||
       cudaStreamSynchronize(s->stream) != cudaSuccess) {
@@ -341,6 +380,8 @@ int abc_surrogate_destroy(abc_surrogate* s) {
   cudaStreamSynchronize(s->stream);
   s->yscf.release();
   s->P.release(); s->G.release(); s->Am.release(); s->Av.release(); s->Ph.release(); s->ymf.release();
+  s->PhT.release(); s->tcerr.release(); s->X0T.release(); s->AhT.release(); s->dYT.release(); s->dZTa.release();
+  s->dZTb.release();
   s->ysf.release(); s->xm.release(); s->xs.release(); s->ym.release(); s->ys.release(); s->th64.release();
   s->st64.release(); s->xn.release(); s->yn.release(); s->T.release(); s->Z.release(); s->Y.release();
   s->X0.release(); s->Ah.release(); s->dY.release(); s->dZa.release(); s->dZb.release(); s->loss.release();
@@ -410,13 +451,10 @@ int abc_surrogate_train(abc_surrogate* s, const double* theta, const double* sta
     int nb = 0;
     for (int64_t base = 0; base < N; base += B, ++nb) {
       const int valid = (int)std::min<int64_t>(B, N - base);
-      SK(mlp_gather(s->xn.p, s->yn.p, N, d, B, base, s->perm.p, E, s->X0.p, s->T.p, s->stream));
-      SK(mlp_forward(d, E, B, s->X0.p, (int64_t)B * d.in_pad, s->Ph.p, s->P.p, s->Z.p, s->Ah.p, s->Y.p, s->stream));
-      SK(mlp_loss(d, E, B, valid, s->Y.p, s->T.p, s->dY.p, s->loss.p, s->stream));
-      SK(mlp_backward(d, E, B, s->X0.p, (int64_t)B * d.in_pad, s->Ph.p, s->Z.p, s->Ah.p, s->dY.p, s->dZa.p,
-                      s->dZb.p, s->G.p, s->stream));
+      st = train_step(s, B, base, valid, N);
+      if (st) return st;
       s->step++;
-      SK(mlp_adam(d, E, s->P.p, s->G.p, s->Am.p, s->Av.p, s->Ph.p, (float)lr, s->step, s->stream));
+      SK(mlp_adam(d, E, s->P.p, s->G.p, s->Am.p, s->Av.p, s->Ph.p, s->PhT.p, (float)lr, s->step, s->stream));
     }
     if (epoch_loss) {
       std::vector<float> hl(E);
@@ -428,7 +466,7 @@ int abc_surrogate_train(abc_surrogate* s, const double* theta, const double* sta
     }
   }
   SK(cudaStreamSynchronize(s->stream));
-  return ABC_OK;
+  return check_tc(s);
 }
 
 // one forward/backward pass without update: per-member loss and gradients
@@ -449,11 +487,8 @@ int abc_surrogate_gradients(abc_surrogate* s, const double* theta, const double*
   for (int e = 0; e < E; ++e) { ab[2 * e] = 1; ab[2 * e + 1] = 0; }
   SK(cudaMemcpyAsync(s->perm.p, ab.data(), sizeof(uint64_t) * 2 * E, cudaMemcpyHostToDevice, s->stream));
   SK(cudaMemsetAsync(s->loss.p, 0, sizeof(float) * E, s->stream));
-  SK(mlp_gather(s->xn.p, s->yn.p, N, d, B, 0, s->perm.p, E, s->X0.p, s->T.p, s->stream));
-  SK(mlp_forward(d, E, B, s->X0.p, (int64_t)B * d.in_pad, s->Ph.p, s->P.p, s->Z.p, s->Ah.p, s->Y.p, s->stream));
-  SK(mlp_loss(d, E, B, B, s->Y.p, s->T.p, s->dY.p, s->loss.p, s->stream));
-  SK(mlp_backward(d, E, B, s->X0.p, (int64_t)B * d.in_pad, s->Ph.p, s->Z.p, s->Ah.p, s->dY.p, s->dZa.p, s->dZb.p,
-                  s->G.p, s->stream));
+  st = train_step(s, B, 0, B, N);
+  if (st) return st;
   std::vector<float> hl(E);
   SK(cudaMemcpyAsync(hl.data(), s->loss.p, sizeof(float) * E, cudaMemcpyDeviceToHost, s->stream));
   if (grads)
@@ -461,7 +496,7 @@ int abc_surrogate_gradients(abc_surrogate* s, const double* theta, const double*
   SK(cudaStreamSynchronize(s->stream));
   if (loss)
     for (int e = 0; e < E; ++e) loss[e] = hl[e];
-  return ABC_OK;
+  return check_tc(s);
 }
 
 int abc_surrogate_get_params(abc_surrogate* s, float* params) {
@@ -475,7 +510,7 @@ int abc_surrogate_set_params(abc_surrogate* s, const float* params) {
   if (!s || !params) return ABC_ERR_INVALID;
   const int64_t n = s->d.n_params * s->members;
   SK(cudaMemcpyAsync(s->P.p, params, sizeof(float) * n, cudaMemcpyHostToDevice, s->stream));
-  SK(mlp_to_bf16(s->P.p, s->Ph.p, n, s->stream));
+  SK(mlp_refresh_bf16(s->d, s->members, s->P.p, s->Ph.p, s->PhT.p, s->stream));
   SK(cudaStreamSynchronize(s->stream));
   return ABC_OK;
 }
@@ -520,7 +555,8 @@ static int predict_chunk(abc_surrogate* s, const double* d_theta, int ld, int64_
   norm_x_kernel<<<blocks(n * d.in_pad), 256, 0, s->stream>>>(d_theta, n, d.in_dim, ld, s->xm.p, s->xs.p, d.in_pad,
                                                               nullptr, s->X0.p);
   SK(cudaGetLastError());
-  SK(mlp_forward(d, E, (int)n, s->X0.p, 0, s->Ph.p, s->P.p, nullptr, s->Ah.p, s->Y.p, s->stream));
+  SK(mlp_forward(d, E, (int)n, s->X0.p, 0, s->PhT.p, s->P.p, nullptr, s->Ah.p, nullptr, 0, s->Y.p, s->tcerr.p,
+                 s->stream));
   SK(mlp_combine(d, E, (int)n, s->Y.p, s->ymf.p, s->ysf.p, s->yscf.p, d_mean, d_var, d_dis, aleatoric_only,
                  s->stream));
   return ABC_OK;
@@ -538,7 +574,7 @@ int abc_surrogate_predict_device(abc_surrogate* s, const double* d_theta, int ld
     if (st) return st;
   }
   SK(cudaStreamSynchronize(s->stream));
-  return ABC_OK;
+  return check_tc(s);
 }
 
 int abc_surrogate_predict(abc_surrogate* s, const double* theta, int64_t N, double* mean, double* var,
@@ -623,7 +659,7 @@ int abc_surrogate_screen_device(abc_surrogate* s, const double* d_theta, int ld_
   SK(cudaStreamSynchronize(s->stream));
   eo.release();
   if (n_keep) *n_keep = (int64_t)hk;
-  return ABC_OK;
+  return check_tc(s);
 }
 
 // Rows with keep[p] != 0, in ascending order: theta rows copied to d_theta_out
