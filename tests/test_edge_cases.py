@@ -1,0 +1,115 @@
+"""Edge cases of the distance/acceptance step (every candidate-pass mode), the
+moment ODE and the data-side statistics against the oracle: single particles
+and genes, K = 1, all-NaN statistics, q = 1, eps = 0, eps at and above the
+clip, tile boundaries, no candidates, extreme rates, silent genes."""
+import numpy as np
+import pytest
+
+from abc_inference_transcription_gb300 import abi
+from abc_inference_transcription_gb300.config import (beta_moments, make_config, reference_prior,
+                                                      synthetic_cells)
+
+pytestmark = pytest.mark.gpu
+MODES = (0, 1, 2)
+
+
+@pytest.fixture(scope="module")
+def Ctx(built):
+    from abc_inference_transcription_gb300.host import Context
+    return Context
+
+
+def _problem(P, G, K, seed):
+    rng = np.random.default_rng(seed)
+    base = np.abs(rng.normal(5.0, 3.0, (50, K))) + 0.1
+    stats = base[rng.integers(0, 50, P)] * rng.lognormal(0, 0.2, (P, K))
+    data = base[rng.integers(0, 50, G)] * rng.lognormal(0, 0.05, (G, K))
+    se = 0.1 * np.abs(data) * rng.lognormal(0, 0.5, (G, K))
+    return data, se, stats
+
+
+def _check(ctx, orc, data, se, stats, sel, x):
+    off, idx, err = ctx.select(data, se, stats, sel, x, None)
+    roff, ridx = orc.accept(orc.errors(data, se, stats, None), sel, x)
+    assert np.array_equal(off, roff), (sel, x)
+    assert np.array_equal(idx, ridx), (sel, x)
+    return off
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("P,G,K", [(1, 1, 72), (1, 5, 53), (7, 1, 1), (129, 257, 72), (300, 3, 2)])
+def test_selection_shapes(Ctx, orc, mode, P, G, K):
+    data, se, stats = _problem(P, G, K, P * 1000 + G + K)
+    with Ctx(make_config("hour"), None) as ctx:
+        ctx.set_distance_mode(mode)
+        for sel, x in ((0, 4.8), (0, 0.0), (0, 10.0), (0, 25.0), (1, 1.0), (1, 0.3), (1, 1e-9)):
+            _check(ctx, orc, data, se, stats, sel, x)
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_selection_nan_and_no_candidates(Ctx, orc, mode):
+    data, se, stats = _problem(400, 40, 24, 3)
+    stats[::3] = np.nan                     # a third of the particles all-NaN
+    data[5] = np.nan                        # a gene with NaN data
+    with Ctx(make_config("hour"), None) as ctx:
+        ctx.set_distance_mode(mode)
+        off = _check(ctx, orc, data, se, stats, 0, 1e-12)   # almost nothing accepted
+        _check(ctx, orc, data, se, stats, 1, 0.05)
+        _check(ctx, orc, data, se, stats, 1, 1.0)           # every non-NaN particle, NaN last
+        all_nan = np.full_like(stats, np.nan)
+        off = _check(ctx, orc, data, se, all_nan, 1, 0.1)
+        assert off[-1] == 0
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_selection_per_gene_extreme_thresholds(Ctx, orc, mode):
+    data, se, stats = _problem(500, 6, 16, 8)
+    thr = np.array([-1.0, 0.0, 1e-300, 10.0, 50.0, 2.0])
+    err = orc.errors(data, se, stats, None)
+    with Ctx(make_config("hour"), None) as ctx:
+        ctx.set_distance_mode(mode)
+        off, idx, _ = ctx.select_thr(data, se, stats, thr, None)
+    want_off, want_idx = [0], []
+    for g in range(6):
+        _, i = orc.accept(err[:, g:g + 1], 0, thr[g])
+        want_idx.append(i)
+        want_off.append(want_off[-1] + i.shape[0])
+    assert np.array_equal(off, want_off) and np.array_equal(idx, np.concatenate(want_idx))
+    assert off[1] == 0                      # thr < 0 accepts nothing
+    assert off[5] - off[4] == 500           # thr >= 10 accepts every finite particle
+
+
+def test_moment_single_particle_and_stiff_rates(Ctx, orc):
+    cfg = make_config("hour", precision=abi.FP64)
+    cells = synthetic_cells(seed=2)
+    bm = beta_moments(cells, 5)
+    iv = np.zeros(9)
+    iv[1] = 0.5
+    th = np.array([[3.0, -3.0, 3.0, 2.0, 0.0],      # fast switching, fast transcription, fast decay
+                   [-3.0, 3.0, -3.0, -3.0, -0.7],   # almost silent
+                   [0.0, 0.0, 2.5, -2.9, -0.3]])    # slow decay
+    with Ctx(cfg, cells) as ctx:
+        for r in range(th.shape[0]):
+            got = ctx.moment_simulate(1, th[r:r + 1], iv, bm, cells.age_dist, moments=True)
+            want = orc.moment_model(cfg, 1, th[r], iv, beta_mom=bm, age_dist=cells.age_dist)
+            assert np.array_equal(got["moments"][0], want["moments"])
+            assert np.array_equal(got["stats"][0], want["stats"], equal_nan=True)
+            assert got["transient_iters"][0] == want["transient_iters"]
+
+
+def test_data_stats_silent_and_minimal_cells(Ctx, orc):
+    cfg = make_config("hour")
+    cells = synthetic_cells(n_per_pulse=10, n_per_chase=10, seed=6)   # 2 cells per (condition, age) group
+    rng = np.random.default_rng(1)
+    C = cells.cond.shape[0]
+    u = rng.poisson(3.0, (4, C)).astype(np.int32)
+    l = rng.poisson(1.0, (4, C)).astype(np.int32)
+    u[1] = 0
+    l[1] = 0                                # a silent gene: FF with eps, ratios 0, correlations 0
+    l[2] = 0                                # labelled species silent
+    with Ctx(cfg, cells) as ctx:
+        st, se = ctx.data_stats(u, l, n_boot=50, seed=4)
+    want_st, want_se = orc.data_stats(cfg, cells, u, l, n_boot=50, seed=4)
+    assert np.array_equal(st, want_st, equal_nan=True)
+    assert np.array_equal(se, want_se, equal_nan=True)
+    assert (st[1][:20] == 0).all() and (st[1][20:] == 0).all()
