@@ -80,7 +80,7 @@ struct abc_ctx {
   size_t ev_used = 0;
   double phase_ms[3] = {0, 0, 0};
   // selection workspace and results
-  DBuf<double> d_data, d_se, d_sel_stats, d_e64, d_se64, d_out_err, d_den, d_rden;
+  DBuf<double> d_data, d_se, d_sel_stats, d_se64, d_out_err, d_den, d_rden;
   DBuf<float> d_sw, d_dw, d_s32, d_X, d_esub;
   DBuf<Cand> d_cand;
   DBuf<float> d_cande;  // FP32 error of each candidate
@@ -93,7 +93,7 @@ struct abc_ctx {
   DBuf<int> d_tcerr;
   DBuf<Cand> d_seg, d_cand2;
   int64_t seg_cap = int64_t(1) << 16;
-  DBuf<int32_t> d_sp;
+  DBuf<int32_t> d_sp, d_sg;
   DBuf<int64_t> d_gcount, d_goff, d_alen, d_aoff, d_out_idx;
   DBuf<unsigned long long> d_gcursor, d_ncand;
   DBuf<int> d_fail;
@@ -214,7 +214,7 @@ int abc_destroy(abc_ctx* c) {
   c->d_beta.release(); c->d_age_dist.release(); c->d_theta.release(); c->d_stats.release();
   c->d_models.release(); c->d_order.release(); c->d_ohist.release(); c->d_rec.release(); c->d_recf.release(); c->d_counts.release(); c->d_captured.release();
   c->d_events.release(); c->d_hash.release(); c->d_misc.release(); c->d_status.release();
-  c->d_data.release(); c->d_se.release(); c->d_sel_stats.release(); c->d_e64.release(); c->d_se64.release();
+  c->d_data.release(); c->d_se.release(); c->d_sel_stats.release(); c->d_se64.release(); c->d_sg.release();
   c->d_out_err.release(); c->d_sw.release(); c->d_dw.release(); c->d_s32.release(); c->d_X.release();
   c->d_esub.release(); c->d_cand.release(); c->d_sp.release(); c->d_gcount.release(); c->d_goff.release();
   c->d_cande.release(); c->d_den.release(); c->d_rden.release(); c->d_tcA.release(); c->d_tcB.release(); c->d_cg32.release(); c->d_b0.release();
@@ -1049,12 +1049,11 @@ static int select_impl(abc_ctx* c, const double* data, const double* se, int64_t
       rc = c->d_cand2.p;
       Xacc = c->d_Xt.p;
     }
-    CK(c->d_e64.ensure((size_t)std::max<int64_t>(nre, 1)));
     CK(c->d_se64.ensure((size_t)std::max<int64_t>(nre, 1)));
     CK(c->d_sp.ensure((size_t)std::max<int64_t>(nre, 1)));
-    CK(launch_dist_recheck(in, rc, nre, c->d_e64.p, c->stream));
-    CK(launch_dist_group_sort(rc, c->d_e64.p, nre, G, c->d_gcount.p, c->d_goff.p, c->d_sp.p, c->d_se64.p,
-                              c->d_gcursor.p, c->stream));
+    CK(c->d_sg.ensure((size_t)std::max<int64_t>(nre, 1)));
+    CK(launch_dist_group_recheck_sort(in, rc, nre, c->d_gcount.p, c->d_goff.p, c->d_gcursor.p, c->d_sp.p,
+                                      c->d_sg.p, c->d_se64.p, c->stream));
     CK(cudaMemsetAsync(c->d_fail.p, 0, sizeof(int) * G, c->stream));
     CK(launch_dist_accept_len(c->d_goff.p, c->d_se64.p, G, mode == 2 ? 0 : mode, eps_or_q,
                               mode == 2 ? c->d_thr.p : nullptr, kq, Xacc, c->d_b0.p, b1, c->d_alen.p, c->d_fail.p,

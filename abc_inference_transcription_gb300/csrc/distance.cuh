@@ -36,11 +36,14 @@ ABC_HDF float dist_bound_f(float e, int K) {
 // RN(a / b) (Markstein's theorem: P. Markstein, IBM J. Res. Dev. 34(1), 1990;
 // J.-M. Muller et al., Handbook of Floating-Point Arithmetic, ch. 4).  The
 // theorem needs a, b and the quotient away from underflow and overflow; outside
-// [2^-900, 2^900] x [2^-400, 2^400] (and for zero, NaN, infinity) the IEEE
-// division is used.
+// [2^-900, 2^900) x [2^-400, 2^400) (and for zero, NaN, infinity) the IEEE
+// division is used.  The ranges are tested on the biased exponent fields with
+// integer instructions: FP64 comparisons would share the FP64 pipe, the
+// recheck's bottleneck, with the six arithmetic operations of a term.
 __device__ __forceinline__ double div_rn(double a, double b, double y) {
-  const double fa = fabs(a), fb = fabs(b);
-  if (fa >= 0x1p-900 && fa <= 0x1p+900 && fb >= 0x1p-400 && fb <= 0x1p+400) {
+  const unsigned ea = ((unsigned)__double2hiint(a) >> 20) & 0x7ffu;  // 2^-900 = 2^(123 - 1023)
+  const unsigned eb = ((unsigned)__double2hiint(b) >> 20) & 0x7ffu;  // 2^-400 = 2^(623 - 1023)
+  if (ea - 123u < 1800u && eb - 623u < 800u) {
     const double q0 = a * y;
     const double r = fma(-q0, b, a);
     return fma(r, y, q0);

@@ -3,6 +3,8 @@
 // oracle; built with -fmad=false), the full FP64 error matrix, and the
 // per-gene grouping and (err, index) sort of accepted particles
 // (scripts/accepted_particles.jl:20-26: findall + sortperm).
+#include <algorithm>
+
 #include "distance.cuh"
 #include "kernels.h"
 
@@ -99,18 +101,94 @@ __device__ __forceinline__ double err_exact(const DistInputs& in, int64_t p, int
   return tot;
 }
 
-__global__ void dist_recheck_kernel(DistInputs in, const Cand* cand, int64_t n, double* e64) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    Cand c = cand[i];
-    e64[i] = err_exact(in, c.p, c.g);
-  }
-}
+// FP64 errors of candidates already grouped by gene (sp, sg: particle and gene
+// of each entry).  A warp takes 32 consecutive entries and walks the
+// statistics in chunks of kRecheckCols columns: it copies the chunk of its 32
+// rows into shared memory with coalesced loads (consecutive lanes read
+// consecutive values, rows back to back), then each lane adds its pair's terms
+// of that chunk from shared memory, carrying the family sums across chunks.
+// The gene rows it reads (data, den, rden) are mostly the same for the whole
+// warp and are broadcast.  Row stride kRecheckCols + 1 (odd) keeps the lanes'
+// column reads on distinct banks; the small chunk keeps 32 warps resident per
+// SM, enough to keep the FP64 pipe (the bound: six FP64 operations per term)
+// busy.
+constexpr int kRecheckWarps = 8;
+constexpr int kRecheckCols = 24;
+constexpr int kRecheckLd = kRecheckCols + 1;
 
-cudaError_t launch_dist_recheck(const DistInputs& in, const Cand* cand, int64_t n, double* e64, cudaStream_t s) {
-  if (n <= 0) return cudaSuccess;
-  int blocks = (int)((n + 127) / 128 < 65536 ? (n + 127) / 128 : 65536);
-  dist_recheck_kernel<<<blocks, 128, 0, s>>>(in, cand, n, e64);
-  return cudaGetLastError();
+__global__ void __launch_bounds__(kRecheckWarps * 32) recheck_grouped_kernel(DistInputs in, const int32_t* sp,
+                                                                             const int32_t* sg, int64_t n,
+                                                                             double* se64) {
+  __shared__ double rs_smem[kRecheckWarps * 32 * kRecheckLd];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int K = in.K;
+  double* S = rs_smem + warp * 32 * kRecheckLd;
+  const double nK = (double)K;
+  const double rK = 1.0 / nK;
+  const int64_t n_chunks = (n + 31) >> 5;
+  const int64_t wstride = (int64_t)gridDim.x * kRecheckWarps;
+  for (int64_t ch = (int64_t)blockIdx.x * kRecheckWarps + warp; ch < n_chunks; ch += wstride) {
+    const int64_t i = ch * 32 + lane;
+    const bool mine = i < n;
+    const int32_t p = mine ? sp[i] : 0;
+    const int64_t g = mine ? sg[i] : 0;
+    const int rows = (int)(n - ch * 32 < 32 ? n - ch * 32 : 32);
+    const double* d = in.data + g * K;
+    const double* dn = in.den + g * K;
+    const double* ry = in.rden + g * K;
+    double tot = 0.0, part = 0.0;
+    // families: f is the open one, fend the column after its last term
+    int f = 0, fend = in.fam[0];
+    while (fend == 0 && f < in.n_fam) {  // leading empty families add 0 / K
+      tot = tot + div_rn(part, nK, rK);
+      ++f;
+      fend = f < in.n_fam ? fend + in.fam[f] : -1;
+    }
+    for (int c0 = 0; c0 < K; c0 += kRecheckCols) {
+      const int cw = K - c0 < kRecheckCols ? K - c0 : kRecheckCols;
+      // flat copy of rows x cw values: lane takes e = lane + 32 t, (r, c) = divmod(e, cw)
+      const int T = (rows * cw + 31) >> 5;
+      int r = lane / cw, c = lane - (lane / cw) * cw;
+      for (int t0 = 0; t0 < T; t0 += 8) {
+        double v[8];
+        int dst[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int32_t pr = __shfl_sync(0xffffffffu, p, r < 31 ? r : 31);
+          const bool take = t0 + u < T && r < rows;
+          dst[u] = take ? r * kRecheckLd + c : -1;
+          v[u] = take ? __ldg(in.stats + (int64_t)pr * K + c0 + c) : 0.0;
+          c += 32;
+          while (c >= cw) {
+            c -= cw;
+            ++r;
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (dst[u] >= 0) S[dst[u]] = v[u];
+      }
+      __syncwarp();
+      if (mine) {
+        const double* s = S + lane * kRecheckLd - c0;
+        for (int k = c0; k < c0 + cw; ++k) {
+          const double diff = __ldg(d + k) - s[k];
+          part = part + div_rn(diff * diff, __ldg(dn + k), __ldg(ry + k));
+          while (k + 1 == fend) {  // close this family and any empty ones after it
+            tot = tot + div_rn(part, nK, rK);
+            part = 0.0;
+            ++f;
+            fend = f < in.n_fam ? fend + in.fam[f] : -1;
+          }
+        }
+      }
+      __syncwarp();
+    }
+    if (mine) {
+      if (tot > 10.0) tot = 10.0;
+      se64[i] = tot;
+    }
+  }
 }
 
 __global__ void dist_full_kernel(DistInputs in, double* err) {
@@ -163,19 +241,27 @@ __global__ void __launch_bounds__(1024) scan_kernel(const int64_t* cnt, int64_t 
   if (G == 0 && threadIdx.x == 0) off[0] = 0;
 }
 
-__global__ void scatter_kernel(const Cand* cand, const double* e64, int64_t n, const int64_t* goff,
-                               unsigned long long* cursor, int32_t* sp, double* se64) {
+__global__ void scatter_kernel(const Cand* cand, int64_t n, const int64_t* goff, unsigned long long* cursor,
+                               int32_t* sp, int32_t* sg) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     Cand c = cand[i];
     unsigned long long pos = (unsigned long long)goff[c.g] + atomicAdd(&cursor[c.g], 1ull);
     sp[pos] = c.p;
-    se64[pos] = e64[i];
+    sg[pos] = c.g;
   }
 }
 
-// Per-gene sort by (err, p): bitonic network in its all-ascending form, so
-// that padding the segment to a power of two with +inf needs no storage (a
-// real element is never exchanged with a padding slot).  NaN sorts last.
+// Per-gene sort by (err, p): bitonic network in its all-ascending form (the
+// first step of every merge pairs i with i ^ (k - 1)).  NaN sorts last, ties by
+// index.  Segments up to kSortSmem entries are padded to a power of two n2 and
+// held in registers, EPT = n2 / 1024 consecutive entries per thread (at least
+// one, 32 threads at least); steps whose partner lies in the same thread run on
+// registers, steps whose partner lies in the same warp on shuffles, and only
+// the steps across warps (partner distance >= 32 EPT) go through shared memory.
+// Keys are the bit patterns of the errors (monotone for non-negative doubles;
+// NaN canonicalised to one pattern), compared with the index as tie-break;
+// padding slots carry (all ones, INT32_MAX), above every real entry.
+// Longer segments run the same network in global memory.
 __device__ __forceinline__ bool key_less(double ea, int32_t pa, double eb, int32_t pb) {
   const bool na = ea != ea, nb = eb != eb;
   if (na != nb) return nb;
@@ -183,10 +269,144 @@ __device__ __forceinline__ bool key_less(double ea, int32_t pa, double eb, int32
   return ea < eb || (ea == eb && pa < pb);
 }
 
-constexpr int kSortSmem = 8192;  // segments up to this size sort in shared memory
+constexpr int kSortSmem = 8192;  // segments up to this size sort in registers
+constexpr uint64_t kNanKey = 0x7ff8000000000000ull;
 
-__global__ void __launch_bounds__(1024) segsort_kernel(const int64_t* goff, int32_t* sp, double* se64) {
-  extern __shared__ double sort_smem[];
+__device__ __forceinline__ uint64_t err_key(double e) {
+  if (e != e) return kNanKey;
+  if (e == 0.0) return 0ull;  // +0 and -0
+  return (uint64_t)__double_as_longlong(e);
+}
+
+// (ka, pa) receives the smaller entry
+__device__ __forceinline__ void cas_lo(uint64_t& ka, int32_t& pa, uint64_t& kb, int32_t& pb) {
+  const bool sw = kb < ka || (kb == ka && pb < pa);
+  const uint64_t tk = sw ? kb : ka;
+  const int32_t tp = sw ? pb : pa;
+  kb = sw ? ka : kb;
+  pb = sw ? pa : pb;
+  ka = tk;
+  pa = tp;
+}
+
+// own entry becomes min (lower) or max of (own, other)
+__device__ __forceinline__ void keep(uint64_t& k, int32_t& p, uint64_t ok, int32_t op, bool lower) {
+  const bool other_less = ok < k || (ok == k && op < p);
+  const bool take = lower ? other_less : !other_less;
+  k = take ? ok : k;
+  p = take ? op : p;
+}
+
+template <int EPT, int J, bool FLIP>
+__device__ __forceinline__ void step_in_thread(uint64_t* key, int32_t* pp) {
+#pragma unroll
+  for (int e = 0; e < EPT; ++e) {
+    const int f = FLIP ? (e ^ (2 * J - 1)) : (e ^ J);
+    if (f > e) cas_lo(key[e], pp[e], key[f], pp[f]);
+  }
+}
+
+template <int EPT>
+__device__ __forceinline__ void in_thread(uint64_t* key, int32_t* pp, int j, bool flip) {
+  if (EPT >= 2 && j == 1) {
+    if (flip) step_in_thread<EPT, 1, true>(key, pp); else step_in_thread<EPT, 1, false>(key, pp);
+  } else if (EPT >= 4 && j == 2) {
+    if (flip) step_in_thread<EPT, 2, true>(key, pp); else step_in_thread<EPT, 2, false>(key, pp);
+  } else if (EPT >= 8 && j == 4) {
+    if (flip) step_in_thread<EPT, 4, true>(key, pp); else step_in_thread<EPT, 4, false>(key, pp);
+  }
+}
+
+__device__ __forceinline__ void shfl_entry(uint64_t k, int32_t p, int mask, uint64_t& ok, int32_t& op) {
+  const unsigned lo = __shfl_xor_sync(0xffffffffu, (unsigned)k, mask);
+  const unsigned hi = __shfl_xor_sync(0xffffffffu, (unsigned)(k >> 32), mask);
+  op = __shfl_xor_sync(0xffffffffu, p, mask);
+  ok = ((uint64_t)hi << 32) | lo;
+}
+
+template <int EPT>
+__device__ void sort_segment_regs(int32_t* P, double* E, int m, int n2, uint64_t* sK, int32_t* sP) {
+  const int t = threadIdx.x;
+  const int nt = n2 / EPT > 32 ? n2 / EPT : 32;  // threads holding entries
+  const bool act = t < nt;
+  uint64_t key[EPT];
+  int32_t pp[EPT];
+#pragma unroll
+  for (int e = 0; e < EPT; ++e) {
+    const int i = t * EPT + e;
+    const bool real = act && i < m;
+    key[e] = real ? err_key(E[i]) : ~0ull;
+    pp[e] = real ? P[i] : 0x7fffffff;
+  }
+  for (int k = 2; k <= n2; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      const bool flip = j == (k >> 1);
+      if (j < EPT) {
+        in_thread<EPT>(key, pp, j, flip);
+      } else if (j < 32 * EPT) {
+        if (act) {
+          if (!flip) {
+            const int mask = j / EPT;
+            const bool lower = (t & mask) == 0;
+#pragma unroll
+            for (int e = 0; e < EPT; ++e) {
+              uint64_t ok;
+              int32_t op;
+              shfl_entry(key[e], pp[e], mask, ok, op);
+              keep(key[e], pp[e], ok, op, lower);
+            }
+          } else {
+            // entry e pairs with the partner's entry EPT - 1 - e
+            const int mask = k / EPT - 1;
+            const bool lower = (t & ((mask + 1) >> 1)) == 0;
+#pragma unroll
+            for (int e = 0; e < (EPT + 1) / 2; ++e) {
+              const int f = EPT - 1 - e;
+              uint64_t o1, o2;
+              int32_t q1, q2;
+              shfl_entry(key[f], pp[f], mask, o1, q1);
+              if (f != e) shfl_entry(key[e], pp[e], mask, o2, q2);
+              keep(key[e], pp[e], o1, q1, lower);
+              if (f != e) keep(key[f], pp[f], o2, q2, lower);
+            }
+          }
+        }
+      } else {
+        // across warps: entry (t, e) in slot e * nt + t
+        if (act) {
+#pragma unroll
+          for (int e = 0; e < EPT; ++e) {
+            sK[e * nt + t] = key[e];
+            sP[e * nt + t] = pp[e];
+          }
+        }
+        __syncthreads();
+        if (act) {
+          const int mask = flip ? k / EPT - 1 : j / EPT;
+          const bool lower = (t & (flip ? (mask + 1) >> 1 : mask)) == 0;
+          const int tp = t ^ mask;
+#pragma unroll
+          for (int e = 0; e < EPT; ++e) {
+            const int f = flip ? EPT - 1 - e : e;
+            keep(key[e], pp[e], sK[f * nt + tp], sP[f * nt + tp], lower);
+          }
+        }
+        __syncthreads();
+      }
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < EPT; ++e) {
+    const int i = t * EPT + e;
+    if (act && i < m) {
+      E[i] = __longlong_as_double((long long)key[e]);
+      P[i] = pp[e];
+    }
+  }
+}
+
+__global__ void __launch_bounds__(1024, 1) segsort_kernel(const int64_t* goff, int32_t* sp, double* se64) {
+  extern __shared__ uint64_t sort_smem[];
   const int64_t g = blockIdx.x;
   const int64_t base = goff[g];
   const int64_t n = goff[g + 1] - base;
@@ -196,36 +416,13 @@ __global__ void __launch_bounds__(1024) segsort_kernel(const int64_t* goff, int3
   int64_t n2 = 1;
   while (n2 < n) n2 <<= 1;
   if (n2 <= kSortSmem) {
-    double* Es = sort_smem;
-    int32_t* Ps = reinterpret_cast<int32_t*>(sort_smem + kSortSmem);
-    const int m = (int)n;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) {
-      Es[i] = E[i];
-      Ps[i] = P[i];
-    }
-    __syncthreads();
-    for (int k = 2; k <= (int)n2; k <<= 1) {
-      for (int j = k >> 1; j > 0; j >>= 1) {
-        for (int i = threadIdx.x; i < (int)n2; i += blockDim.x) {
-          const int partner = (j == (k >> 1)) ? (i ^ (k - 1)) : (i ^ j);
-          if (partner > i && partner < m) {
-            const double ea = Es[i], eb = Es[partner];
-            const int32_t pa = Ps[i], pb = Ps[partner];
-            if (key_less(eb, pb, ea, pa)) {
-              Es[i] = eb;
-              Es[partner] = ea;
-              Ps[i] = pb;
-              Ps[partner] = pa;
-            }
-          }
-        }
-        __syncthreads();
-      }
-    }
-    for (int i = threadIdx.x; i < m; i += blockDim.x) {
-      E[i] = Es[i];
-      P[i] = Ps[i];
-    }
+    uint64_t* sK = sort_smem;
+    int32_t* sP = reinterpret_cast<int32_t*>(sort_smem + kSortSmem);
+    const int m = (int)n, w = (int)n2;
+    if (w <= 1024) sort_segment_regs<1>(P, E, m, w, sK, sP);
+    else if (w == 2048) sort_segment_regs<2>(P, E, m, w, sK, sP);
+    else if (w == 4096) sort_segment_regs<4>(P, E, m, w, sK, sP);
+    else sort_segment_regs<8>(P, E, m, w, sK, sP);
     return;
   }
   for (int64_t k = 2; k <= n2; k <<= 1) {
@@ -252,9 +449,10 @@ __global__ void __launch_bounds__(1024) segsort_kernel(const int64_t* goff, int3
   }
 }
 
-cudaError_t launch_dist_group_sort(const Cand* cand, const double* e64, int64_t n, int64_t G, int64_t* gcount,
-                                   int64_t* goff, int32_t* sp, double* se64, unsigned long long* gcursor,
-                                   cudaStream_t s) {
+cudaError_t launch_dist_group_recheck_sort(const DistInputs& in, const Cand* cand, int64_t n, int64_t* gcount,
+                                           int64_t* goff, unsigned long long* gcursor, int32_t* sp, int32_t* sg,
+                                           double* se64, cudaStream_t s) {
+  const int64_t G = in.G;
   cudaError_t err = cudaMemsetAsync(gcount, 0, sizeof(int64_t) * (size_t)G, s);
   if (err) return err;
   err = cudaMemsetAsync(gcursor, 0, sizeof(unsigned long long) * (size_t)G, s);
@@ -264,10 +462,19 @@ cudaError_t launch_dist_group_sort(const Cand* cand, const double* e64, int64_t 
     gene_count_kernel<<<blocks, 256, 0, s>>>(cand, n, gcount);
   }
   scan_kernel<<<1, 1024, 0, s>>>(gcount, G, goff);
-  if (n > 0) {
+  if (n <= 0) return cudaGetLastError();
+  {
     int blocks = (int)((n + 255) / 256 < 65536 ? (n + 255) / 256 : 65536);
-    scatter_kernel<<<blocks, 256, 0, s>>>(cand, e64, n, goff, gcursor, sp, se64);
-    constexpr int smem = kSortSmem * (int)(sizeof(double) + sizeof(int32_t));
+    scatter_kernel<<<blocks, 256, 0, s>>>(cand, n, goff, gcursor, sp, sg);
+  }
+  {
+    const int64_t chunks = (n + 31) / 32;
+    const int64_t want = (chunks + kRecheckWarps - 1) / kRecheckWarps;
+    int blocks = (int)(want < 65536 ? want : 65536);
+    recheck_grouped_kernel<<<blocks, kRecheckWarps * 32, 0, s>>>(in, sp, sg, n, se64);
+  }
+  {
+    constexpr int smem = kSortSmem * (int)(sizeof(uint64_t) + sizeof(int32_t));
     static bool attr = false;
     if (!attr) {
       err = cudaFuncSetAttribute(segsort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);

@@ -120,12 +120,12 @@ cudaError_t launch_refine(const Cand* cand, const float* cand_e, int64_t n, int6
 // den[g][k] = (se^2 + 0.01 d^2) + eps_gk, the denominators of the error terms,
 // evaluated as in the per-term FP64 expression (bit-identical), and rden = 1/den.
 cudaError_t launch_dist_den(const DistInputs& in, double* den, double* rden, cudaStream_t s);
-// FP64 error of each candidate, in the reference's operation order.
-cudaError_t launch_dist_recheck(const DistInputs& in, const Cand* cand, int64_t n, double* e64, cudaStream_t s);
-// group candidates by gene and sort each gene's list by (err, p).
-cudaError_t launch_dist_group_sort(const Cand* cand, const double* e64, int64_t n, int64_t G,
-                                   int64_t* gcount, int64_t* goff, int32_t* sp, double* se64,
-                                   unsigned long long* gcursor, cudaStream_t s);
+// Group candidates by gene (goff: G + 1 offsets; sp, sg: particle and gene per
+// entry), evaluate their FP64 errors in the reference's operation order (se64;
+// needs in.den and in.rden) and sort each gene's list by (err, p).
+cudaError_t launch_dist_group_recheck_sort(const DistInputs& in, const Cand* cand, int64_t n, int64_t* gcount,
+                                           int64_t* goff, unsigned long long* gcursor, int32_t* sp, int32_t* sg,
+                                           double* se64, cudaStream_t s);
 // accepted prefix length per gene (mode 0: err <= eps; mode 1: the k smallest
 // finite errors) and, in mode 1, a failure flag when the candidate threshold
 // X[g] could have excluded a member of the top k.

@@ -113,3 +113,17 @@ def test_data_stats_silent_and_minimal_cells(Ctx, orc):
     assert np.array_equal(st, want_st, equal_nan=True)
     assert np.array_equal(se, want_se, equal_nan=True)
     assert (st[1][:20] == 0).all() and (st[1][20:] == 0).all()
+
+
+@pytest.mark.parametrize("mode", (0, 2))
+def test_selection_sort_paths_and_ties(Ctx, orc, mode):
+    """Per-gene lists of every sort size class (one entry per thread up to
+    1,024 entries, 2, 4 and 8 per thread, and the global-memory network above
+    8,192) with exact error ties (duplicated particles), ordered by (err, index)."""
+    data, se, stats = _problem(30000, 3, 8, 21)
+    stats[1::3] = stats[0::3][: stats[1::3].shape[0]]      # every third particle repeated
+    stats[7::50] = np.nan
+    with Ctx(make_config("hour"), None) as ctx:
+        ctx.set_distance_mode(mode)
+        for q in (0.0005, 0.01, 0.05, 0.1, 0.2, 0.4, 1.0):
+            _check(ctx, orc, data, se, stats, 1, q)
