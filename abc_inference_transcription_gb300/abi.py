@@ -175,6 +175,7 @@ def _declare(lib: C.CDLL) -> None:
         "abc_surrogate_destroy": (C.c_int, [sp]),
         "abc_surrogate_last_error": (C.c_char_p, [sp]),
         "abc_surrogate_num_params": (C.c_int, [sp]),
+        "abc_surrogate_set_screen_mode": (C.c_int, [sp, C.c_int]),
         "abc_surrogate_train": (C.c_int, [sp, dp, dp, i64, C.c_int, C.c_int, C.c_double, dp]),
         "abc_surrogate_gradients": (C.c_int, [sp, dp, dp, i64, dp, C.POINTER(C.c_float)]),
         "abc_surrogate_get_params": (C.c_int, [sp, C.POINTER(C.c_float)]),
@@ -206,5 +207,5 @@ ABI_SYMBOLS = [
     "abc_surrogate_create", "abc_surrogate_destroy", "abc_surrogate_last_error", "abc_surrogate_num_params",
     "abc_surrogate_train", "abc_surrogate_gradients", "abc_surrogate_get_params", "abc_surrogate_set_params",
     "abc_surrogate_get_norm", "abc_surrogate_set_norm", "abc_surrogate_predict", "abc_surrogate_predict_device",
-    "abc_surrogate_screen_device", "abc_surrogate_compact_device",
+    "abc_surrogate_screen_device", "abc_surrogate_compact_device", "abc_surrogate_set_screen_mode",
 ]

@@ -301,12 +301,19 @@ cudaError_t launch_refine(const Cand* cand, const float* cand_e, int64_t n, int6
 }
 
 
-// Surrogate screen: a lower confidence bound of the error of particle p for
-// gene g under the predicted statistics (mean mu_pk, predictive std sd_pk):
-//   L_pg = sum_k w_gk max(0, |d_gk - mu_pk| - z sd_pk)^2 / K,
-// keep[p] = 1 when L_pg <= X[g] for some gene (X = calibrated threshold).
-// A draw is dropped only when it is confidently far from every gene.  Same
+// Surrogate screen of particle p against gene g under the predicted
+// statistics (mean mu_pk, predictive std sd_pk), a = sqrt(w_gk):
+//   mode 0, per-statistic lower bound
+//     L_pg = sum_k max(0, |a (d_gk - mu_pk)| - z a sd_pk)^2 / K;
+//   mode 1, lower quantile of the error's predictive distribution: with
+//     s_pk ~ N(mu_pk, sd_pk^2) independent, err = sum_k a^2 (d - s)^2 / K has
+//     mean m = sum_k (delta^2 + sig^2) / K and variance
+//     v = sum_k (2 sig^4 + 4 sig^2 delta^2) / K^2 (delta = a (d - mu),
+//     sig = a sd), and L_pg = m - z sqrt(v).
+// keep[p] = 1 when L_pg <= X[g] for some gene (X = calibrated threshold).  A
+// draw is dropped only when it is confidently far from every gene.  Same
 // 128 x 128 tiling as dist_fast_kernel.
+template <int MODE>
 __global__ void __launch_bounds__(256) dist_screen_kernel(const float* __restrict__ mu,
                                                           const float* __restrict__ var,
                                                           const float* __restrict__ sw,
@@ -317,14 +324,19 @@ __global__ void __launch_bounds__(256) dist_screen_kernel(const float* __restric
   __shared__ float sv[kDistKc][kDistTile];
   __shared__ float sa[kDistKc][kDistTile];
   __shared__ float sd[kDistKc][kDistTile];
+  constexpr int N2 = MODE ? 8 : 1;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const int64_t g0 = (int64_t)blockIdx.x * kDistTile;
   const int64_t p0 = (int64_t)blockIdx.y * kDistTile;
-  float acc[8][8];
+  float acc[8][8], acc2[N2][N2];
 #pragma unroll
   for (int i = 0; i < 8; ++i)
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+#pragma unroll
+  for (int i = 0; i < N2; ++i)
+#pragma unroll
+    for (int j = 0; j < N2; ++j) acc2[i][j] = 0.0f;
   for (int k0 = 0; k0 < K; k0 += kDistKc) {
     for (int idx = threadIdx.x; idx < kDistKc * kDistTile; idx += 256) {
       const int r = idx / kDistKc, kk = idx - (idx / kDistKc) * kDistKc;
@@ -333,7 +345,8 @@ __global__ void __launch_bounds__(256) dist_screen_kernel(const float* __restric
       float m = 0.0f, v = 0.0f, a = 0.0f, d = 0.0f;
       if (p < P && k < K) {
         m = mu[p * K + k];
-        v = z * sqrtf(fmaxf(var[p * K + k], 0.0f));  // z x predictive std
+        v = sqrtf(fmaxf(var[p * K + k], 0.0f));  // predictive std
+        if (MODE == 0) v *= z;
       }
       if (g < G && k < K) {
         a = sw[g * K + k];
@@ -363,8 +376,16 @@ __global__ void __launch_bounds__(256) dist_screen_kernel(const float* __restric
       for (int i = 0; i < 8; ++i)
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-          const float t = fmaxf(fabsf(fmaf(-a[j], m[i], d[j])) - a[j] * v[i], 0.0f);
-          acc[i][j] = fmaf(t, t, acc[i][j]);
+          if (MODE == 0) {
+            const float t = fmaxf(fabsf(fmaf(-a[j], m[i], d[j])) - a[j] * v[i], 0.0f);
+            acc[i][j] = fmaf(t, t, acc[i][j]);
+          } else {
+            const float dl = fmaf(-a[j], m[i], d[j]);
+            const float sg = a[j] * v[i];
+            const float s2 = sg * sg, d2 = dl * dl;
+            acc[i][j] += d2 + s2;
+            acc2[i & (N2 - 1)][j & (N2 - 1)] = fmaf(s2, fmaf(4.0f, d2, 2.0f * s2), acc2[i & (N2 - 1)][j & (N2 - 1)]);
+          }
         }
     }
     __syncthreads();
@@ -379,7 +400,9 @@ __global__ void __launch_bounds__(256) dist_screen_kernel(const float* __restric
     for (int j = 0; j < 8; ++j) {
       const int64_t g = g0 + tx + 16 * j;
       if (g >= G) continue;
-      const float e = acc[i][j] * invK;  // not clipped: far draws keep large expected errors
+      // not clipped: far draws keep large predicted errors
+      float e = acc[i][j] * invK;
+      if (MODE == 1) e -= z * sqrtf(acc2[i & (N2 - 1)][j & (N2 - 1)]) * invK;
       if (err_out) err_out[p * G + g] = e;
       any = any || (e <= X[g]);
     }
@@ -388,11 +411,14 @@ __global__ void __launch_bounds__(256) dist_screen_kernel(const float* __restric
 }
 
 cudaError_t launch_dist_screen(const float* mu, const float* var, const float* sw, const float* dw, int64_t P,
-                               int64_t G, int K, const float* X, float z, uint8_t* keep, float* err_out,
+                               int64_t G, int K, const float* X, float z, int mode, uint8_t* keep, float* err_out,
                                cudaStream_t s) {
   if (P <= 0 || G <= 0) return cudaSuccess;
   dim3 grid((unsigned)((G + kDistTile - 1) / kDistTile), (unsigned)((P + kDistTile - 1) / kDistTile));
-  dist_screen_kernel<<<grid, 256, 0, s>>>(mu, var, sw, dw, P, G, K, X, z, keep, err_out);
+  if (mode == 1)
+    dist_screen_kernel<1><<<grid, 256, 0, s>>>(mu, var, sw, dw, P, G, K, X, z, keep, err_out);
+  else
+    dist_screen_kernel<0><<<grid, 256, 0, s>>>(mu, var, sw, dw, P, G, K, X, z, keep, err_out);
   return cudaGetLastError();
 }
 

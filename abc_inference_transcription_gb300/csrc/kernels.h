@@ -193,9 +193,11 @@ cudaError_t launch_ssa_fp64(const SsaArgs& a, int grid, cudaStream_t s);
 constexpr int kSsaVariants = 2;
 cudaError_t launch_ssa_fp32(const SsaArgs& a, int grid, cudaStream_t s, int variant = 0);
 cudaError_t launch_stats(const StatsArgs& a, cudaStream_t s);
-// surrogate screen: keep[p] = 1 if sum_k w max(0, |d - mu| - z sqrt(var))^2 / K <= X[g] for some g
+// surrogate screen: keep[p] = 1 if L_pg <= X[g] for some g; mode 0:
+// L = sum_k w max(0, |d - mu| - z sqrt(var))^2 / K, mode 1: L = m - z sqrt(v)
+// with m, v the mean and variance of the error under s ~ N(mu, var)
 cudaError_t launch_dist_screen(const float* mu, const float* var, const float* sw, const float* dw, int64_t P,
-                               int64_t G, int K, const float* X, float z, uint8_t* keep, float* err_out,
+                               int64_t G, int K, const float* X, float z, int mode, uint8_t* keep, float* err_out,
                                cudaStream_t s);
 
 // particles ordered by expected trajectory cost, descending (hist128: 128 scratch words)

@@ -259,6 +259,7 @@ struct abc_surrogate {
   std::string err;
   int step = 0;
   bool normed = false;
+  int screen_mode = 0;           // 0: per-statistic lower bound, 1: error-distribution lower quantile
   Buf<float> P, G, Am, Av, ymf, ysf, yscf;  // yscf: asinh scale per statistic (0: identity)
   Buf<__nv_bfloat16> Ph, PhT;   // BF16 weights as stored and transposed
   Buf<int> tcerr;                // tensor-core GEMM error word
@@ -396,6 +397,13 @@ int abc_surrogate_destroy(abc_surrogate* s) {
 const char* abc_surrogate_last_error(const abc_surrogate* s) { return s ? s->err.c_str() : "null surrogate"; }
 
 int abc_surrogate_num_params(const abc_surrogate* s) { return s ? (int)s->d.n_params : ABC_ERR_INVALID; }
+
+int abc_surrogate_set_screen_mode(abc_surrogate* s, int mode) {
+  if (!s) return ABC_ERR_INVALID;
+  if (mode != 0 && mode != 1) return sfail(s, ABC_ERR_INVALID, "screen mode must be 0 or 1");
+  s->screen_mode = mode;
+  return ABC_OK;
+}
 
 // load host data and standardise it (normalisation constants from this data
 // when `fit_norm`, else the stored ones)
@@ -641,7 +649,7 @@ int abc_surrogate_screen_device(abc_surrogate* s, const double* d_theta, int ld_
     if (st) return st;
     d2f_kernel<<<blocks(n * K), 256, 0, s->stream>>>(s->pm.p, s->pmf.p, n * K);
     d2f_kernel<<<blocks(n * K), 256, 0, s->stream>>>(s->pv.p, s->pvf.p, n * K);
-    SK(launch_dist_screen(s->pmf.p, s->pvf.p, s->sw.p, s->dw.p, n, G, K, s->X.p, (float)z, d_keep + p0,
+    SK(launch_dist_screen(s->pmf.p, s->pvf.p, s->sw.p, s->dw.p, n, G, K, s->X.p, (float)z, s->screen_mode, d_keep + p0,
                           err_out ? eo.p + p0 * G : nullptr, s->stream));
     disagree_keep_kernel<<<blocks(n), 256, 0, s->stream>>>(s->pd.p, n, disagree_max, d_keep + p0);
     SK(cudaGetLastError());

@@ -91,7 +91,12 @@ def thresholds_from_lists(off: np.ndarray, err: np.ndarray) -> np.ndarray:
     return thr
 
 
-def _screened(ctx, sg, data, se, thr, factor, dmax, per_model_s, prior, seed, offset, z=2.0):
+def _screen_x(thr: np.ndarray, factor: float) -> np.ndarray:
+    """Screen thresholds f thr_g; genes without a threshold (thr < 0) keep no draw."""
+    return np.where(thr >= 0, thr * factor, -1e30)
+
+
+def _screened(ctx, sg, data, se, thr, factor, dmax, per_model_s, prior, seed, offset, z=2.0, mode=0):
     """Screened ABC: draw, screen, compact, simulate the survivors, accept with
     the per-gene thresholds.  Returns (accepted pairs, simulated draws, times)."""
     torch = _torch()
@@ -99,8 +104,8 @@ def _screened(ctx, sg, data, se, thr, factor, dmax, per_model_s, prior, seed, of
     th_s, m_s = draw(ctx, per_model_s, seed, prior, offset=offset)
     x_s = surrogate_input(th_s, m_s)
     keep = torch.zeros(th_s.shape[0], dtype=torch.uint8, device="cuda")
-    n_keep = sg.screen_device(x_s.data_ptr(), IN_DIM, th_s.shape[0], data, se, thr * factor, 0.0, dmax,
-                              keep.data_ptr(), z=z)
+    n_keep = sg.screen_device(x_s.data_ptr(), IN_DIM, th_s.shape[0], data, se, _screen_x(thr, factor), 0.0, dmax,
+                              keep.data_ptr(), z=z, mode=mode)
     sidx = torch.empty(max(n_keep, 1), dtype=torch.int64, device="cuda")
     sg.compact_device(keep.data_ptr(), 0, LD, th_s.shape[0], 0, sidx.data_ptr())
     sel = sidx[:n_keep]
@@ -110,23 +115,71 @@ def _screened(ctx, sg, data, se, thr, factor, dmax, per_model_s, prior, seed, of
     st_k = simulate(ctx, th_k, m_k, seed + 7, offset=offset)
     t_sim = time.perf_counter() - t0 - t_screen
     acc = 0
+    off_k = idx_k = None
     if n_keep:
-        off_k, _, _ = ctx.select_device(data, se, st_k.data_ptr(), n_keep, 2, thr=thr)
+        off_k, idx_k, _ = ctx.select_device(data, se, st_k.data_ptr(), n_keep, 2, thr=thr)
         acc = int(off_k[-1])
     torch.cuda.synchronize()
-    return acc, int(n_keep), int(th_s.shape[0]), time.perf_counter() - t0, t_screen, t_sim
+    t_all = time.perf_counter() - t0
+    lists = None
+    if n_keep:
+        lists = (off_k, idx_k, th_k.cpu().numpy(), m_k.cpu().numpy())
+    return acc, int(n_keep), int(th_s.shape[0]), t_all, t_screen, t_sim, lists
+
+
+def shared_rates(theta: np.ndarray, models: np.ndarray) -> np.ndarray:
+    """log10 (k_on, k_off, alpha, gamma, lambda) of draws of any of the five
+    models; a rate that varies over the age steps (k_on for model 3, alpha for
+    4, gamma for 5) is represented by the mean of its per-step log values."""
+    out = np.empty((theta.shape[0], 5))
+    for m in range(1, 6):
+        r = models == m
+        t = theta[r]
+        if m <= 2:
+            out[r] = t[:, :5]
+        elif m == 3:
+            out[r] = np.column_stack([t[:, 0:5].mean(1), t[:, 5], t[:, 6], t[:, 7], t[:, 8]])
+        elif m == 4:
+            out[r] = np.column_stack([t[:, 0], t[:, 1], t[:, 2:7].mean(1), t[:, 7], t[:, 8]])
+        else:
+            out[r] = np.column_stack([t[:, 0], t[:, 1], t[:, 2], t[:, 3:8].mean(1), t[:, 8]])
+    return out
+
+
+def posterior_agreement(plain: list, screened: list, min_n: int = 10) -> dict:
+    """Per gene and shared rate, z = (mean_screened - mean_plain) /
+    sqrt(var_plain / n_plain + var_screened / n_screened) over the accepted
+    particles of the two runs (genes with at least min_n accepted in both)."""
+    zs = []
+    for a, b in zip(plain, screened):
+        if a.shape[0] < min_n or b.shape[0] < min_n:
+            continue
+        se = np.sqrt(a.var(0, ddof=1) / a.shape[0] + b.var(0, ddof=1) / b.shape[0])
+        zs.append((b.mean(0) - a.mean(0)) / np.where(se > 0, se, np.inf))
+    if not zs:
+        return {"genes_compared": 0}
+    z = np.abs(np.concatenate(zs))
+    return {"genes_compared": len(zs), "abs_z_median": float(np.median(z)), "abs_z_max": float(z.max()),
+            "fraction_abs_z_above_3": float((z > 3).mean())}
 
 
 def run(genes=(2000,), per_model_train: int = 20000, per_model_plain: int = 2000, screen_factor: int = 10,
-        q: float = 0.001, seed: int = 1, epochs: int = 40, ensemble: int = 4, cells=None, z: float = 2.0) -> dict:
+        q: float = 0.001, seed: int = 1, epochs: int = 40, ensemble: int = 4, cells=None, z: float = 2.0,
+        screens=((0, 1.0), (0, 2.0)), recall: float = 0.995,
+        disagree_q: float = 0.99) -> dict:
     """Plain vs screened ABC on the five-model batch for each gene-set size in
-    `genes` (one surrogate, trained once on the pipeline's own simulations)."""
+    `genes` (one surrogate, trained once on the pipeline's own simulations).
+    `screens`: candidate screen statistics (mode, z), chosen per gene set on a
+    calibration half of the plain draws; `recall`: fraction of the calibration
+    half's accepted pairs the screen must keep; draws whose ensemble
+    disagreement exceeds its `disagree_q` quantile are always simulated."""
     torch = _torch()
     cfg = make_config("hour")
     cells = cells if cells is not None else synthetic_cells(seed=1)
     prior = factor_prior()
     rng = np.random.default_rng(seed)
-    out = {"q": q, "screen_factor": screen_factor, "z": z, "runs": []}
+    out = {"q": q, "screen_factor": screen_factor, "recall_target": recall, "disagree_quantile": disagree_q,
+           "runs": []}
     with Context(cfg, cells) as ctx:
         ctx.autotune(1, ctx.sample_prior(1, 500, seed + 99, prior)[:, :5], seed=3)
         # ---- training data: exact simulations the pipeline generates itself
@@ -149,6 +202,7 @@ def run(genes=(2000,), per_model_train: int = 20000, per_model_plain: int = 2000
         st_p = simulate(ctx, th_p, m_p, seed + 2, offset=off_plain)
         t_sim_plain = time.perf_counter() - t0
         st_host = st_p.cpu().numpy()
+        th_host, m_host = th_p.cpu().numpy(), m_p.cpu().numpy()
         Pp = th_p.shape[0]
         x_p = surrogate_input(th_p, m_p)
         rows = rng.permutation(Pp)
@@ -156,7 +210,7 @@ def run(genes=(2000,), per_model_train: int = 20000, per_model_plain: int = 2000
         x_cal = x_p[torch.from_numpy(cal).cuda()].contiguous()
         x_hold = x_p[torch.from_numpy(hold).cuda()].contiguous()
         _, _, dis = sg.predict(x_cal.cpu().numpy())
-        dmax = float(np.quantile(dis, 0.99))
+        dmax = float(np.quantile(dis, disagree_q))
         for gi, G in enumerate(genes):
             res = {"genes": G}
             data, se = make_genes(st_host, G, rng)
@@ -172,39 +226,77 @@ def run(genes=(2000,), per_model_train: int = 20000, per_model_plain: int = 2000
             res["informative_genes"] = int((thr >= 0).sum())
             res["plain"] = {"draws": int(Pp), "accepted_pairs": acc_plain, "seconds": t_plain,
                             "accepted_per_s": acc_plain / t_plain}
-            # calibration half: multiplicative factor at the 99th percentile of
-            # pred/thr over truly accepted pairs; held-out half: false rejection
-            keep_cal = torch.zeros(cal.shape[0], dtype=torch.uint8, device="cuda")
-            pred = np.zeros((cal.shape[0], G))
-            sg.screen_device(x_cal.data_ptr(), IN_DIM, cal.shape[0], data, se, thr, 0.0, 1e30, keep_cal.data_ptr(),
-                             err_out=pred, z=z)
+            # calibration half: for each screen statistic (mode, z) the factor f
+            # such that a fraction `recall` of the truly accepted pairs pass
+            # (bound <= f thr), and the fraction of calibration draws it keeps;
+            # the statistic keeping the fewest draws is used, and the held-out
+            # half measures the false-rejection rate
             pos = np.full(Pp, -1, np.int64)
             pos[cal] = np.arange(cal.shape[0])
             in_cal = pos[p_of] >= 0
-            ratios = pred[pos[p_of[in_cal]], gene_of[in_cal]] / np.maximum(thr[gene_of[in_cal]], 1e-12)
-            ratios = np.where(np.isfinite(ratios), ratios, np.inf)
-            # the 99th percentile of bound / threshold over truly accepted pairs; below 1
-            # when the bound is conservative (the screen then tightens)
-            factor = float(max(0.05, np.quantile(ratios, 0.99))) if ratios.size else 1.0
+            informative = thr >= 0
+            keep_cal = torch.zeros(cal.shape[0], dtype=torch.uint8, device="cuda")
+            dis_keep = dis > dmax
+            best = None
+            tried = []
+            for mode, zz in screens:
+                pred = np.zeros((cal.shape[0], G))
+                sg.screen_device(x_cal.data_ptr(), IN_DIM, cal.shape[0], data, se, thr, 0.0, 1e30,
+                                 keep_cal.data_ptr(), err_out=pred, z=zz, mode=mode)
+                ratios = pred[pos[p_of[in_cal]], gene_of[in_cal]] / np.maximum(thr[gene_of[in_cal]], 1e-12)
+                ratios = np.where(np.isfinite(ratios), ratios, np.inf)
+                if not ratios.size:
+                    continue
+                f = float(np.quantile(ratios, recall))
+                if mode == 0:
+                    f = max(0.05, f)
+                kept_c = ((pred <= _screen_x(thr, f)[None, :]).any(axis=1) | dis_keep).mean()
+                tried.append({"mode": mode, "z": zz, "factor": f, "kept_fraction": float(kept_c)})
+                if best is None or kept_c < best[0]:
+                    best = (float(kept_c), mode, zz, f)
+            if best is None:
+                best = (1.0, 0, z, 1.0)
+            _, mode, zz, factor = best
             keep_h = torch.zeros(hold.shape[0], dtype=torch.uint8, device="cuda")
-            sg.screen_device(x_hold.data_ptr(), IN_DIM, hold.shape[0], data, se, thr * factor, 0.0, dmax,
-                             keep_h.data_ptr(), z=z)
+            sg.screen_device(x_hold.data_ptr(), IN_DIM, hold.shape[0], data, se, _screen_x(thr, factor), 0.0, dmax,
+                             keep_h.data_ptr(), z=zz, mode=mode)
             kept = np.zeros(Pp, bool)
             kept[hold] = keep_h.cpu().numpy().astype(bool)
             n_hold = int((~in_cal).sum())
             frr = float((~kept[p_of[~in_cal]]).sum() / max(n_hold, 1))
-            res["calibration"] = {"factor": factor, "disagree_max": dmax, "calibration_pairs": int(in_cal.sum()),
+            res["calibration"] = {"screen_mode": mode, "z": zz, "factor": factor,
+                                  "calibration_kept_fraction": best[0], "recall_target": recall,
+                                  "candidates": tried,
+                                  "disagree_max": dmax, "calibration_pairs": int(in_cal.sum()),
                                   "held_out_pairs": n_hold, "false_rejection_rate": frr}
             # warm-up of the whole screened path, then the timed run
-            _screened(ctx, sg, data, se, thr, factor, dmax, 64, prior, seed * 1000 + 40 + gi, 10 ** 8, z)
-            acc, n_sim, n_draw, t_all, t_scr, t_sim = _screened(
+            _screened(ctx, sg, data, se, thr, factor, dmax, 64, prior, seed * 1000 + 40 + gi, 10 ** 8, zz, mode)
+            acc, n_sim, n_draw, t_all, t_scr, t_sim, lists = _screened(
                 ctx, sg, data, se, thr, factor, dmax, per_model_plain * screen_factor, prior,
-                seed * 1000 + 30 + gi, off_plain + Pp + gi * 5 * per_model_plain * screen_factor, z)
+                seed * 1000 + 30 + gi, off_plain + Pp + gi * 5 * per_model_plain * screen_factor, zz, mode)
             res["screened"] = {"draws": n_draw, "simulated": n_sim, "simulated_fraction": n_sim / n_draw,
                                "accepted_pairs": acc, "seconds": t_all, "screen_seconds": t_scr,
                                "ssa_seconds": t_sim, "accepted_per_s": acc / t_all}
             res["gain_accepted_per_s"] = res["screened"]["accepted_per_s"] / max(res["plain"]["accepted_per_s"],
                                                                                   1e-30)
+            # posterior means of the shared rates per gene, plain vs screened
+            rates_p = shared_rates(th_host, m_host)
+            post_p = [rates_p[p_of[gene_of == g]] for g in range(G)]
+            post_s = [np.zeros((0, 5))] * G
+            if lists is not None:
+                off_k, idx_k, th_k, m_k = lists
+                rates_k = shared_rates(th_k, m_k)
+                post_s = [rates_k[idx_k[off_k[g]:off_k[g + 1]] - 1] for g in range(G)]
+            res["posterior_agreement"] = posterior_agreement(post_p, post_s)
+            res["_lost_held"] = (int((~kept[p_of[~in_cal]]).sum()), n_hold)
             out["runs"].append(res)
         sg.close()
+    # over the gene sets: median gain, false rejections pooled over held-out pairs
+    lost = sum(r["_lost_held"][0] for r in out["runs"])
+    held = sum(r["_lost_held"][1] for r in out["runs"])
+    for r in out["runs"]:
+        del r["_lost_held"]
+    out["summary"] = {"gene_sets": len(out["runs"]),
+                      "median_gain_accepted_per_s": float(np.median([r["gain_accepted_per_s"] for r in out["runs"]])),
+                      "pooled_false_rejection_rate": lost / max(held, 1), "pooled_held_out_pairs": held}
     return out

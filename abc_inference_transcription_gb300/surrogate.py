@@ -98,7 +98,10 @@ class Surrogate:
         return mean, var, dis
 
     def screen_device(self, d_theta: int, ld: int, n: int, data, se, thr, margin: float, disagree_max: float,
-                      d_keep: int, err_out: np.ndarray | None = None, z: float = 2.0) -> int:
+                      d_keep: int, err_out: np.ndarray | None = None, z: float = 2.0, mode: int = 0) -> int:
+        """mode 0: per-statistic lower bound; mode 1: lower z-quantile (normal
+        approximation) of the error's predictive distribution."""
+        self._check(self.lib.abc_surrogate_set_screen_mode(self.h, int(mode)))
         d = np.ascontiguousarray(data, np.float64)
         e = np.ascontiguousarray(se, np.float64)
         t = np.ascontiguousarray(thr, np.float64)

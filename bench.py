@@ -579,9 +579,11 @@ def main():
             line["abc_screened"] = pipeline.run(genes=(8, 50, args.genes), per_model_train=20000,
                                                 per_model_plain=2000, screen_factor=10, q=0.01, seed=1, epochs=40)
             # a few genes at a small quantile: the regime where the screen can
-            # drop most draws (top 0.2 % of 5 x 10^4 plain draws, 4 genes)
-            line["abc_screened_small_q"] = pipeline.run(genes=(4,), per_model_train=40000, per_model_plain=10000,
-                                                        screen_factor=10, q=0.002, seed=2, epochs=40)
+            # drop most draws (top 0.2 % of 10^5 plain draws; four independent
+            # sets of 4 genes, one surrogate)
+            line["abc_screened_small_q"] = pipeline.run(genes=(4, 4, 4, 4), per_model_train=40000,
+                                                        per_model_plain=20000, screen_factor=10, q=0.002, seed=2,
+                                                        epochs=40)
         except Exception as exc:
             line["abc_screened"] = {"error": repr(exc)}
     print(json.dumps(line))

@@ -357,6 +357,12 @@ int abc_surrogate_screen_device(abc_surrogate* s, const double* d_theta, int ld_
                                 const double* data, const double* se, int64_t n_genes, const double* thr,
                                 double margin, double z, double disagree_max, uint8_t* d_keep, int64_t* n_keep,
                                 double* err_out);
+/* Statistic of abc_surrogate_screen_device.  0 (default): per-statistic lower
+ * bound L = sum_k w_k max(0, |d_k - mu_k| - z sd_k)^2 / K.  1: lower quantile of
+ * the error's predictive distribution, L = m - z sqrt(v), where m and v are
+ * the mean and variance of sum_k w_k (d_k - s_k)^2 / K for independent
+ * s_k ~ N(mu_k, sd_k^2).  No reference counterpart. */
+int abc_surrogate_set_screen_mode(abc_surrogate* s, int mode);
 /* Survivors of a screen in ascending order: rows with d_keep != 0 copied from
  * d_theta (row stride ld_theta) to d_theta_out and their indices to d_idx_out
  * (either output may be NULL); *n_out = number of survivors. */

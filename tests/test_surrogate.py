@@ -111,12 +111,64 @@ def test_screen_gain_at_calibrated_false_rejection(mods):
         n_keep = sg.screen_device(d_th[half:].data_ptr(), 5, th_ex.shape[0] - half, data, se, thr * factor, 0.0,
                                   dmax, d_keep[half:].data_ptr())
         keep = d_keep[half:].cpu().numpy()
+        # the error-distribution statistic (mode 1), calibrated the same way
+        pred1 = np.zeros((half, G))
+        sg.screen_device(d_th.data_ptr(), 5, half, data, se, thr, 0.0, 1e30, d_keep.data_ptr(), err_out=pred1, z=1.0,
+                         mode=1)
+        acc1 = err[:half] <= thr[None, :]
+        factor1 = float(np.quantile((pred1 / thr[None, :])[acc1], 0.99))
+        d_keep.zero_()
+        n_keep1 = sg.screen_device(d_th[half:].data_ptr(), 5, th_ex.shape[0] - half, data, se, thr * factor1, 0.0,
+                                   dmax, d_keep[half:].data_ptr(), z=1.0, mode=1)
+        keep1 = d_keep[half:].cpu().numpy()
     frr, n_acc = S.false_rejection_rate(keep, err[half:], thr)
     frac = n_keep / (th_ex.shape[0] - half)
-    info = dict(thr=thr.round(3).tolist(), factor=factor, dmax=dmax, frr=frr, n_acc=n_acc, frac=frac)
+    frr1, _ = S.false_rejection_rate(keep1, err[half:], thr)
+    frac1 = n_keep1 / (th_ex.shape[0] - half)
+    info = dict(thr=thr.round(3).tolist(), factor=factor, dmax=dmax, frr=frr, n_acc=n_acc, frac=frac,
+                factor1=factor1, frr1=frr1, frac1=frac1)
     assert n_acc > 50, info
-    assert frr <= 0.03, info
-    assert frac < 0.5, info   # >= 2x fewer exact simulations per accepted particle
+    assert frr <= 0.03 and frr1 <= 0.03, info
+    assert frac < 0.5 and frac1 < 0.5, info   # >= 2x fewer exact simulations per accepted particle
+
+
+def test_screen_statistics_match_numpy(mods):
+    """Both screen statistics, from the GPU's FP32 kernel, against an FP64 numpy
+    restatement built from predict()'s means and variances."""
+    S, Context = mods
+    torch = pytest.importorskip("torch")
+    cfg = make_config("hour", precision=abi.FP32)
+    cells = synthetic_cells(seed=4)
+    rng = np.random.default_rng(3)
+    with Context(cfg, cells) as ctx:
+        th = ctx.sample_prior(1, 6000, 31, reference_prior())
+        st = _exact(ctx, th, 4)
+    ok = np.flatnonzero(np.isfinite(st).all(axis=1))
+    data = st[ok[:5]] * rng.lognormal(0, 0.05, (5, 53))
+    se = 0.1 * np.abs(data) * rng.lognormal(0, 0.5, data.shape)
+    thr = np.full(5, 1.0)
+    with S.Surrogate(5, 53, ensemble=4, seed=6) as sg:
+        sg.train(th[:5000], st[:5000], epochs=5, batch=1024, lr=2e-3)
+        x = th[5000:5300]
+        mean, var, _ = sg.predict(x)
+        d_th = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+        d_keep = torch.zeros(x.shape[0], dtype=torch.uint8, device="cuda")
+        w = 1.0 / ((se ** 2 + 0.01 * data ** 2) + np.where(se + data != 0, 0.0, 1e-4))
+        a = np.sqrt(w)
+        dl = a[None] * (data[None] - mean[:, None])           # n x G x K
+        sig = a[None] * np.sqrt(np.maximum(var, 0))[:, None]
+        for mode, z in ((0, 2.0), (1, 0.0), (1, 1.5)):
+            got = np.zeros((x.shape[0], 5))
+            sg.screen_device(d_th.data_ptr(), 5, x.shape[0], data, se, thr, 0.0, 1e30, d_keep.data_ptr(),
+                             err_out=got, z=z, mode=mode)
+            if mode == 0:
+                want = (np.maximum(np.abs(dl) - z * sig, 0.0) ** 2).mean(axis=2)
+            else:
+                m = (dl ** 2 + sig ** 2).mean(axis=2)
+                v = (2 * sig ** 4 + 4 * sig ** 2 * dl ** 2).sum(axis=2) / 53.0 ** 2
+                want = m - z * np.sqrt(v)
+            scale = np.abs(want) + (dl ** 2 + sig ** 2).mean(axis=2)
+            assert np.all(np.abs(got - want) <= 2e-4 * scale + 1e-6), (mode, z, np.max(np.abs(got - want) / scale))
 
 
 def test_screened_pipeline_small(mods):
