@@ -24,7 +24,8 @@ namespace {
 
 constexpr int kThreads = 256;
 
-// position in [0, n) of draw i of stream (seed, family, resample, gene)
+// position in [0, n) of draw i of stream (seed, family, resample, gene):
+// floor(x n / 2^52) of a 52-bit uniform integer x, in exact integer arithmetic
 __device__ __forceinline__ int64_t draw_pos(uint64_t seed, int fam, int b, int64_t g, int64_t i, int64_t n) {
   U4 c;
   c.x = (uint32_t)(i >> 1);
@@ -32,9 +33,9 @@ __device__ __forceinline__ int64_t draw_pos(uint64_t seed, int fam, int b, int64
   c.z = (uint32_t)b | ((uint32_t)(fam + 1) << 24);
   c.w = (uint32_t)g;
   const U4 o = philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
-  const double u = (i & 1) ? u52(o.z, o.w) : u52(o.x, o.y);
-  int64_t p = (int64_t)(u * (double)n);
-  return p < n ? p : n - 1;
+  const uint32_t hi = (i & 1) ? o.z : o.x, lo = (i & 1) ? o.w : o.y;
+  const uint64_t x = ((uint64_t)hi << 20) | (uint64_t)(lo >> 12);
+  return (int64_t)__umul64hi(x << 12, (uint64_t)n);
 }
 
 // exact sample variance / covariance from integer sums: (n sxy - sx sy) / (n (n - 1))
@@ -85,13 +86,18 @@ __global__ void __launch_bounds__(kThreads) data_stats_kernel(DataStatsArgs a) {
     atomicAdd(&S[5], uu * ll);
   }
   __syncthreads();
-  if (threadIdx.x != 0) return;
+  // The statistics of one (family, age) cell or one condition are independent
+  // FP64 computations: lanes of warp 0 take the (family, age) cells, lanes of
+  // warp 1 the conditions (GB300 issues FP64 warp instructions slowly, so one
+  // instruction stream per warp serves all of them).
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   double* st = a.out + (g * (int64_t)(a.n_boot + 1) + b) * K;
-  // mean and Fano factor of u + l per age cluster (get_mean_ccp_data, get_ff_ccp_data)
-  for (int f = 0; f < 2; ++f) {
-    const unsigned long long* S = f == 0 ? Sp : Sc;
-    const int off = f == 0 ? 0 : 2 * A;
-    for (int ag = 0; ag < A; ++ag) {
+  if (warp == 0) {
+    // mean and Fano factor of u + l per age cluster (get_mean_ccp_data, get_ff_ccp_data)
+    for (int t = lane; t < 2 * A; t += 32) {
+      const int f = t / A, ag = t - (t / A) * A;
+      const unsigned long long* S = f == 0 ? Sp : Sc;
+      const int off = f == 0 ? 0 : 2 * A;
       const unsigned long long n = S[3 * ag];
       double m = 0.0, ff = 0.0;
       if (n > 0) {
@@ -103,8 +109,10 @@ __global__ void __launch_bounds__(kThreads) data_stats_kernel(DataStatsArgs a) {
       st[off + ag] = m;
       st[off + A + ag] = ff;
     }
+    return;
   }
-  for (int j = 0; j < J; ++j) {
+  if (warp != 1) return;
+  for (int j = lane; j < J; j += 32) {
     double m1[kMaxAges], m2[kMaxAges], v1[kMaxAges], v2[kMaxAges], c12[kMaxAges], w[kMaxAges];
     unsigned long long nj = 0, suj = 0, slj = 0;
     for (int ag = 0; ag < A; ++ag) {

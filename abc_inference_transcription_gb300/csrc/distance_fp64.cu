@@ -5,6 +5,7 @@
 // (scripts/accepted_particles.jl:20-26: findall + sortperm).
 #include <algorithm>
 
+#include "bitonic.cuh"
 #include "distance.cuh"
 #include "kernels.h"
 
@@ -251,17 +252,13 @@ __global__ void scatter_kernel(const Cand* cand, int64_t n, const int64_t* goff,
   }
 }
 
-// Per-gene sort by (err, p): bitonic network in its all-ascending form (the
-// first step of every merge pairs i with i ^ (k - 1)).  NaN sorts last, ties by
-// index.  Segments up to kSortSmem entries are padded to a power of two n2 and
-// held in registers, EPT = n2 / 1024 consecutive entries per thread (at least
-// one, 32 threads at least); steps whose partner lies in the same thread run on
-// registers, steps whose partner lies in the same warp on shuffles, and only
-// the steps across warps (partner distance >= 32 EPT) go through shared memory.
-// Keys are the bit patterns of the errors (monotone for non-negative doubles;
-// NaN canonicalised to one pattern), compared with the index as tie-break;
-// padding slots carry (all ones, INT32_MAX), above every real entry.
-// Longer segments run the same network in global memory.
+// Per-gene sort by (err, p), NaN last, ties by index.  Segments up to
+// kSortSmem entries run the register-resident bitonic network of bitonic.cuh
+// (EPT = n2 / 1024 entries per thread, n2 the padded power of two) on keys
+// that are the bit patterns of the errors (monotone for the non-negative
+// errors; NaN canonicalised to one pattern) with the index as tie-break;
+// padding slots carry (all ones, INT32_MAX), above every real entry.  Longer
+// segments run the same network on (err, p) in global memory.
 __device__ __forceinline__ bool key_less(double ea, int32_t pa, double eb, int32_t pb) {
   const bool na = ea != ea, nb = eb != eb;
   if (na != nb) return nb;
@@ -278,52 +275,6 @@ __device__ __forceinline__ uint64_t err_key(double e) {
   return (uint64_t)__double_as_longlong(e);
 }
 
-// (ka, pa) receives the smaller entry
-__device__ __forceinline__ void cas_lo(uint64_t& ka, int32_t& pa, uint64_t& kb, int32_t& pb) {
-  const bool sw = kb < ka || (kb == ka && pb < pa);
-  const uint64_t tk = sw ? kb : ka;
-  const int32_t tp = sw ? pb : pa;
-  kb = sw ? ka : kb;
-  pb = sw ? pa : pb;
-  ka = tk;
-  pa = tp;
-}
-
-// own entry becomes min (lower) or max of (own, other)
-__device__ __forceinline__ void keep(uint64_t& k, int32_t& p, uint64_t ok, int32_t op, bool lower) {
-  const bool other_less = ok < k || (ok == k && op < p);
-  const bool take = lower ? other_less : !other_less;
-  k = take ? ok : k;
-  p = take ? op : p;
-}
-
-template <int EPT, int J, bool FLIP>
-__device__ __forceinline__ void step_in_thread(uint64_t* key, int32_t* pp) {
-#pragma unroll
-  for (int e = 0; e < EPT; ++e) {
-    const int f = FLIP ? (e ^ (2 * J - 1)) : (e ^ J);
-    if (f > e) cas_lo(key[e], pp[e], key[f], pp[f]);
-  }
-}
-
-template <int EPT>
-__device__ __forceinline__ void in_thread(uint64_t* key, int32_t* pp, int j, bool flip) {
-  if (EPT >= 2 && j == 1) {
-    if (flip) step_in_thread<EPT, 1, true>(key, pp); else step_in_thread<EPT, 1, false>(key, pp);
-  } else if (EPT >= 4 && j == 2) {
-    if (flip) step_in_thread<EPT, 2, true>(key, pp); else step_in_thread<EPT, 2, false>(key, pp);
-  } else if (EPT >= 8 && j == 4) {
-    if (flip) step_in_thread<EPT, 4, true>(key, pp); else step_in_thread<EPT, 4, false>(key, pp);
-  }
-}
-
-__device__ __forceinline__ void shfl_entry(uint64_t k, int32_t p, int mask, uint64_t& ok, int32_t& op) {
-  const unsigned lo = __shfl_xor_sync(0xffffffffu, (unsigned)k, mask);
-  const unsigned hi = __shfl_xor_sync(0xffffffffu, (unsigned)(k >> 32), mask);
-  op = __shfl_xor_sync(0xffffffffu, p, mask);
-  ok = ((uint64_t)hi << 32) | lo;
-}
-
 template <int EPT>
 __device__ void sort_segment_regs(int32_t* P, double* E, int m, int n2, uint64_t* sK, int32_t* sP) {
   const int t = threadIdx.x;
@@ -338,63 +289,7 @@ __device__ void sort_segment_regs(int32_t* P, double* E, int m, int n2, uint64_t
     key[e] = real ? err_key(E[i]) : ~0ull;
     pp[e] = real ? P[i] : 0x7fffffff;
   }
-  for (int k = 2; k <= n2; k <<= 1) {
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      const bool flip = j == (k >> 1);
-      if (j < EPT) {
-        in_thread<EPT>(key, pp, j, flip);
-      } else if (j < 32 * EPT) {
-        if (act) {
-          if (!flip) {
-            const int mask = j / EPT;
-            const bool lower = (t & mask) == 0;
-#pragma unroll
-            for (int e = 0; e < EPT; ++e) {
-              uint64_t ok;
-              int32_t op;
-              shfl_entry(key[e], pp[e], mask, ok, op);
-              keep(key[e], pp[e], ok, op, lower);
-            }
-          } else {
-            // entry e pairs with the partner's entry EPT - 1 - e
-            const int mask = k / EPT - 1;
-            const bool lower = (t & ((mask + 1) >> 1)) == 0;
-#pragma unroll
-            for (int e = 0; e < (EPT + 1) / 2; ++e) {
-              const int f = EPT - 1 - e;
-              uint64_t o1, o2;
-              int32_t q1, q2;
-              shfl_entry(key[f], pp[f], mask, o1, q1);
-              if (f != e) shfl_entry(key[e], pp[e], mask, o2, q2);
-              keep(key[e], pp[e], o1, q1, lower);
-              if (f != e) keep(key[f], pp[f], o2, q2, lower);
-            }
-          }
-        }
-      } else {
-        // across warps: entry (t, e) in slot e * nt + t
-        if (act) {
-#pragma unroll
-          for (int e = 0; e < EPT; ++e) {
-            sK[e * nt + t] = key[e];
-            sP[e * nt + t] = pp[e];
-          }
-        }
-        __syncthreads();
-        if (act) {
-          const int mask = flip ? k / EPT - 1 : j / EPT;
-          const bool lower = (t & (flip ? (mask + 1) >> 1 : mask)) == 0;
-          const int tp = t ^ mask;
-#pragma unroll
-          for (int e = 0; e < EPT; ++e) {
-            const int f = flip ? EPT - 1 - e : e;
-            keep(key[e], pp[e], sK[f * nt + tp], sP[f * nt + tp], lower);
-          }
-        }
-        __syncthreads();
-      }
-    }
-  }
+  bitonic_regs<EPT>(key, pp, n2, sK, sP);
 #pragma unroll
   for (int e = 0; e < EPT; ++e) {
     const int i = t * EPT + e;

@@ -5,6 +5,7 @@
 // FP64, built with -fmad=false: results are bit-identical to the C oracle.
 #include <cuda_runtime.h>
 
+#include "bitonic.cuh"
 #include "common.cuh"
 #include "kernels.h"
 
@@ -116,13 +117,44 @@ __global__ void post_gather_kernel(const int64_t* aoff, const int64_t* idx, cons
   }
 }
 
-constexpr int kPostSmem = 8192;  // segments up to this size sort in shared memory
+constexpr int kPostSmem = 8192;  // segments up to this size sort in registers
 
-// Sort of one (gene, column) segment of doubles, ascending (bitonic network in
-// its all-ascending form; padding slots never take part in an exchange).
-__global__ void __launch_bounds__(1024) post_sort_kernel(const int64_t* aoff, int64_t total, int64_t G,
-                                                         double* scratch) {
-  extern __shared__ double post_smem[];
+// order-preserving 64-bit keys of doubles (negative values reversed)
+__device__ __forceinline__ uint64_t dkey(double x) {
+  const uint64_t b = (uint64_t)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double dkey_inv(uint64_t k) {
+  const uint64_t b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double((long long)b);
+}
+
+template <int EPT>
+__device__ void post_sort_regs(double* v, int m, int n2, uint64_t* sK, int32_t* sP) {
+  const int t = threadIdx.x;
+  const int nt = n2 / EPT > 32 ? n2 / EPT : 32;
+  const bool act = t < nt;
+  uint64_t key[EPT];
+  int32_t pp[EPT];
+#pragma unroll
+  for (int e = 0; e < EPT; ++e) {
+    const int i = t * EPT + e;
+    const bool real = act && i < m;
+    key[e] = real ? dkey(v[i]) : ~0ull;
+    pp[e] = real ? 0 : 0x7fffffff;
+  }
+  bitonic_regs<EPT>(key, pp, n2, sK, sP);
+#pragma unroll
+  for (int e = 0; e < EPT; ++e) {
+    const int i = t * EPT + e;
+    if (act && i < m) v[i] = dkey_inv(key[e]);
+  }
+}
+
+// Ascending sort of each (parameter, gene) column of the gathered values.
+__global__ void __launch_bounds__(1024, 1) post_sort_kernel(const int64_t* aoff, int64_t total, int64_t G,
+                                                            double* scratch) {
+  extern __shared__ uint64_t post_smem[];
   const int64_t g = blockIdx.x % G;
   const int c = (int)(blockIdx.x / G);
   double* v = scratch + (int64_t)c * total + aoff[g];
@@ -130,32 +162,33 @@ __global__ void __launch_bounds__(1024) post_sort_kernel(const int64_t* aoff, in
   if (n <= 1) return;
   int64_t n2 = 1;
   while (n2 < n) n2 <<= 1;
-  double* w = n2 <= kPostSmem ? post_smem : v;
-  if (w != v) {
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) w[i] = v[i];
-    __syncthreads();
+  if (n2 <= kPostSmem) {
+    uint64_t* sK = post_smem;
+    int32_t* sP = reinterpret_cast<int32_t*>(post_smem + kPostSmem);
+    const int m = (int)n, w = (int)n2;
+    if (w <= 1024) post_sort_regs<1>(v, m, w, sK, sP);
+    else if (w == 2048) post_sort_regs<2>(v, m, w, sK, sP);
+    else if (w == 4096) post_sort_regs<4>(v, m, w, sK, sP);
+    else post_sort_regs<8>(v, m, w, sK, sP);
+    return;
   }
   for (int64_t k = 2; k <= n2; k <<= 1) {
     for (int64_t j = k >> 1; j > 0; j >>= 1) {
       for (int64_t i = threadIdx.x; i < n2; i += blockDim.x) {
         const int64_t partner = (j == (k >> 1)) ? (i ^ (k - 1)) : (i ^ j);
         if (partner > i && partner < n) {
-          const double a = w[i], b = w[partner];
+          const double a = v[i], b = v[partner];
           if (b < a) {
-            w[i] = b;
-            w[partner] = a;
+            v[i] = b;
+            v[partner] = a;
           }
         }
       }
       __syncthreads();
     }
   }
-  if (w != v)
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) v[i] = w[i];
 }
 
-// One thread per (gene, column): MAP = the first accepted particle (lowest
-// error), mean = sum in list order / n, bounds = quantiles 1 - q and q.
 __global__ void post_summary_kernel(const int64_t* aoff, const int64_t* idx, const double* theta, int64_t ld,
                                     int npar, int64_t G, int64_t total, const double* scratch, double q,
                                     double* map, double* mean, double* lb, double* ub, int64_t* n_out) {
@@ -188,7 +221,7 @@ cudaError_t launch_posterior_summary(const int64_t* aoff, const int64_t* idx, in
   if (G <= 0 || npar <= 0) return cudaSuccess;
   if (total > 0) {
     post_gather_kernel<<<(unsigned)G, 256, 0, s>>>(aoff, idx, theta, ld, npar, total, scratch);
-    constexpr int smem = kPostSmem * (int)sizeof(double);
+    constexpr int smem = kPostSmem * (int)(sizeof(uint64_t) + sizeof(int32_t));
     static bool attr = false;
     if (!attr) {
       cudaError_t e = cudaFuncSetAttribute(post_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);

@@ -197,8 +197,10 @@ class Context:
         return out, b0, b1.value, used.value
 
     def select(self, data: np.ndarray, se: np.ndarray, stats: np.ndarray, mode: int, eps_or_q: float,
-               families=None) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
-        """Accepted particles per gene: (offsets[G+1], 1-based indices, errors)."""
+               families=None, errors: bool = True) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """Accepted particles per gene: (offsets[G+1], 1-based indices, errors);
+        errors=False leaves the FP64 errors on the device and returns None for
+        them (the reference's acceptance writes only the sorted indices)."""
         d = np.ascontiguousarray(data, np.float64)
         e = np.ascontiguousarray(se, np.float64)
         s = np.ascontiguousarray(stats, np.float64)
@@ -207,17 +209,18 @@ class Context:
         tot = C.c_int64()
         self._check(self.lib.abc_errors_select(self.h, ptr(d), ptr(e), G, K, nf, ptr(f, C.c_int32), ptr(s),
                                                s.shape[0], mode, float(eps_or_q), C.byref(tot)))
-        return self._fetch(G, tot.value)
+        return self._fetch(G, tot.value, errors)
 
-    def _fetch(self, G: int, total: int):
+    def _fetch(self, G: int, total: int, errors: bool = True):
         self._sel_G = G
         off = np.zeros(G + 1, np.int64)
-        idx = np.zeros(max(total, 1), np.int64)
-        err = np.zeros(max(total, 1))
+        idx = np.empty(max(total, 1), np.int64)
+        err = np.empty(max(total, 1)) if errors else None
         self._check(self.lib.abc_accept_fetch(self.h, ptr(off, C.c_int64), ptr(idx, C.c_int64), ptr(err)))
-        return off, idx[:total], err[:total]
+        return off, idx[:total], (err[:total] if errors else None)
 
-    def select_thr(self, data: np.ndarray, se: np.ndarray, stats: np.ndarray, thr: np.ndarray, families=None):
+    def select_thr(self, data: np.ndarray, se: np.ndarray, stats: np.ndarray, thr: np.ndarray, families=None,
+                   errors: bool = True):
         """Acceptance with one threshold per gene."""
         d = np.ascontiguousarray(data, np.float64)
         e = np.ascontiguousarray(se, np.float64)
@@ -228,10 +231,10 @@ class Context:
         tot = C.c_int64()
         self._check(self.lib.abc_errors_select_thr(self.h, ptr(d), ptr(e), G, K, nf, ptr(f, C.c_int32), ptr(s),
                                                    s.shape[0], ptr(t), C.byref(tot)))
-        return self._fetch(G, tot.value)
+        return self._fetch(G, tot.value, errors)
 
     def select_device(self, data: np.ndarray, se: np.ndarray, d_stats: int, n: int, mode: int, eps_or_q: float = 0.0,
-                      thr: np.ndarray | None = None, families=None):
+                      thr: np.ndarray | None = None, families=None, errors: bool = True):
         """Acceptance with the statistics already in device memory."""
         d = np.ascontiguousarray(data, np.float64)
         e = np.ascontiguousarray(se, np.float64)
@@ -242,7 +245,7 @@ class Context:
         self._check(self.lib.abc_errors_select_device(self.h, ptr(d), ptr(e), G, K, nf, ptr(f, C.c_int32),
                                                       C.c_void_p(d_stats), n, mode, float(eps_or_q), ptr(t),
                                                       C.byref(tot)))
-        return self._fetch(G, tot.value)
+        return self._fetch(G, tot.value, errors)
 
     def select_profile(self) -> tuple[float, int]:
         """(candidate-pass kernel ms, passes) of the last selection (needs profile(True))."""

@@ -1209,9 +1209,10 @@ static int64_t draw_pos(uint64_t seed, int fam, int b, int64_t g, int64_t i, int
                    (uint32_t)b | ((uint32_t)(fam + 1) << 24), (uint32_t)g};
   uint32_t k[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)}, o[4];
   orc_philox4x32_10(c, k, o);
-  double u = (i & 1) ? u52(o[2], o[3]) : u52(o[0], o[1]);
-  int64_t p = (int64_t)(u * (double)n);
-  return p < n ? p : n - 1;
+  /* floor(x n / 2^52) of a 52-bit uniform integer x, exact */
+  uint32_t hi = (i & 1) ? o[2] : o[0], lo = (i & 1) ? o[3] : o[1];
+  uint64_t x = ((uint64_t)hi << 20) | (uint64_t)(lo >> 12);
+  return (int64_t)(((unsigned __int128)x * (unsigned __int128)(uint64_t)n) >> 52);
 }
 
 static double sample_cov(unsigned long long n, unsigned long long sx, unsigned long long sy, unsigned long long sxy) {
