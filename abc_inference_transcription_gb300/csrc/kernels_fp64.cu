@@ -173,7 +173,8 @@ __global__ void __launch_bounds__(256) stats_kernel(StatsArgs A) {
       }
     }
     __syncthreads();
-    if (threadIdx.x == 0) stats_from_moments(A.cfg, mom, wts, A.stats + p * K);
+    if (warp == 0)  // one condition per lane
+      for (int j = lane; j < A.cfg.n_conds; j += 32) stats_from_moments_cond(A.cfg, mom, wts, A.stats + p * K, j);
     __syncthreads();
   }
 }

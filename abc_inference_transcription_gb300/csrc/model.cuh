@@ -175,10 +175,13 @@ ABC_HD double wcov(const double* x, const double* y, const double* w, int A) {
   return s;
 }
 
-ABC_HD void stats_from_moments(const DevCfg& cfg, const double* m, const double* age_dist, double* st) {
+// the statistics of condition j (its ratio, mean_corr and corr_mean, and the
+// pulse or chase means and Fano factors when j is that condition); conditions
+// write disjoint entries, so they may run in any order or in parallel
+ABC_HD void stats_from_moments_cond(const DevCfg& cfg, const double* m, const double* age_dist, double* st, int j) {
   const int A = cfg.n_ages, J = cfg.n_conds;
   double w[kMaxAges], mu[kMaxAges], ml[kMaxAges], vu[kMaxAges], cv[kMaxAges], vl[kMaxAges];
-  for (int j = 0; j < J; ++j) {
+  {
     for (int a = 0; a < A; ++a) {
       const double* g = m + (j * A + a) * 5;
       w[a] = age_dist[a * J + j];
@@ -205,6 +208,10 @@ ABC_HD void stats_from_moments(const DevCfg& cfg, const double* m, const double*
       }
     }
   }
+}
+
+ABC_HD void stats_from_moments(const DevCfg& cfg, const double* m, const double* age_dist, double* st) {
+  for (int j = 0; j < cfg.n_conds; ++j) stats_from_moments_cond(cfg, m, age_dist, st, j);
 }
 
 // int128 -> double with the oracle's rounding (exact below 2^62).

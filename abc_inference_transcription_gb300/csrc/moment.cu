@@ -276,21 +276,23 @@ __global__ void __launch_bounds__(kMomThreads) moment_kernel(MomArgs a) {
     if (a.moments)
       for (int i = threadIdx.x; i < J * A * 5; i += blockDim.x) a.moments[p * (J * A * 5) + i] = mom[i];
     // ---- D: capture moment transform (model.jl:221-239) and statistics
-    if (threadIdx.x == 0) {
-      for (int j = 0; j < J; ++j)
-        for (int ai = 0; ai < A; ++ai) {
-          const double* bm = a.beta_mom + ((j < a.n_pulse_conds ? 0 : 1) * A + ai) * 3;
-          const double mb = bm[0], m2 = bm[1], vb = bm[2];
-          const double* s = mom + (j * A + ai) * 5;
-          double* d = ds + (j * A + ai) * 5;
-          d[0] = s[0] * mb;
-          d[1] = s[1] * mb;
-          d[2] = ((mb - m2) * s[0] + vb * (s[0] * s[0] + s[2])) + mb * mb * s[2];
-          d[4] = ((mb - m2) * s[1] + vb * (s[1] * s[1] + s[4])) + mb * mb * s[4];
-          d[3] = vb * (s[0] * s[1] + s[3]) + mb * mb * s[3];
-        }
-      stats_from_moments(cfg, ds, a.age_dist, a.stats + p * K);
+    // capture transform (model.jl:221-239) per (condition, age), then the
+    // statistics per condition on the lanes of warp 0
+    for (int t = threadIdx.x; t < J * A; t += blockDim.x) {
+      const int j = t / A, ai = t - (t / A) * A;
+      const double* bm = a.beta_mom + ((j < a.n_pulse_conds ? 0 : 1) * A + ai) * 3;
+      const double mb = bm[0], m2 = bm[1], vb = bm[2];
+      const double* sm = mom + (j * A + ai) * 5;
+      double* d = ds + (j * A + ai) * 5;
+      d[0] = sm[0] * mb;
+      d[1] = sm[1] * mb;
+      d[2] = ((mb - m2) * sm[0] + vb * (sm[0] * sm[0] + sm[2])) + mb * mb * sm[2];
+      d[4] = ((mb - m2) * sm[1] + vb * (sm[1] * sm[1] + sm[4])) + mb * mb * sm[4];
+      d[3] = vb * (sm[0] * sm[1] + sm[3]) + mb * mb * sm[3];
     }
+    __syncthreads();
+    if (threadIdx.x < 32)
+      for (int j = threadIdx.x; j < J; j += 32) stats_from_moments_cond(cfg, ds, a.age_dist, a.stats + p * K, j);
     __syncthreads();
   }
 }
