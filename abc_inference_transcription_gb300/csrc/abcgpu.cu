@@ -1367,7 +1367,7 @@ int abc_posterior_summary(abc_ctx* c, const double* theta, int64_t ld, int npar,
       e = cudaMemcpyAsync(d_theta.p, theta, sizeof(double) * P * ld, cudaMemcpyHostToDevice, c->stream);
     th = d_theta.p;
   }
-  if (e == cudaSuccess) e = d_scr.ensure((size_t)std::max<int64_t>(total, 1) * npar);
+  if (e == cudaSuccess) e = d_scr.ensure((size_t)total * npar + (size_t)4 * G * npar);
   if (e == cudaSuccess) e = d_out.ensure((size_t)4 * G * npar);
   if (e == cudaSuccess) e = d_n.ensure((size_t)G);
   if (e == cudaSuccess)

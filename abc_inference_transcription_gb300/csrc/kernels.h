@@ -182,6 +182,7 @@ cudaError_t launch_data_stats(const DataStatsArgs& a, double* se, cudaStream_t s
 // model probabilities with bootstrap intervals and per-gene posterior summaries (posterior.cu)
 cudaError_t launch_model_probs(const int64_t* counts, int64_t G, int M, int n_boot, double alpha, uint64_t seed,
                                double* prob, double* lb, double* ub, double* boot, cudaStream_t s);
+// scratch: total * npar + 4 * G * npar doubles
 cudaError_t launch_posterior_summary(const int64_t* aoff, const int64_t* idx, int64_t G, int64_t total,
                                      const double* theta, int64_t ld, int npar, double q, double* scratch,
                                      double* map, double* mean, double* lb, double* ub, int64_t* n_out,

@@ -5,7 +5,6 @@
 // FP64, built with -fmad=false: results are bit-identical to the C oracle.
 #include <cuda_runtime.h>
 
-#include "bitonic.cuh"
 #include "common.cuh"
 #include "kernels.h"
 
@@ -14,24 +13,31 @@ namespace abc {
 // Julia's default quantile (Statistics.quantile, alpha = beta = 1) of a sorted
 // vector: m = 1 - p, aleph = n p + m, j = clamp(trunc(aleph), 1, n - 1),
 // gamma = clamp(aleph - j, 0, 1), v[j] + gamma (v[j+1] - v[j]) (1-based).
-__device__ double quantile_sorted(const double* v, int64_t n, double p) {
+// position of Julia's default quantile (type 7: m = 1 - p, aleph = n p + m),
+// j clamped to [1, n - 1], and its interpolation weight
+__device__ __forceinline__ void quantile_pos(int64_t n, double p, int64_t& j, double& gmm) {
   const double m = 1.0 + p * ((1.0 - 1.0) - 1.0);
   const double aleph = (double)n * p + m;
-  int64_t j = (int64_t)aleph;
+  j = (int64_t)aleph;
   if (j > n - 1) j = n - 1;
   if (j < 1 && n > 1) j = 1;
-  double gmm = aleph - (double)j;
+  gmm = aleph - (double)j;
   gmm = gmm < 0.0 ? 0.0 : (gmm > 1.0 ? 1.0 : gmm);
-  double a, b;
-  if (n == 1) {
-    a = v[0];
-    b = v[0];
-  } else {
-    a = v[j - 1];
-    b = v[j];
-  }
+}
+
+// quantile from the order statistics a = v[j - 1], b = v[j] (v[0] twice for n = 1)
+__device__ __forceinline__ double quantile_mix(double a, double b, double gmm) {
   if (isfinite(a) && isfinite(b)) return a + gmm * (b - a);
   return (1.0 - gmm) * a + gmm * b;
+}
+
+__device__ double quantile_sorted(const double* v, int64_t n, double p) {
+  int64_t j;
+  double gmm;
+  quantile_pos(n, p, j, gmm);
+  const double a = n == 1 ? v[0] : v[j - 1];
+  const double b = n == 1 ? v[0] : v[j];
+  return quantile_mix(a, b, gmm);
 }
 
 // One thread per gene.  counts[g][m] = accepted particles of model group m.
@@ -117,7 +123,9 @@ __global__ void post_gather_kernel(const int64_t* aoff, const int64_t* idx, cons
   }
 }
 
-constexpr int kPostSmem = 8192;  // segments up to this size sort in registers
+constexpr int kPostSmem = 8192;   // columns up to this size are staged in shared memory
+constexpr int kSelThreads = 256;
+constexpr int kSelSmall = 64;     // candidate sets this small are ranked by counting
 
 // order-preserving 64-bit keys of doubles (negative values reversed)
 __device__ __forceinline__ uint64_t dkey(double x) {
@@ -129,68 +137,129 @@ __device__ __forceinline__ double dkey_inv(uint64_t k) {
   return __longlong_as_double((long long)b);
 }
 
-template <int EPT>
-__device__ void post_sort_regs(double* v, int m, int n2, uint64_t* sK, int32_t* sP) {
-  const int t = threadIdx.x;
-  const int nt = n2 / EPT > 32 ? n2 / EPT : 32;
-  const bool act = t < nt;
-  uint64_t key[EPT];
-  int32_t pp[EPT];
+struct SelShared {
+  unsigned hist[256];
+  uint64_t cand[kSelSmall];
+  uint64_t result;
+  int bin, cnt, ncand;
+  long long rr;
+};
+
+// The rank-th smallest (0-based) of the n keys K: radix select over 8-bit
+// digits from the top, narrowing to the digit bucket that holds the rank;
+// once the bucket has at most kSelSmall keys they are collected and the rank
+// is found by counting.  Every thread of the block calls it.
+__device__ uint64_t block_select(const uint64_t* K, int64_t n, int64_t rank, SelShared& sh) {
+  uint64_t prefix = 0, mask = 0;
+  long long rr = rank;
+  const int lane = threadIdx.x & 31;
+  for (int shift = 56; shift >= 0; shift -= 8) {
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) sh.hist[i] = 0u;
+    __syncthreads();
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+      const uint64_t k = K[i];
+      if ((k & mask) == prefix) atomicAdd(&sh.hist[(k >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      unsigned loc[8], sum = 0;
 #pragma unroll
-  for (int e = 0; e < EPT; ++e) {
-    const int i = t * EPT + e;
-    const bool real = act && i < m;
-    key[e] = real ? dkey(v[i]) : ~0ull;
-    pp[e] = real ? 0 : 0x7fffffff;
+      for (int b = 0; b < 8; ++b) {
+        loc[b] = sh.hist[lane * 8 + b];
+        sum += loc[b];
+      }
+      unsigned incl = sum;
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+      }
+      const long long excl = (long long)(incl - sum);
+      if (rr >= excl && rr < (long long)incl) {
+        long long c = excl;
+        for (int b = 0; b < 8; ++b) {
+          if (rr < c + (long long)loc[b]) {
+            sh.bin = lane * 8 + b;
+            sh.rr = rr - c;
+            sh.cnt = (int)loc[b];
+            break;
+          }
+          c += loc[b];
+        }
+      }
+    }
+    __syncthreads();
+    prefix |= (uint64_t)sh.bin << shift;
+    mask |= (uint64_t)255u << shift;
+    rr = sh.rr;
+    const int cnt = sh.cnt;
+    __syncthreads();
+    if (shift == 0) return prefix;  // every bit fixed
+    if (cnt <= kSelSmall) {
+      if (threadIdx.x == 0) sh.ncand = 0;
+      __syncthreads();
+      for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const uint64_t k = K[i];
+        if ((k & mask) == prefix) sh.cand[atomicAdd(&sh.ncand, 1)] = k;
+      }
+      __syncthreads();
+      if (threadIdx.x < cnt) {
+        const uint64_t x = sh.cand[threadIdx.x];
+        int less = 0, eq = 0;
+        for (int u = 0; u < cnt; ++u) {
+          less += sh.cand[u] < x ? 1 : 0;
+          eq += sh.cand[u] == x ? 1 : 0;
+        }
+        if (less <= rr && rr < less + eq) sh.result = x;  // equal keys write the same value
+      }
+      __syncthreads();
+      const uint64_t res = sh.result;
+      __syncthreads();
+      return res;
+    }
   }
-  bitonic_regs<EPT>(key, pp, n2, sK, sP);
-#pragma unroll
-  for (int e = 0; e < EPT; ++e) {
-    const int i = t * EPT + e;
-    if (act && i < m) v[i] = dkey_inv(key[e]);
-  }
+  return prefix;
 }
 
-// Ascending sort of each (parameter, gene) column of the gathered values.
-__global__ void __launch_bounds__(1024, 1) post_sort_kernel(const int64_t* aoff, int64_t total, int64_t G,
-                                                            double* scratch) {
-  extern __shared__ uint64_t post_smem[];
+// Per (parameter, gene) column of the gathered values, the order statistics
+// the two quantiles read: q4 = {v[j_lo - 1], v[j_lo], v[j_hi - 1], v[j_hi]} of
+// the sorted column (quantile_pos with p = 1 - q and p = q).  Columns longer
+// than kPostSmem are keyed in place in the scratch.
+__global__ void __launch_bounds__(kSelThreads) post_select_kernel(const int64_t* aoff, int64_t total, int64_t G,
+                                                                  double* scratch, double q, double* q4) {
+  extern __shared__ uint64_t sel_keys[];
+  __shared__ SelShared sh;
   const int64_t g = blockIdx.x % G;
   const int c = (int)(blockIdx.x / G);
   double* v = scratch + (int64_t)c * total + aoff[g];
   const int64_t n = aoff[g + 1] - aoff[g];
-  if (n <= 1) return;
-  int64_t n2 = 1;
-  while (n2 < n) n2 <<= 1;
-  if (n2 <= kPostSmem) {
-    uint64_t* sK = post_smem;
-    int32_t* sP = reinterpret_cast<int32_t*>(post_smem + kPostSmem);
-    const int m = (int)n, w = (int)n2;
-    if (w <= 1024) post_sort_regs<1>(v, m, w, sK, sP);
-    else if (w == 2048) post_sort_regs<2>(v, m, w, sK, sP);
-    else if (w == 4096) post_sort_regs<4>(v, m, w, sK, sP);
-    else post_sort_regs<8>(v, m, w, sK, sP);
+  double* out = q4 + ((int64_t)c * G + g) * 4;
+  if (n == 0) return;
+  if (n == 1) {
+    if (threadIdx.x < 4) out[threadIdx.x] = v[0];
     return;
   }
-  for (int64_t k = 2; k <= n2; k <<= 1) {
-    for (int64_t j = k >> 1; j > 0; j >>= 1) {
-      for (int64_t i = threadIdx.x; i < n2; i += blockDim.x) {
-        const int64_t partner = (j == (k >> 1)) ? (i ^ (k - 1)) : (i ^ j);
-        if (partner > i && partner < n) {
-          const double a = v[i], b = v[partner];
-          if (b < a) {
-            v[i] = b;
-            v[partner] = a;
-          }
-        }
-      }
-      __syncthreads();
-    }
+  uint64_t* K;
+  if (n <= kPostSmem) {
+    K = sel_keys;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) K[i] = dkey(v[i]);
+  } else {
+    K = reinterpret_cast<uint64_t*>(v);
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) K[i] = dkey(v[i]);
+  }
+  __syncthreads();
+  int64_t jl, jh;
+  double gl, gh;
+  quantile_pos(n, 1.0 - q, jl, gl);
+  quantile_pos(n, q, jh, gh);
+  const int64_t ranks[4] = {jl - 1, jl, jh - 1, jh};
+  for (int r = 0; r < 4; ++r) {
+    const uint64_t k = block_select(K, n, ranks[r], sh);
+    if (threadIdx.x == 0) out[r] = dkey_inv(k);
   }
 }
 
 __global__ void post_summary_kernel(const int64_t* aoff, const int64_t* idx, const double* theta, int64_t ld,
-                                    int npar, int64_t G, int64_t total, const double* scratch, double q,
+                                    int npar, int64_t G, int64_t total, const double* q4, double q,
                                     double* map, double* mean, double* lb, double* ub, int64_t* n_out) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= G * npar) return;
@@ -209,9 +278,13 @@ __global__ void post_summary_kernel(const int64_t* aoff, const int64_t* idx, con
   double s = 0.0;
   for (int64_t i = 0; i < n; ++i) s = s + theta[(idx[o + i] - 1) * ld + c];
   mean[t] = s / (double)n;
-  const double* v = scratch + (int64_t)c * total + o;
-  lb[t] = quantile_sorted(v, n, 1.0 - q);
-  ub[t] = quantile_sorted(v, n, q);
+  const double* v4 = q4 + ((int64_t)c * G + g) * 4;
+  int64_t j;
+  double gl, gh;
+  quantile_pos(n, 1.0 - q, j, gl);
+  quantile_pos(n, q, j, gh);
+  lb[t] = quantile_mix(v4[0], v4[1], gl);
+  ub[t] = quantile_mix(v4[2], v4[3], gh);
 }
 
 cudaError_t launch_posterior_summary(const int64_t* aoff, const int64_t* idx, int64_t G, int64_t total,
@@ -219,19 +292,21 @@ cudaError_t launch_posterior_summary(const int64_t* aoff, const int64_t* idx, in
                                      double* map, double* mean, double* lb, double* ub, int64_t* n_out,
                                      cudaStream_t s) {
   if (G <= 0 || npar <= 0) return cudaSuccess;
+  // scratch: total x npar gathered values, then G x npar x 4 order statistics
+  double* q4 = scratch + (size_t)total * npar;
   if (total > 0) {
     post_gather_kernel<<<(unsigned)G, 256, 0, s>>>(aoff, idx, theta, ld, npar, total, scratch);
-    constexpr int smem = kPostSmem * (int)(sizeof(uint64_t) + sizeof(int32_t));
+    constexpr int smem = kPostSmem * (int)sizeof(uint64_t);
     static bool attr = false;
     if (!attr) {
-      cudaError_t e = cudaFuncSetAttribute(post_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+      cudaError_t e = cudaFuncSetAttribute(post_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
       if (e != cudaSuccess) return e;
       attr = true;
     }
-    post_sort_kernel<<<(unsigned)(G * npar), 1024, smem, s>>>(aoff, total, G, scratch);
+    post_select_kernel<<<(unsigned)(G * npar), kSelThreads, smem, s>>>(aoff, total, G, scratch, q, q4);
   }
   const int64_t n = G * npar;
-  post_summary_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(aoff, idx, theta, ld, npar, G, total, scratch, q,
+  post_summary_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(aoff, idx, theta, ld, npar, G, total, q4, q,
                                                                   map, mean, lb, ub, n_out);
   return cudaGetLastError();
 }

@@ -118,13 +118,17 @@ def test_posterior_summary_gpu_bit_exact(built, orc):
     data = base[rng.integers(0, 200, G)] * rng.lognormal(0, 0.05, (G, K))
     se = 0.1 * np.abs(data) * rng.lognormal(0, 0.5, (G, K))
     theta = rng.normal(size=(P, 9))
+    tied = np.round(theta * 2.0) / 2.0                   # heavy ties, negative values and zeros
     with Context(make_config("hour"), None) as ctx:
-        for mode, x in ((1, 0.3), (1, 0.002), (0, 0.5)):    # 9,000 per gene (global-memory sort) and small lists
+        # 9,000 per gene (columns keyed in place), small lists, one entry per gene
+        for mode, x in ((1, 0.3), (1, 0.002), (0, 0.5), (1, 1.0 / P)):
             off, idx, _ = ctx.select(data, se, stats, mode, x, None)
-            got = ctx.posterior_summary(theta, q=0.95)
-            want = orc.posterior_summary(theta, off, idx, 0.95)
-            for k in ("map", "mean", "lower", "upper", "n_particles"):
-                assert np.array_equal(got[k], want[k], equal_nan=True), (mode, x, k)
+            for th in (theta, tied):
+                got = ctx.posterior_summary(th, q=0.95)
+                want = orc.posterior_summary(th, off, idx, 0.95)
+                for k in ("map", "mean", "lower", "upper", "n_particles"):
+                    assert np.array_equal(got[k], want[k], equal_nan=True), (mode, x, k)
+        off, idx, _ = ctx.select(data, se, stats, 1, 0.002, None)
         d_theta = torch.from_numpy(theta).cuda()
         got = ctx.posterior_summary(d_theta.data_ptr(), npar=5, on_device=True, ld=9, q=0.9)
         want = orc.posterior_summary(np.ascontiguousarray(theta[:, :5]), off, idx, 0.9)
