@@ -24,12 +24,13 @@ ERR_EVENT_CAP = -4
 ERR_NONFINITE = -5
 ERR_CAPACITY = -6
 ERR_STATE = -7
+ERR_IO = -8
 
 STATUS_NAMES = {
     OK: "ABC_OK", ERR_INVALID: "ABC_ERR_INVALID", ERR_CUDA: "ABC_ERR_CUDA",
     ERR_NOMEM: "ABC_ERR_NOMEM", ERR_EVENT_CAP: "ABC_ERR_EVENT_CAP",
     ERR_NONFINITE: "ABC_ERR_NONFINITE", ERR_CAPACITY: "ABC_ERR_CAPACITY",
-    ERR_STATE: "ABC_ERR_STATE",
+    ERR_STATE: "ABC_ERR_STATE", ERR_IO: "ABC_ERR_IO",
 }
 
 # model index m of wrapper.jl:47-51
@@ -154,6 +155,10 @@ def _declare(lib: C.CDLL) -> None:
                                                C.c_double, dp, i64p]),
         "abc_accept_fetch": (C.c_int, [vp, i64p, i64p, dp]),
         "abc_select_counters": (C.c_int, [vp, i64p, i64p]),
+        "abc_write_particles": (C.c_int, [C.c_char_p, C.c_int, C.c_int64, i64p, i64p]),
+        "abc_write_matrix": (C.c_int, [C.c_char_p, C.c_int, C.c_int64, C.c_int64, dp, C.c_int64]),
+        "abc_format_double": (C.c_int, [C.c_double, C.c_char_p, C.c_int]),
+        "abc_read_particles": (C.c_int, [C.c_char_p, i64p, i64p, i64p, i64p]),
         "abc_select_profile_read": (C.c_int, [vp, dp, C.POINTER(C.c_int)]),
         "abc_set_distance_mode": (C.c_int, [vp, C.c_int]),
         "abc_set_graph": (C.c_int, [vp, C.c_int]),
@@ -201,7 +206,8 @@ ABI_SYMBOLS = [
     "abc_synchronize", "abc_simulate_batch", "abc_simulate_batch_device", "abc_simulate_noalloc", "abc_simulate_cells", "abc_last_counters",
     "abc_profile", "abc_profile_read", "abc_autotune", "abc_set_variant", "abc_errors",
     "abc_errors_select", "abc_errors_select_thr", "abc_errors_select_device", "abc_accept_fetch",
-    "abc_select_counters", "abc_select_profile_read", "abc_set_distance_mode", "abc_get_distance_mode",
+    "abc_select_counters", "abc_select_profile_read", "abc_write_particles", "abc_write_matrix",
+    "abc_format_double", "abc_read_particles", "abc_set_distance_mode", "abc_get_distance_mode",
     "abc_errors_candidate", "abc_model_probs", "abc_posterior_summary",
     "abc_moment_simulate", "abc_data_stats", "abc_set_graph", "abc_graph_counters",
     "abc_surrogate_create", "abc_surrogate_destroy", "abc_surrogate_last_error", "abc_surrogate_num_params",

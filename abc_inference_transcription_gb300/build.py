@@ -37,6 +37,7 @@ UNITS = {
     "mlp.cu": [],
     "mlp_tc.cu": [],
     "surrogate.cu": [],
+    "formats.cu": [],
 }
 
 

@@ -46,7 +46,8 @@ typedef enum abc_status {
   ABC_ERR_EVENT_CAP = -4, /* a trajectory exceeded abc_config.event_cap fired events */
   ABC_ERR_NONFINITE = -5, /* non-finite rate or count overflow inside a kernel */
   ABC_ERR_CAPACITY = -6,  /* candidate buffer could not be grown or top-q did not converge */
-  ABC_ERR_STATE = -7      /* call order violated (e.g. simulate before set_cells) */
+  ABC_ERR_STATE = -7,     /* call order violated (e.g. simulate before set_cells) */
+  ABC_ERR_IO = -8         /* a file could not be opened, written or parsed */
 } abc_status;
 
 /* Model index m, as in wrapper.jl:47-51 and scripts/abc_simulation.jl:82-85. */
@@ -368,6 +369,31 @@ int abc_surrogate_set_screen_mode(abc_surrogate* s, int mode);
  * (either output may be NULL); *n_out = number of survivors. */
 int abc_surrogate_compact_device(abc_surrogate* s, const uint8_t* d_keep, const double* d_theta, int ld_theta,
                                  int64_t n, double* d_theta_out, int64_t* d_idx_out, int64_t* n_out);
+
+/* ---- on-disk text formats (host only, no context) ----------------------
+ * Tab-delimited rows as the reference's DelimitedFiles.writedlm writes them;
+ * floats in the shortest form that reads back to the same double (Julia's
+ * spelling: "1.0", "2.5e-5", NaN, Inf).  append != 0 appends, as the
+ * reference's scripts do.  Return ABC_OK, ABC_ERR_INVALID or ABC_ERR_IO. */
+/* particles_<model>.txt (scripts/accepted_particles.jl:21-29): one line per
+ * gene with its accepted 1-based indices, or "0" when none; gene_offsets has
+ * n_genes + 1 entries (the layout abc_accept_fetch returns). */
+int abc_write_particles(const char* path, int append, int64_t n_genes, const int64_t* gene_offsets,
+                        const int64_t* particle_idx);
+/* rows x cols row-major matrix with leading dimension ld: sets_<model>.txt
+ * (scripts/abc_simulation.jl:93-94), the s_pulse / s_chase / s_ratios /
+ * s_mean_corr / s_corr_mean files (:47-60), error_<model>.txt
+ * (scripts/compute_errors.jl:66-67), model_prob / l_bound / u_bound
+ * (scripts/model_probs.jl:54-61), posterior estimates
+ * (scripts/posterior_kinetics.jl:72-75). */
+int abc_write_matrix(const char* path, int append, int64_t rows, int64_t cols, const double* m, int64_t ld);
+/* one float as abc_write_matrix writes it (buf_len >= 32); returns its length */
+int abc_format_double(double x, char* buf, int buf_len);
+/* particles file -> offsets (n_genes + 1) and 1-based indices, as
+ * scripts/posterior_kinetics.jl:56-60 reads it ("0" = no particle).  First
+ * call with gene_offsets = particle_idx = NULL for the sizes. */
+int abc_read_particles(const char* path, int64_t* n_genes, int64_t* n_total, int64_t* gene_offsets,
+                       int64_t* particle_idx);
 
 #ifdef __cplusplus
 }
