@@ -6,8 +6,8 @@
 // every moment depends only on itself and on moments listed before it.
 // Products of lower-triangular matrices stay lower triangular, so an
 // exponential product costs 220 FMA instead of 1000 and a substep 55 instead
-// of 100.  Taylor order 10 after scaling to a column-sum norm <= 1/2
-// (truncation < 3e-10).  Substep and labelling indices are integers (the
+// of 100.  Taylor order 8 after scaling to a column-sum norm <= 1/2
+// (truncation < 6e-9, below FP32's 6e-8 resolution).  Substep and labelling indices are integers (the
 // grid is aligned with every breakpoint), so the per-substep work has no FP64
 // operation; rates, times and the statistics stay in FP64.  The transient
 // phase applies the one-cycle propagator (the ordered product of the cycle's
@@ -28,7 +28,7 @@ constexpr int NA = 10;
 constexpr int NT = NA * (NA + 1) / 2;  // 55 lower-triangular entries, row-major packed
 constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
-constexpr int kTaylor = 10;
+constexpr int kTaylor = 8;
 
 // packed index of (r, c), c <= r
 __host__ __device__ constexpr int tri(int r, int c) { return r * (r + 1) / 2 + c; }
