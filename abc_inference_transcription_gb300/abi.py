@@ -155,6 +155,7 @@ def _declare(lib: C.CDLL) -> None:
                                                C.c_double, dp, i64p]),
         "abc_accept_fetch": (C.c_int, [vp, i64p, i64p, dp]),
         "abc_select_counters": (C.c_int, [vp, i64p, i64p]),
+        "abc_set_select_errors": (C.c_int, [vp, C.c_int]),
         "abc_write_particles": (C.c_int, [C.c_char_p, C.c_int, C.c_int64, i64p, i64p]),
         "abc_write_matrix": (C.c_int, [C.c_char_p, C.c_int, C.c_int64, C.c_int64, dp, C.c_int64]),
         "abc_format_double": (C.c_int, [C.c_double, C.c_char_p, C.c_int]),
@@ -206,7 +207,7 @@ ABI_SYMBOLS = [
     "abc_synchronize", "abc_simulate_batch", "abc_simulate_batch_device", "abc_simulate_noalloc", "abc_simulate_cells", "abc_last_counters",
     "abc_profile", "abc_profile_read", "abc_autotune", "abc_set_variant", "abc_errors",
     "abc_errors_select", "abc_errors_select_thr", "abc_errors_select_device", "abc_accept_fetch",
-    "abc_select_counters", "abc_select_profile_read", "abc_write_particles", "abc_write_matrix",
+    "abc_select_counters", "abc_select_profile_read", "abc_set_select_errors", "abc_write_particles", "abc_write_matrix",
     "abc_format_double", "abc_read_particles", "abc_set_distance_mode", "abc_get_distance_mode",
     "abc_errors_candidate", "abc_model_probs", "abc_posterior_summary",
     "abc_moment_simulate", "abc_data_stats", "abc_set_graph", "abc_graph_counters",

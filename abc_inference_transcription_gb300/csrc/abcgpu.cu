@@ -104,6 +104,13 @@ struct abc_ctx {
   int64_t cand_cap = int64_t(1) << 22;
   int64_t sel_G = 0, sel_P = 0, sel_total = 0, sel_cands = 0, sel_rechecked = 0, sel_cands_emitted = 0;
   bool sel_ready = false;
+  bool sel_errors = true;        // selections keep the FP64 error of every accepted pair
+  bool sel_errors_exact = true;  // the last selection's stored errors are FP64
+  DBuf<float4> d_ffg;
+  DBuf<int32_t> d_pos;
+  DBuf<uint8_t> d_flag;
+  DBuf<unsigned long long> d_cnt2;
+  DBuf<int> d_dirty;
 };
 
 static int fail(abc_ctx* c, int status, const std::string& msg) {
@@ -215,6 +222,8 @@ int abc_destroy(abc_ctx* c) {
   c->d_models.release(); c->d_order.release(); c->d_ohist.release(); c->d_rec.release(); c->d_recf.release(); c->d_counts.release(); c->d_captured.release();
   c->d_events.release(); c->d_hash.release(); c->d_misc.release(); c->d_status.release();
   c->d_data.release(); c->d_se.release(); c->d_sel_stats.release(); c->d_se64.release(); c->d_sg.release();
+  c->d_ffg.release(); c->d_pos.release(); c->d_flag.release(); c->d_cnt2.release();
+  c->d_dirty.release();
   c->d_out_err.release(); c->d_sw.release(); c->d_dw.release(); c->d_s32.release(); c->d_X.release();
   c->d_esub.release(); c->d_cand.release(); c->d_sp.release(); c->d_gcount.release(); c->d_goff.release();
   c->d_cande.release(); c->d_den.release(); c->d_rden.release(); c->d_tcA.release(); c->d_tcB.release(); c->d_cg32.release(); c->d_b0.release();
@@ -1052,14 +1061,35 @@ static int select_impl(abc_ctx* c, const double* data, const double* se, int64_t
     CK(c->d_se64.ensure((size_t)std::max<int64_t>(nre, 1)));
     CK(c->d_sp.ensure((size_t)std::max<int64_t>(nre, 1)));
     CK(c->d_sg.ensure((size_t)std::max<int64_t>(nre, 1)));
-    CK(launch_dist_group_recheck_sort(in, rc, nre, c->d_gcount.p, c->d_goff.p, c->d_gcursor.p, c->d_sp.p,
-                                      c->d_sg.p, c->d_se64.p, c->stream));
+    if (c->sel_errors) {
+      CK(launch_dist_group_recheck_sort(in, rc, nre, c->d_gcount.p, c->d_goff.p, c->d_gcursor.p, c->d_sp.p,
+                                        c->d_sg.p, c->d_se64.p, c->stream));
+    } else {
+      // indices only: certified FP32 errors, FP64 where they cannot decide
+      CK(c->d_ffg.ensure((size_t)G * K));
+      CK(c->d_pos.ensure((size_t)std::max<int64_t>(nre, 1)));
+      CK(c->d_flag.ensure((size_t)std::max<int64_t>(nre, 1)));
+      CK(c->d_cnt2.ensure(2));
+      CK(c->d_dirty.ensure((size_t)G));
+      CK(launch_dist_group_certify_sort(in, rc, nre, mode, eps_or_q, mode == 2 ? c->d_thr.p : nullptr,
+                                        c->d_gcount.p, c->d_goff.p, c->d_gcursor.p, c->d_sp.p, c->d_sg.p,
+                                        c->d_se64.p, c->d_ffg.p, c->d_pos.p, c->d_flag.p,
+                                        c->d_cnt2.p,
+                                        c->d_dirty.p, c->stream));
+    }
     CK(cudaMemsetAsync(c->d_fail.p, 0, sizeof(int) * G, c->stream));
     CK(launch_dist_accept_len(c->d_goff.p, c->d_se64.p, G, mode == 2 ? 0 : mode, eps_or_q,
                               mode == 2 ? c->d_thr.p : nullptr, kq, Xacc, c->d_b0.p, b1, c->d_alen.p, c->d_fail.p,
-                              c->stream));
+                              !c->sel_errors, c->stream));
     c->sel_cands_emitted += ncand;
-    c->sel_rechecked += nre;
+    if (c->sel_errors) {
+      c->sel_rechecked += nre;
+    } else {
+      unsigned long long hc[2] = {0ull, 0ull};
+      CK(cudaMemcpyAsync(hc, c->d_cnt2.p, sizeof(hc), cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+      c->sel_rechecked += (int64_t)(hc[0] + hc[1]);
+    }
     if (mode != 1) break;
     std::vector<int> hf((size_t)G);
     CK(cudaMemcpyAsync(hf.data(), c->d_fail.p, sizeof(int) * G, cudaMemcpyDeviceToHost, c->stream));
@@ -1087,6 +1117,7 @@ static int select_impl(abc_ctx* c, const double* data, const double* se, int64_t
   c->sel_G = G;
   c->sel_P = P;
   c->sel_total = total;
+  c->sel_errors_exact = c->sel_errors;
   c->sel_cands = c->sel_cands_emitted;
   c->sel_ready = true;
   if (n_accepted_total) *n_accepted_total = total;
@@ -1157,10 +1188,19 @@ int abc_accept_fetch(abc_ctx* c, int64_t* gene_offsets, int64_t* particle_idx, d
   if (c->sel_total > 0) {
     CK(cudaMemcpyAsync(particle_idx, c->d_out_idx.p, sizeof(int64_t) * c->sel_total, cudaMemcpyDeviceToHost,
                        c->stream));
-    if (err)
+    if (err) {
+      if (!c->sel_errors_exact)
+        return fail(c, ABC_ERR_STATE, "the selection kept no FP64 errors (abc_set_select_errors(ctx, 0)); pass err = NULL");
       CK(cudaMemcpyAsync(err, c->d_out_err.p, sizeof(double) * c->sel_total, cudaMemcpyDeviceToHost, c->stream));
+    }
   }
   CK(cudaStreamSynchronize(c->stream));
+  return ABC_OK;
+}
+
+int abc_set_select_errors(abc_ctx* c, int keep_errors) {
+  if (!c) return ABC_ERR_INVALID;
+  c->sel_errors = keep_errors != 0;
   return ABC_OK;
 }
 

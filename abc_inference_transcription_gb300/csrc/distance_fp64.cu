@@ -192,6 +192,223 @@ __global__ void __launch_bounds__(kRecheckWarps * 32) recheck_grouped_kernel(Dis
   }
 }
 
+// ---------------------------------------------------------------------------
+// Certified FP32 errors for selections that return indices only
+// ---------------------------------------------------------------------------
+// A candidate's error is evaluated in FP32 from two-float splits of its FP64
+// inputs: x = h + l with |x - h - l| <= 2^-47 |x|, |l| <= 2^-23 |x| (data: h =
+// RN32(x), l = RN32(x - h); statistics: h = the top 24 significand bits,
+// exact integer bit manipulation, l = the remaining 29 bits rounded to float).
+// With r = 1/den rounded to float, u = 2^-24:
+//   delta = RN(RN(dh - sh) + RN(dl - sl))       (the hi parts cancel exactly)
+//   T     = RN(delta RN(delta r))               per statistic
+//   S     = Kahan sum of the T, e = RN(S RN(1/K))
+// and, writing T* = (d - s)^2 / den for the exact term and a = den^-1/2 (so
+// a |d| <= 10 because den >= 0.01 d^2): |delta - (d - s)| <= 2.0001 u |d - s| +
+// 2^-45.4 (|d| + |s|), hence |T - T*| <= 7.03 u T* + 2^-44.4 (20 sqrt(T*) + T*)
+// + 2^-90 (20 + sqrt(T*))^2; Kahan summation adds <= 2.1 u sum T, the final
+// scaling 2.01 u, and the reference's FP64 evaluation differs from the exact
+// value by < 1e-14 relative.  Altogether |e - err64| <= 11.2 u err +
+// 2^-40 sqrt(err) + 2^-80; 1e-6 e + 1.5e-12 sqrt(e + 1e-12) covers that with a
+// 1.5x margin, and approx_bound uses its linear majorant (1e-6 + 1e-12) e +
+// 1e-12 (sqrt(x) <= (1 + x) / 2), one FMA instead of an FP64 square root;
+// v - B(v) and v + B(v) are increasing in v.  The derivation
+// needs every |d|, |s| in {0} u [2^-60, 2^60] (no underflow in the splits),
+// den in [2^-120, 2^120] (1/den a normal float; an underflow in delta r then
+// costs at most 2^-88 per term, far inside the bound's absolute part) and a
+// finite result; other pairs are computed in FP64.
+__device__ __forceinline__ bool key_less(double ea, int32_t pa, double eb, int32_t pb);
+__device__ __forceinline__ double approx_bound(double v) { return fma(1.000001e-6, v, 1e-12); }
+
+// x = h + l by truncation of the significand, on the two 32-bit halves of x
+// (integer operations only): h keeps the sign, the exponent rebiased from 1023
+// to 127 and the top 23 stored significand bits; l is the remaining 29 bits
+// rounded to float and scaled by 2^(e - 1075).
+__device__ __forceinline__ bool split_trunc(double x, float& h, float& l) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned mag = hi & 0x7fffffffu, sign = hi & 0x80000000u;
+  const unsigned e = mag >> 20;
+  const bool zero = (mag | lo) == 0u;
+  const bool ok = zero || e - (1023u - 60u) <= 120u;  // exponent in [-60, 60]
+  // ((e - 896) << 23) | (top 20 bits << 3) | (next 3 bits): the float's exponent and significand
+  h = __uint_as_float(zero ? 0u : (sign | ((mag - (896u << 20)) << 3) | (lo >> 29)));
+  const float r = __uint2float_rn(lo & 0x1fffffffu);
+  const float scale = __uint_as_float(((e - 948u) & 0xffu) << 23);  // 2^(e - 1075); garbage when !ok
+  l = zero ? 0.0f : __uint_as_float(__float_as_uint(__fmul_rn(r, scale)) | sign);
+  return ok;
+}
+
+// per (gene, statistic): (h, l, 1/den, 0) with d = h + l
+__global__ void ff_prep_genes_kernel(DistInputs in, float4* gt) {
+  const int64_t n = in.G * in.K;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double d = in.data[i], den = in.den[i];
+    const double ad = fabs(d);
+    const bool ok = (d == 0.0 || (ad >= 0x1p-60 && ad <= 0x1p60)) && den >= 0x1p-120 && den <= 0x1p120;
+    const float h = (float)d;
+    gt[i] = make_float4(h, (float)(d - (double)h), ok ? (float)in.rden[i] : __int_as_float(0x7fc00000), 0.0f);
+  }
+}
+
+// Candidates grouped by gene, statistics rows staged as in
+// recheck_grouped_kernel.  v[i] = the certified FP32 error (10 exactly when
+// it lies above 10 by more than its bound); pairs outside the derivation's
+// range get their position appended to pos (FP64 later).
+__global__ void __launch_bounds__(kRecheckWarps * 32) approx_grouped_kernel(DistInputs in, const int32_t* sp,
+                                                                            const int32_t* sg, int64_t n,
+                                                                            const float4* gt, float rK, double* v,
+                                                                            int32_t* pos,
+                                                                            unsigned long long* count) {
+  __shared__ double rs_smem[kRecheckWarps * 32 * kRecheckLd];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int K = in.K;
+  double* S = rs_smem + warp * 32 * kRecheckLd;
+  const int64_t n_chunks = (n + 31) >> 5;
+  const int64_t wstride = (int64_t)gridDim.x * kRecheckWarps;
+  for (int64_t ch = (int64_t)blockIdx.x * kRecheckWarps + warp; ch < n_chunks; ch += wstride) {
+    const int64_t i = ch * 32 + lane;
+    const bool mine = i < n;
+    const int32_t p = mine ? sp[i] : 0;
+    const int64_t g = mine ? sg[i] : 0;
+    const int rows = (int)(n - ch * 32 < 32 ? n - ch * 32 : 32);
+    const float4* gk = gt + g * K;
+    float acc = 0.0f, comp = 0.0f;
+    bool ok = true;
+    for (int c0 = 0; c0 < K; c0 += kRecheckCols) {
+      const int cw = K - c0 < kRecheckCols ? K - c0 : kRecheckCols;
+      const int T = (rows * cw + 31) >> 5;
+      int r = lane / cw, c = lane - (lane / cw) * cw;
+      for (int t0 = 0; t0 < T; t0 += 8) {
+        double vv[8];
+        int dst[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int32_t pr = __shfl_sync(0xffffffffu, p, r < 31 ? r : 31);
+          const bool take = t0 + u < T && r < rows;
+          dst[u] = take ? r * kRecheckLd + c : -1;
+          vv[u] = take ? __ldg(in.stats + (int64_t)pr * K + c0 + c) : 0.0;
+          c += 32;
+          while (c >= cw) {
+            c -= cw;
+            ++r;
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (dst[u] >= 0) S[dst[u]] = vv[u];
+      }
+      __syncwarp();
+      if (mine) {
+        const double* s = S + lane * kRecheckLd - c0;
+        for (int k = c0; k < c0 + cw; ++k) {
+          float sh, sl;
+          ok = split_trunc(s[k], sh, sl) && ok;
+          const float4 q = __ldg(gk + k);
+          const float x = __fsub_rn(q.x, sh);
+          const float y = __fsub_rn(q.y, sl);
+          const float dd = __fadd_rn(x, y);
+          const float term = __fmul_rn(dd, __fmul_rn(dd, q.z));
+          const float yk = __fsub_rn(term, comp);
+          const float t = __fadd_rn(acc, yk);
+          comp = __fsub_rn(__fsub_rn(t, acc), yk);
+          acc = t;
+        }
+      }
+      __syncwarp();
+    }
+    if (mine) {
+      const float e = __fmul_rn(acc, rK);
+      ok = ok && e == e && e < INFINITY;
+      if (ok) {
+        const double ed = (double)e;
+        v[i] = ed - approx_bound(ed) >= 10.0 ? 10.0 : ed;
+      } else {
+        v[i] = 0.0;
+        pos[atomicAdd(count, 1ull)] = (int32_t)i;
+      }
+    }
+  }
+}
+
+// E[pos[j]] = the FP64 error of the pair at that position, j < *count
+__global__ void recheck_list_kernel(DistInputs in, const int32_t* sp, const int32_t* sg, const int32_t* pos,
+                                    const unsigned long long* count, double* E) {
+  const int64_t m = (int64_t)*count;
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t i = pos[j];
+    E[i] = err_exact(in, sp[i], sg[i]);
+  }
+}
+
+// After the sort by the certified values: a position whose interval
+// [v - B(v), v + B(v)] overlaps a neighbour's in its gene's list, or holds
+// the clip value 10 or the gene's threshold (modes 0 and 2), is appended to pos
+// and its gene marked dirty.  Intervals have increasing ends along the sorted
+// list, so an interval that overlaps no neighbour overlaps no other; every
+// other pair is then in its exact place, and exact values for the listed
+// pairs plus one more sort give the exact order.
+__global__ void ambiguous_kernel(const int32_t* sg, const int64_t* goff, const double* E, int64_t n, int mode,
+                                 double eps_all, const double* eps_g, int32_t* pos, unsigned long long* count,
+                                 uint8_t* flag) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = E[i];
+    if (v != v) continue;  // NaN: exact (FP64 path), sorts last
+    const int64_t g = sg[i];
+    const int64_t a = goff[g], b = goff[g + 1];
+    const double B = approx_bound(v);
+    bool amb = fabs(v - 10.0) <= B;
+    if (i > a) {
+      const double w = E[i - 1];
+      if (w == w && w + approx_bound(w) >= v - B) amb = true;
+    }
+    if (i + 1 < b) {
+      const double w = E[i + 1];
+      if (w == w && v + B >= w - approx_bound(w)) amb = true;
+    }
+    if (mode != 1) {
+      const double thr = eps_g ? eps_g[g] : eps_all;
+      if (fabs(v - thr) <= B) amb = true;
+    }
+    flag[i] = amb ? 1 : 0;
+    if (amb) pos[atomicAdd(count, 1ull)] = (int32_t)i;
+  }
+}
+
+// After the FP64 values of the flagged positions are in: every maximal run
+// of consecutive flagged positions in a gene's list is sorted in place by
+// (err, p) (the neighbours of a run have intervals wholly below or above it,
+// so nothing else moves); a run longer than kRunSort marks its gene for a
+// full re-sort instead.
+constexpr int kRunSort = 64;
+
+__global__ void run_sort_kernel(const int32_t* sg, const int64_t* goff, const uint8_t* flag, int64_t n,
+                                int32_t* sp, double* E, int* dirty) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (!flag[i]) continue;
+    const int64_t g = sg[i];
+    const int64_t a = goff[g], b = goff[g + 1];
+    if (i > a && flag[i - 1]) continue;  // not the start of a run
+    int64_t e = i + 1;
+    while (e < b && flag[e] && e - i <= kRunSort) ++e;
+    if (e - i > kRunSort) {
+      dirty[g] = 1;
+      continue;
+    }
+    for (int64_t j = i + 1; j < e; ++j) {  // insertion sort
+      const double x = E[j];
+      const int32_t px = sp[j];
+      int64_t k = j - 1;
+      while (k >= i && key_less(x, px, E[k], sp[k])) {
+        E[k + 1] = E[k];
+        sp[k + 1] = sp[k];
+        --k;
+      }
+      E[k + 1] = x;
+      sp[k + 1] = px;
+    }
+  }
+}
+
 __global__ void dist_full_kernel(DistInputs in, double* err) {
   const int64_t n = in.P * in.G;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -300,9 +517,11 @@ __device__ void sort_segment_regs(int32_t* P, double* E, int m, int n2, uint64_t
   }
 }
 
-__global__ void __launch_bounds__(1024, 1) segsort_kernel(const int64_t* goff, int32_t* sp, double* se64) {
+__global__ void __launch_bounds__(1024, 1) segsort_kernel(const int64_t* goff, int32_t* sp, double* se64,
+                                                          const int* dirty) {
   extern __shared__ uint64_t sort_smem[];
   const int64_t g = blockIdx.x;
+  if (dirty && !dirty[g]) return;
   const int64_t base = goff[g];
   const int64_t n = goff[g + 1] - base;
   if (n <= 1) return;
@@ -344,10 +563,8 @@ __global__ void __launch_bounds__(1024, 1) segsort_kernel(const int64_t* goff, i
   }
 }
 
-cudaError_t launch_dist_group_recheck_sort(const DistInputs& in, const Cand* cand, int64_t n, int64_t* gcount,
-                                           int64_t* goff, unsigned long long* gcursor, int32_t* sp, int32_t* sg,
-                                           double* se64, cudaStream_t s) {
-  const int64_t G = in.G;
+cudaError_t launch_dist_group(const Cand* cand, int64_t n, int64_t G, int64_t* gcount, int64_t* goff,
+                              unsigned long long* gcursor, int32_t* sp, int32_t* sg, cudaStream_t s) {
   cudaError_t err = cudaMemsetAsync(gcount, 0, sizeof(int64_t) * (size_t)G, s);
   if (err) return err;
   err = cudaMemsetAsync(gcursor, 0, sizeof(unsigned long long) * (size_t)G, s);
@@ -357,28 +574,69 @@ cudaError_t launch_dist_group_recheck_sort(const DistInputs& in, const Cand* can
     gene_count_kernel<<<blocks, 256, 0, s>>>(cand, n, gcount);
   }
   scan_kernel<<<1, 1024, 0, s>>>(gcount, G, goff);
-  if (n <= 0) return cudaGetLastError();
-  {
+  if (n > 0) {
     int blocks = (int)((n + 255) / 256 < 65536 ? (n + 255) / 256 : 65536);
     scatter_kernel<<<blocks, 256, 0, s>>>(cand, n, goff, gcursor, sp, sg);
   }
-  {
-    const int64_t chunks = (n + 31) / 32;
-    const int64_t want = (chunks + kRecheckWarps - 1) / kRecheckWarps;
-    int blocks = (int)(want < 65536 ? want : 65536);
-    recheck_grouped_kernel<<<blocks, kRecheckWarps * 32, 0, s>>>(in, sp, sg, n, se64);
-  }
-  {
-    constexpr int smem = kSortSmem * (int)(sizeof(uint64_t) + sizeof(int32_t));
-    static bool attr = false;
-    if (!attr) {
-      err = cudaFuncSetAttribute(segsort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-      if (err) return err;
-      attr = true;
-    }
-    segsort_kernel<<<(unsigned)G, 1024, smem, s>>>(goff, sp, se64);
-  }
   return cudaGetLastError();
+}
+
+static cudaError_t launch_segsort(const int64_t* goff, int64_t G, int32_t* sp, double* se64, const int* dirty,
+                                  cudaStream_t s) {
+  constexpr int smem = kSortSmem * (int)(sizeof(uint64_t) + sizeof(int32_t));
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t err = cudaFuncSetAttribute(segsort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (err) return err;
+    attr = true;
+  }
+  segsort_kernel<<<(unsigned)G, 1024, smem, s>>>(goff, sp, se64, dirty);
+  return cudaGetLastError();
+}
+
+static int grouped_blocks(int64_t n) {
+  const int64_t chunks = (n + 31) / 32;
+  const int64_t want = (chunks + kRecheckWarps - 1) / kRecheckWarps;
+  return (int)(want < 65536 ? want : 65536);
+}
+
+cudaError_t launch_dist_group_recheck_sort(const DistInputs& in, const Cand* cand, int64_t n, int64_t* gcount,
+                                           int64_t* goff, unsigned long long* gcursor, int32_t* sp, int32_t* sg,
+                                           double* se64, cudaStream_t s) {
+  cudaError_t err = launch_dist_group(cand, n, in.G, gcount, goff, gcursor, sp, sg, s);
+  if (err || n <= 0) return err;
+  recheck_grouped_kernel<<<grouped_blocks(n), kRecheckWarps * 32, 0, s>>>(in, sp, sg, n, se64);
+  err = cudaGetLastError();
+  if (err) return err;
+  return launch_segsort(goff, in.G, sp, se64, nullptr, s);
+}
+
+cudaError_t launch_dist_group_certify_sort(const DistInputs& in, const Cand* cand, int64_t n, int mode, double eps,
+                                           const double* eps_g, int64_t* gcount, int64_t* goff,
+                                           unsigned long long* gcursor, int32_t* sp, int32_t* sg, double* se64,
+                                           float4* gt, int32_t* pos, uint8_t* flag,
+                                           unsigned long long* counts, int* dirty, cudaStream_t s) {
+  cudaError_t err = launch_dist_group(cand, n, in.G, gcount, goff, gcursor, sp, sg, s);
+  if (err) return err;
+  err = cudaMemsetAsync(counts, 0, 2 * sizeof(unsigned long long), s);
+  if (err) return err;
+  if (n <= 0) return cudaSuccess;
+  const int64_t gk = in.G * in.K;
+  ff_prep_genes_kernel<<<(unsigned)((gk + 255) / 256 < 4096 ? (gk + 255) / 256 : 4096), 256, 0, s>>>(in, gt);
+  const float rK = (float)(1.0 / (double)in.K);
+  approx_grouped_kernel<<<grouped_blocks(n), kRecheckWarps * 32, 0, s>>>(in, sp, sg, n, gt, rK, se64, pos,
+                                                                         counts);
+  const int list_blocks = 152 * 8;
+  recheck_list_kernel<<<list_blocks, 128, 0, s>>>(in, sp, sg, pos, counts, se64);
+  err = launch_segsort(goff, in.G, sp, se64, nullptr, s);
+  if (err) return err;
+  err = cudaMemsetAsync(dirty, 0, sizeof(int) * (size_t)in.G, s);
+  if (err) return err;
+  const int blocks = (int)((n + 255) / 256 < 65536 ? (n + 255) / 256 : 65536);
+  ambiguous_kernel<<<blocks, 256, 0, s>>>(sg, goff, se64, n, mode, eps, eps_g, pos, counts + 1, flag);
+  recheck_list_kernel<<<list_blocks, 128, 0, s>>>(in, sp, sg, pos, counts + 1, se64);
+  run_sort_kernel<<<blocks, 256, 0, s>>>(sg, goff, flag, n, sp, se64, dirty);
+  return launch_segsort(goff, in.G, sp, se64, dirty, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -386,7 +644,7 @@ cudaError_t launch_dist_group_recheck_sort(const DistInputs& in, const Cand* can
 // ---------------------------------------------------------------------------
 __global__ void accept_len_kernel(const int64_t* goff, const double* se64, int64_t G, int mode, double eps_all,
                                   const double* eps_g, int64_t k, const float* X, const float* b0, float b1,
-                                  int64_t* alen, int* fail) {
+                                  int64_t* alen, int* fail, bool approx) {
   const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= G) return;
   const double eps = eps_g ? eps_g[g] : eps_all;
@@ -419,7 +677,8 @@ __global__ void accept_len_kernel(const int64_t* goff, const double* se64, int64
     } else {
       // every particle with err <= L had a candidate-pass error <= X
       const double L = (double)x - ((double)b0[g] + (double)b1 * (double)x);
-      ok = E[k - 1] <= L;
+      // certified values: the k-th error may be above its stored value by its bound
+      ok = (approx ? E[k - 1] + approx_bound(E[k - 1]) : E[k - 1]) <= L;
     }
     if (!ok) fail[g] = 1;
   }
@@ -428,10 +687,10 @@ __global__ void accept_len_kernel(const int64_t* goff, const double* se64, int64
 
 cudaError_t launch_dist_accept_len(const int64_t* goff, const double* se64, int64_t G, int mode, double eps,
                                    const double* eps_g, int64_t k, const float* X, const float* b0, float b1,
-                                   int64_t* alen, int* fail, cudaStream_t s) {
+                                   int64_t* alen, int* fail, bool approx, cudaStream_t s) {
   if (G <= 0) return cudaSuccess;
   accept_len_kernel<<<(unsigned)((G + 127) / 128), 128, 0, s>>>(goff, se64, G, mode, eps, eps_g, k, X, b0, b1,
-                                                                alen, fail);
+                                                                alen, fail, approx);
   return cudaGetLastError();
 }
 

@@ -126,12 +126,22 @@ cudaError_t launch_dist_den(const DistInputs& in, double* den, double* rden, cud
 cudaError_t launch_dist_group_recheck_sort(const DistInputs& in, const Cand* cand, int64_t n, int64_t* gcount,
                                            int64_t* goff, unsigned long long* gcursor, int32_t* sp, int32_t* sg,
                                            double* se64, cudaStream_t s);
+// The same grouping and order with certified FP32 errors instead of FP64 ones
+// (selections that return indices only): se64 holds each pair's certified
+// value or, where that cannot decide the order or the threshold (mode 0/2:
+// eps or eps_g), its FP64 error.  Scratch: gt (G x K float4), pos and flag
+// (n), counts (2: pairs computed in FP64 before / after the sort), dirty (G).
+cudaError_t launch_dist_group_certify_sort(const DistInputs& in, const Cand* cand, int64_t n, int mode, double eps,
+                                           const double* eps_g, int64_t* gcount, int64_t* goff,
+                                           unsigned long long* gcursor, int32_t* sp, int32_t* sg, double* se64,
+                                           float4* gt, int32_t* pos, uint8_t* flag,
+                                           unsigned long long* counts, int* dirty, cudaStream_t s);
 // accepted prefix length per gene (mode 0: err <= eps; mode 1: the k smallest
 // finite errors) and, in mode 1, a failure flag when the candidate threshold
 // X[g] could have excluded a member of the top k.
 cudaError_t launch_dist_accept_len(const int64_t* goff, const double* se64, int64_t G, int mode, double eps,
                                    const double* eps_g, int64_t k, const float* X, const float* b0, float b1,
-                                   int64_t* alen, int* fail, cudaStream_t s);
+                                   int64_t* alen, int* fail, bool approx, cudaStream_t s);
 // compact the accepted prefixes: idx (1-based particle index + p_base) and err.
 cudaError_t launch_dist_compact(const int64_t* goff, const int32_t* sp, const double* se64, const int64_t* aoff,
                                 int64_t G, int64_t p_base, int64_t* idx, double* err, cudaStream_t s);

@@ -199,14 +199,17 @@ class Context:
     def select(self, data: np.ndarray, se: np.ndarray, stats: np.ndarray, mode: int, eps_or_q: float,
                families=None, errors: bool = True) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
         """Accepted particles per gene: (offsets[G+1], 1-based indices, errors);
-        errors=False leaves the FP64 errors on the device and returns None for
-        them (the reference's acceptance writes only the sorted indices)."""
+        errors=False returns None for them and lets the selection order the
+        pairs from certified FP32 errors, computing FP64 only where those
+        cannot decide (the reference's acceptance writes only the sorted
+        indices); the accepted sets and their order are the same."""
         d = np.ascontiguousarray(data, np.float64)
         e = np.ascontiguousarray(se, np.float64)
         s = np.ascontiguousarray(stats, np.float64)
         G, K = d.shape
         nf, f = self._fam(families, K)
         tot = C.c_int64()
+        self._check(self.lib.abc_set_select_errors(self.h, int(errors)))
         self._check(self.lib.abc_errors_select(self.h, ptr(d), ptr(e), G, K, nf, ptr(f, C.c_int32), ptr(s),
                                                s.shape[0], mode, float(eps_or_q), C.byref(tot)))
         return self._fetch(G, tot.value, errors)
@@ -221,7 +224,7 @@ class Context:
 
     def select_thr(self, data: np.ndarray, se: np.ndarray, stats: np.ndarray, thr: np.ndarray, families=None,
                    errors: bool = True):
-        """Acceptance with one threshold per gene."""
+        """Acceptance with one threshold per gene (errors: as in select)."""
         d = np.ascontiguousarray(data, np.float64)
         e = np.ascontiguousarray(se, np.float64)
         s = np.ascontiguousarray(stats, np.float64)
@@ -229,19 +232,21 @@ class Context:
         G, K = d.shape
         nf, f = self._fam(families, K)
         tot = C.c_int64()
+        self._check(self.lib.abc_set_select_errors(self.h, int(errors)))
         self._check(self.lib.abc_errors_select_thr(self.h, ptr(d), ptr(e), G, K, nf, ptr(f, C.c_int32), ptr(s),
                                                    s.shape[0], ptr(t), C.byref(tot)))
         return self._fetch(G, tot.value, errors)
 
     def select_device(self, data: np.ndarray, se: np.ndarray, d_stats: int, n: int, mode: int, eps_or_q: float = 0.0,
                       thr: np.ndarray | None = None, families=None, errors: bool = True):
-        """Acceptance with the statistics already in device memory."""
+        """Acceptance with the statistics already in device memory (errors: as in select)."""
         d = np.ascontiguousarray(data, np.float64)
         e = np.ascontiguousarray(se, np.float64)
         t = None if thr is None else np.ascontiguousarray(thr, np.float64)
         G, K = d.shape
         nf, f = self._fam(families, K)
         tot = C.c_int64()
+        self._check(self.lib.abc_set_select_errors(self.h, int(errors)))
         self._check(self.lib.abc_errors_select_device(self.h, ptr(d), ptr(e), G, K, nf, ptr(f, C.c_int32),
                                                       C.c_void_p(d_stats), n, mode, float(eps_or_q), ptr(t),
                                                       C.byref(tot)))

@@ -219,8 +219,17 @@ int abc_errors_select_device(abc_ctx* ctx, const double* data, const double* se,
                              int n_families, const int32_t* family_sizes, const double* d_stats,
                              int64_t n_particles, int mode, double eps_or_q, const double* thr,
                              int64_t* n_accepted_total);
+/* Whether selections keep the FP64 error of every accepted pair (1, the
+ * default) or return indices only (0).  With 0 the accepted sets and their
+ * order are the same, but the order is decided from certified FP32 errors
+ * (|e32 - err64| <= (1e-6 + 1e-12) e32 + 1e-12, derived in distance_fp64.cu)
+ * and FP64 is computed only for pairs those cannot place;
+ * abc_accept_fetch then requires err = NULL.  The reference's acceptance
+ * writes indices only (scripts/accepted_particles.jl:21-29). */
+int abc_set_select_errors(abc_ctx* ctx, int keep_errors);
 /* gene_offsets: G+1 entries; particle_idx: 1-based, n_accepted_total entries;
- * err: FP64 errors of the accepted pairs (may be NULL). */
+ * err: FP64 errors of the accepted pairs (may be NULL; must be NULL after a
+ * selection with abc_set_select_errors(ctx, 0)). */
 int abc_accept_fetch(abc_ctx* ctx, int64_t* gene_offsets, int64_t* particle_idx, double* err);
 /* CUDA graph mode for the simulation chain (setup -> work order -> SSA ->
  * capture + statistics) of abc_simulate_device, abc_simulate_batch_device

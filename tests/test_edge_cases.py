@@ -28,47 +28,50 @@ def _problem(P, G, K, seed):
     return data, se, stats
 
 
-def _check(ctx, orc, data, se, stats, sel, x):
-    off, idx, err = ctx.select(data, se, stats, sel, x, None)
+def _check(ctx, orc, data, se, stats, sel, x, errors=True):
+    off, idx, err = ctx.select(data, se, stats, sel, x, None, errors=errors)
     roff, ridx = orc.accept(orc.errors(data, se, stats, None), sel, x)
     assert np.array_equal(off, roff), (sel, x)
     assert np.array_equal(idx, ridx), (sel, x)
     return off
 
 
+@pytest.mark.parametrize("errors", (True, False))
 @pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("P,G,K", [(1, 1, 72), (1, 5, 53), (7, 1, 1), (129, 257, 72), (300, 3, 2)])
-def test_selection_shapes(Ctx, orc, mode, P, G, K):
+def test_selection_shapes(Ctx, orc, mode, P, G, K, errors):
     data, se, stats = _problem(P, G, K, P * 1000 + G + K)
     with Ctx(make_config("hour"), None) as ctx:
         ctx.set_distance_mode(mode)
         for sel, x in ((0, 4.8), (0, 0.0), (0, 10.0), (0, 25.0), (1, 1.0), (1, 0.3), (1, 1e-9)):
-            _check(ctx, orc, data, se, stats, sel, x)
+            _check(ctx, orc, data, se, stats, sel, x, errors)
 
 
+@pytest.mark.parametrize("errors", (True, False))
 @pytest.mark.parametrize("mode", MODES)
-def test_selection_nan_and_no_candidates(Ctx, orc, mode):
+def test_selection_nan_and_no_candidates(Ctx, orc, mode, errors):
     data, se, stats = _problem(400, 40, 24, 3)
     stats[::3] = np.nan                     # a third of the particles all-NaN
     data[5] = np.nan                        # a gene with NaN data
     with Ctx(make_config("hour"), None) as ctx:
         ctx.set_distance_mode(mode)
-        off = _check(ctx, orc, data, se, stats, 0, 1e-12)   # almost nothing accepted
-        _check(ctx, orc, data, se, stats, 1, 0.05)
-        _check(ctx, orc, data, se, stats, 1, 1.0)           # every non-NaN particle, NaN last
+        off = _check(ctx, orc, data, se, stats, 0, 1e-12, errors)   # almost nothing accepted
+        _check(ctx, orc, data, se, stats, 1, 0.05, errors)
+        _check(ctx, orc, data, se, stats, 1, 1.0, errors)           # every non-NaN particle, NaN last
         all_nan = np.full_like(stats, np.nan)
-        off = _check(ctx, orc, data, se, all_nan, 1, 0.1)
+        off = _check(ctx, orc, data, se, all_nan, 1, 0.1, errors)
         assert off[-1] == 0
 
 
+@pytest.mark.parametrize("errors", (True, False))
 @pytest.mark.parametrize("mode", MODES)
-def test_selection_per_gene_extreme_thresholds(Ctx, orc, mode):
+def test_selection_per_gene_extreme_thresholds(Ctx, orc, mode, errors):
     data, se, stats = _problem(500, 6, 16, 8)
     thr = np.array([-1.0, 0.0, 1e-300, 10.0, 50.0, 2.0])
     err = orc.errors(data, se, stats, None)
     with Ctx(make_config("hour"), None) as ctx:
         ctx.set_distance_mode(mode)
-        off, idx, _ = ctx.select_thr(data, se, stats, thr, None)
+        off, idx, _ = ctx.select_thr(data, se, stats, thr, None, errors=errors)
     want_off, want_idx = [0], []
     for g in range(6):
         _, i = orc.accept(err[:, g:g + 1], 0, thr[g])
@@ -115,8 +118,9 @@ def test_data_stats_silent_and_minimal_cells(Ctx, orc):
     assert (st[1][:20] == 0).all() and (st[1][20:] == 0).all()
 
 
+@pytest.mark.parametrize("errors", (True, False))
 @pytest.mark.parametrize("mode", (0, 2))
-def test_selection_sort_paths_and_ties(Ctx, orc, mode):
+def test_selection_sort_paths_and_ties(Ctx, orc, mode, errors):
     """Per-gene lists of every sort size class (one entry per thread up to
     1,024 entries, 2, 4 and 8 per thread, and the global-memory network above
     8,192) with exact error ties (duplicated particles), ordered by (err, index)."""
@@ -126,4 +130,15 @@ def test_selection_sort_paths_and_ties(Ctx, orc, mode):
     with Ctx(make_config("hour"), None) as ctx:
         ctx.set_distance_mode(mode)
         for q in (0.0005, 0.01, 0.05, 0.1, 0.2, 0.4, 1.0):
-            _check(ctx, orc, data, se, stats, 1, q)
+            _check(ctx, orc, data, se, stats, 1, q, errors)
+        for eps in (0.5, 2.0):
+            _check(ctx, orc, data, se, stats, 0, eps, errors)
+
+
+def test_indices_only_selection_refuses_error_fetch(Ctx):
+    data, se, stats = _problem(200, 4, 16, 9)
+    with Ctx(make_config("hour"), None) as ctx:
+        off, idx, err = ctx.select(data, se, stats, 1, 0.1, None, errors=False)
+        assert err is None and off[-1] == 4 * 20
+        with pytest.raises(RuntimeError, match="ABC_ERR_STATE"):
+            ctx._fetch(4, int(off[-1]), True)
