@@ -344,33 +344,100 @@ __device__ __forceinline__ void split_tf32f(float x, float& hi, float& lo) {
 // s^2 = fl(s s): both within 2^-23 relative, inside the bound's rounding terms).
 // One warp per row, rows strided over the grid; the overflow monitors are
 // reduced per warp before one atomic each.
+// RN32(x) from the bit fields of x (integer operations; GB300 runs FP64 -> FP32
+// conversions on its narrow FP64 pipe): the top 23 stored significand bits,
+// rounded to nearest even on bit 28 and the sticky bits 0-27, with the carry
+// rippling into the exponent (and to infinity above the float range); the
+// conversion instruction only for results below the normal float range and
+// for zero, infinity and NaN.  Identical to (float)x.
+__device__ __forceinline__ float rn32_bits(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned mag = hi & 0x7fffffffu;
+  const unsigned e = mag >> 20;
+  if (e - 897u > 253u) return (float)x;  // e outside [897, 1150]
+  unsigned f = (hi & 0x80000000u) | ((mag - (896u << 20)) << 3) | (lo >> 29);
+  const unsigned rb = (lo >> 28) & 1u, sticky = lo & 0x0fffffffu;
+  f += rb & ((sticky != 0u) | (f & 1u));
+  return __uint_as_float(f);
+}
+
+// One warp per batch of R consecutive rows (R x K <= 32 kPrepLoads values): all
+// of the batch's loads are issued before any conversion, so each warp keeps
+// up to kPrepLoads 256-byte requests in flight (HBM needs that many bytes in
+// flight per SM to stream at full rate).
+constexpr int kPrepLoads = 16;
+
 __global__ void tc_prep_rows_kernel(const double* stats, int64_t P, int K, int KA, int NH, float* A,
                                     unsigned* flags) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   const int64_t ld = (int64_t)NH * KA;
+  const int R = K <= 32 * kPrepLoads ? (32 * kPrepLoads) / K < 4 ? (32 * kPrepLoads) / K : 4 : 1;
   unsigned inf = 0, mx = 0;
-  for (int64_t p = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); p < P; p += warps) {
-    const double* srow = stats + p * K;
-    float* arow = A + p * ld;
-    for (int k = lane; k < K; k += 32) {
-      const float sv = (float)srow[k];
-      const float s2 = sv * sv;
-      float h1, l1, h2, l2;
-      split_tf32f(sv, h1, l1);
-      split_tf32f(s2, h2, l2);
-      arow[k] = h1;
-      arow[K + k] = h2;
-      if (NH == 2) {
-        arow[KA + k] = l1;
-        arow[KA + K + k] = l2;
+  for (int64_t p0 = ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * R; p0 < P; p0 += warps * R) {
+    const int rows = P - p0 < R ? (int)(P - p0) : R;
+    if (K > 32 * kPrepLoads) {  // very wide rows: one row at a time
+      const double* srow = stats + p0 * K;
+      float* arow = A + p0 * ld;
+      for (int k = lane; k < K; k += 32) {
+        const float sv = rn32_bits(srow[k]);
+        const float s2 = sv * sv;
+        float h1, l1, h2, l2;
+        split_tf32f(sv, h1, l1);
+        split_tf32f(s2, h2, l2);
+        arow[k] = h1;
+        arow[K + k] = h2;
+        if (NH == 2) {
+          arow[KA + k] = l1;
+          arow[KA + K + k] = l2;
+        }
+        if (fabsf(sv) == INFINITY || fabsf(s2) == INFINITY) inf = 1u;
+        if (s2 == s2) mx = max(mx, __float_as_uint(s2));
       }
-      if (fabsf(sv) == INFINITY || fabsf(s2) == INFINITY) inf = 1u;
-      if (s2 == s2) mx = max(mx, __float_as_uint(s2));
+    } else {
+      // flat index f = lane + 32 t over rows x K, (r, k) = divmod(f, K)
+      const int n = rows * K;
+      double v[kPrepLoads];
+      {
+        const double* src = stats + p0 * K;  // rows are contiguous
+#pragma unroll
+        for (int t = 0; t < kPrepLoads; ++t) {
+          const int f = lane + 32 * t;
+          v[t] = f < n ? __ldg(src + f) : 0.0;
+        }
+      }
+      int r = lane / K, k = lane - (lane / K) * K;
+#pragma unroll
+      for (int t = 0; t < kPrepLoads; ++t) {
+        if (lane + 32 * t < n) {
+          const float sv = rn32_bits(v[t]);
+          const float s2 = sv * sv;
+          float h1, l1, h2, l2;
+          split_tf32f(sv, h1, l1);
+          split_tf32f(s2, h2, l2);
+          float* arow = A + (p0 + r) * ld;
+          arow[k] = h1;
+          arow[K + k] = h2;
+          if (NH == 2) {
+            arow[KA + k] = l1;
+            arow[KA + K + k] = l2;
+          }
+          if (fabsf(sv) == INFINITY || fabsf(s2) == INFINITY) inf = 1u;
+          if (s2 == s2) mx = max(mx, __float_as_uint(s2));
+        }
+        k += 32;
+        while (k >= K) {
+          k -= K;
+          ++r;
+        }
+      }
     }
-    for (int k = 2 * K + lane; k < KA; k += 32) {
-      arow[k] = 0.0f;
-      if (NH == 2) arow[KA + k] = 0.0f;
+    for (int rr = 0; rr < rows; ++rr) {
+      float* arow = A + (p0 + rr) * ld;
+      for (int k = 2 * K + lane; k < KA; k += 32) {
+        arow[k] = 0.0f;
+        if (NH == 2) arow[KA + k] = 0.0f;
+      }
     }
   }
   inf = __reduce_or_sync(0xffffffffu, inf);
@@ -509,7 +576,7 @@ cudaError_t launch_tc_prep(const DistInputs& in, int nh, double beta, float* A, 
                            float* b0, unsigned* flags, cudaStream_t s) {
   const int KA = tc_ka(in.K);
   if (in.P > 0) {
-    const int64_t blocks = (in.P + 7) / 8 < 8192 ? (in.P + 7) / 8 : 8192;
+    const int64_t blocks = (in.P + 31) / 32 < 8192 ? (in.P + 31) / 32 : 8192;
     tc_prep_rows_kernel<<<(unsigned)blocks, 256, 0, s>>>(in.stats, in.P, in.K, KA, nh, A, flags);
   }
   if (in.G > 0)
