@@ -50,6 +50,23 @@ __device__ __forceinline__ double div_rn(double a, double b, double y) {
   }
   return a / b;
 }
+
+// RN32(x) from the bit fields of x (integer operations; GB300 runs FP64 -> FP32
+// conversions on its narrow FP64 pipe): the top 23 stored significand bits,
+// rounded to nearest even on bit 28 and the sticky bits 0-27, with the carry
+// rippling into the exponent (and to infinity above the float range); the
+// conversion instruction only for results below the normal float range and
+// for zero, infinity and NaN.  Identical to (float)x.
+__device__ __forceinline__ float rn32_bits(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned mag = hi & 0x7fffffffu;
+  const unsigned e = mag >> 20;
+  if (e - 897u > 253u) return (float)x;  // e outside [897, 1150]
+  unsigned f = (hi & 0x80000000u) | ((mag - (896u << 20)) << 3) | (lo >> 29);
+  const unsigned rb = (lo >> 28) & 1u, sticky = lo & 0x0fffffffu;
+  f += rb & ((sticky != 0u) | (f & 1u));
+  return __uint_as_float(f);
+}
 #endif
 
 constexpr int kDistTile = 128;  // particles and genes per CTA tile

@@ -31,6 +31,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "distance.cuh"
 #include "kernels.h"
 #include "tcgen05.cuh"
 
@@ -344,23 +345,6 @@ __device__ __forceinline__ void split_tf32f(float x, float& hi, float& lo) {
 // s^2 = fl(s s): both within 2^-23 relative, inside the bound's rounding terms).
 // One warp per row, rows strided over the grid; the overflow monitors are
 // reduced per warp before one atomic each.
-// RN32(x) from the bit fields of x (integer operations; GB300 runs FP64 -> FP32
-// conversions on its narrow FP64 pipe): the top 23 stored significand bits,
-// rounded to nearest even on bit 28 and the sticky bits 0-27, with the carry
-// rippling into the exponent (and to infinity above the float range); the
-// conversion instruction only for results below the normal float range and
-// for zero, infinity and NaN.  Identical to (float)x.
-__device__ __forceinline__ float rn32_bits(double x) {
-  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
-  const unsigned mag = hi & 0x7fffffffu;
-  const unsigned e = mag >> 20;
-  if (e - 897u > 253u) return (float)x;  // e outside [897, 1150]
-  unsigned f = (hi & 0x80000000u) | ((mag - (896u << 20)) << 3) | (lo >> 29);
-  const unsigned rb = (lo >> 28) & 1u, sticky = lo & 0x0fffffffu;
-  f += rb & ((sticky != 0u) | (f & 1u));
-  return __uint_as_float(f);
-}
-
 // One warp per batch of R consecutive rows (R x K <= 32 kPrepLoads values): all
 // of the batch's loads are issued before any conversion, so each warp keeps
 // up to kPrepLoads 256-byte requests in flight (HBM needs that many bytes in

@@ -130,6 +130,24 @@ def test_many_tiles_topq_and_segment_growth(Ctx, orc, mode):
     assert (np.abs(e32 - E) <= b0[None, :] + b1 * E).all()
 
 
+@pytest.mark.gpu
+def test_rn32_bits_matches_conversion(tmp_path):
+    """The operand preparation of the tensor-core pass rounds FP64 to FP32 on
+    the bit fields (rn32_bits); it must equal the conversion instruction bit
+    for bit, here on 2 x 2^31 patterns including every exponent of the float
+    range and its edges, ties and near-ties at the rounding position."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    so = tmp_path / "librn32.so"
+    subprocess.run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
+                    "-shared", "-Xcompiler", "-fPIC", os.path.join(root, "tests", "gpu_helpers", "rn32.cu"),
+                    "-o", str(so)], check=True)
+    lib = C.CDLL(str(so))
+    for seed in (3, 0x5EED):
+        bad, first = C.c_ulonglong(0), C.c_ulonglong(0)
+        assert lib.rn32_check(C.c_ulonglong(1 << 31), C.c_ulonglong(seed), C.byref(bad), C.byref(first)) == 0
+        assert bad.value == 0, hex(first.value)
+
+
 def test_markstein_division_matches_ieee(tmp_path):
     """The FP64 recheck divides through div_rn (three operations from RN(1/b));
     it must equal the IEEE quotient bit for bit, here on 2^30 operand pairs
