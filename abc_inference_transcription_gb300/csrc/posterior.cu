@@ -25,92 +25,11 @@ __device__ __forceinline__ void quantile_pos(int64_t n, double p, int64_t& j, do
   gmm = gmm < 0.0 ? 0.0 : (gmm > 1.0 ? 1.0 : gmm);
 }
 
-// quantile from the order statistics a = v[j - 1], b = v[j] (v[0] twice for n = 1)
+// quantile from the order statistics a = v[j - 1], b = v[j] of the sorted
+// values (v[0] twice for n = 1)
 __device__ __forceinline__ double quantile_mix(double a, double b, double gmm) {
   if (isfinite(a) && isfinite(b)) return a + gmm * (b - a);
   return (1.0 - gmm) * a + gmm * b;
-}
-
-__device__ double quantile_sorted(const double* v, int64_t n, double p) {
-  int64_t j;
-  double gmm;
-  quantile_pos(n, p, j, gmm);
-  const double a = n == 1 ? v[0] : v[j - 1];
-  const double b = n == 1 ? v[0] : v[j];
-  return quantile_mix(a, b, gmm);
-}
-
-// One thread per gene.  counts[g][m] = accepted particles of model group m.
-// No acceptance: zeros; one group with acceptances: that group 1, 1, 1 (the
-// `which` branch of model_probs.jl:41-48); otherwise l / sum(l) and n_boot
-// bootstrap resamples of the sum(l) model labels (a multinomial draw, made
-// as conditional binomials from the (bootstrap, gene) Philox stream), with
-// quantiles 1 - alpha and alpha of the resampled proportions.
-__global__ void model_probs_kernel(const int64_t* counts, int64_t G, int M, int n_boot, double alpha,
-                                   uint64_t seed, double* prob, double* lb, double* ub, double* boot) {
-  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= G) return;
-  const int64_t* l = counts + g * M;
-  double* P = prob + g * M;
-  double* LB = lb + g * M;
-  double* UB = ub + g * M;
-  int64_t L = 0;
-  int nz = 0, which = -1;
-  for (int m = 0; m < M; ++m) {
-    L += l[m];
-    if (l[m] > 0) {
-      nz++;
-      which = m;
-    }
-    P[m] = 0.0;
-    LB[m] = 0.0;
-    UB[m] = 0.0;
-  }
-  if (L == 0) return;
-  if (nz == 1) {
-    P[which] = 1.0;
-    LB[which] = 1.0;
-    UB[which] = 1.0;
-    return;
-  }
-  for (int m = 0; m < M; ++m) P[m] = (double)l[m] / (double)L;
-  double* bv = boot + g * (int64_t)M * n_boot;
-  for (int b = 0; b < n_boot; ++b) {
-    Rng r;
-    rng_init(r, seed, ST_AUX, (uint32_t)b, (uint32_t)g);
-    int64_t nrem = L, lrem = L;
-    for (int m = 0; m < M; ++m) {
-      int64_t x;
-      if (m == M - 1 || lrem == l[m]) x = nrem;
-      else if (l[m] == 0 || nrem == 0) x = 0;
-      else x = binomial(r, nrem, (double)l[m] / (double)lrem);
-      nrem -= x;
-      lrem -= l[m];
-      bv[(int64_t)m * n_boot + b] = (double)x / (double)L;
-    }
-  }
-  for (int m = 0; m < M; ++m) {
-    double* v = bv + (int64_t)m * n_boot;
-    for (int i = 1; i < n_boot; ++i) {  // insertion sort of n_boot values
-      const double x = v[i];
-      int j = i - 1;
-      while (j >= 0 && v[j] > x) {
-        v[j + 1] = v[j];
-        --j;
-      }
-      v[j + 1] = x;
-    }
-    LB[m] = quantile_sorted(v, n_boot, 1.0 - alpha);
-    UB[m] = quantile_sorted(v, n_boot, alpha);
-  }
-}
-
-cudaError_t launch_model_probs(const int64_t* counts, int64_t G, int M, int n_boot, double alpha, uint64_t seed,
-                               double* prob, double* lb, double* ub, double* boot, cudaStream_t s) {
-  if (G <= 0) return cudaSuccess;
-  model_probs_kernel<<<(unsigned)((G + 127) / 128), 128, 0, s>>>(counts, G, M, n_boot, alpha, seed, prob, lb, ub,
-                                                                 boot);
-  return cudaGetLastError();
 }
 
 // scratch[c][aoff[g] + i] = theta[idx - 1][c] for the accepted particles of gene g
@@ -256,6 +175,91 @@ __global__ void __launch_bounds__(kSelThreads) post_select_kernel(const int64_t*
     const uint64_t k = block_select(K, n, ranks[r], sh);
     if (threadIdx.x == 0) out[r] = dkey_inv(k);
   }
+}
+
+// One block per gene.  counts[g][m] = accepted particles of model group m.
+// No acceptance: zeros; one group with acceptances: that group 1, 1, 1 (the
+// `which` branch of model_probs.jl:41-48); otherwise l / sum(l) and n_boot
+// bootstrap resamples of the sum(l) model labels (a multinomial draw, made
+// as conditional binomials from the (bootstrap, gene) Philox stream; the
+// block's threads take the resamples), with quantiles 1 - alpha and alpha of
+// the resampled proportions from the order statistics they read
+// (block_select on order-preserving keys; keys: G x M x n_boot scratch).
+__global__ void __launch_bounds__(kSelThreads) model_probs_kernel(const int64_t* counts, int64_t G, int M,
+                                                                  int n_boot, double alpha, uint64_t seed,
+                                                                  double* prob, double* lb, double* ub,
+                                                                  uint64_t* keys) {
+  __shared__ SelShared sh;
+  __shared__ long long s_L;
+  __shared__ int s_nz;
+  const int64_t g = blockIdx.x;
+  const int64_t* l = counts + g * M;
+  double* P = prob + g * M;
+  double* LB = lb + g * M;
+  double* UB = ub + g * M;
+  if (threadIdx.x == 0) {
+    int64_t L = 0;
+    int nz = 0, which = -1;
+    for (int m = 0; m < M; ++m) {
+      L += l[m];
+      if (l[m] > 0) {
+        nz++;
+        which = m;
+      }
+      P[m] = 0.0;
+      LB[m] = 0.0;
+      UB[m] = 0.0;
+    }
+    if (L > 0 && nz == 1) {
+      P[which] = 1.0;
+      LB[which] = 1.0;
+      UB[which] = 1.0;
+    }
+    s_L = L;
+    s_nz = nz;
+  }
+  __syncthreads();
+  const int64_t L = s_L;
+  if (L == 0 || s_nz == 1) return;
+  for (int m = threadIdx.x; m < M; m += blockDim.x) P[m] = (double)l[m] / (double)L;
+  uint64_t* kv = keys + g * (int64_t)M * n_boot;
+  for (int b = threadIdx.x; b < n_boot; b += blockDim.x) {
+    Rng r;
+    rng_init(r, seed, ST_AUX, (uint32_t)b, (uint32_t)g);
+    int64_t nrem = L, lrem = L;
+    for (int m = 0; m < M; ++m) {
+      int64_t x;
+      if (m == M - 1 || lrem == l[m]) x = nrem;
+      else if (l[m] == 0 || nrem == 0) x = 0;
+      else x = binomial(r, nrem, (double)l[m] / (double)lrem);
+      nrem -= x;
+      lrem -= l[m];
+      kv[(int64_t)m * n_boot + b] = dkey((double)x / (double)L);
+    }
+  }
+  __syncthreads();
+  int64_t jl, jh;
+  double gl, gh;
+  quantile_pos(n_boot, 1.0 - alpha, jl, gl);
+  quantile_pos(n_boot, alpha, jh, gh);
+  const int64_t ranks[4] = {n_boot == 1 ? 0 : jl - 1, n_boot == 1 ? 0 : jl, n_boot == 1 ? 0 : jh - 1,
+                            n_boot == 1 ? 0 : jh};
+  for (int m = 0; m < M; ++m) {
+    double q[4];
+    for (int r = 0; r < 4; ++r) q[r] = dkey_inv(block_select(kv + (int64_t)m * n_boot, n_boot, ranks[r], sh));
+    if (threadIdx.x == 0) {
+      LB[m] = quantile_mix(q[0], q[1], gl);
+      UB[m] = quantile_mix(q[2], q[3], gh);
+    }
+  }
+}
+
+cudaError_t launch_model_probs(const int64_t* counts, int64_t G, int M, int n_boot, double alpha, uint64_t seed,
+                               double* prob, double* lb, double* ub, double* boot, cudaStream_t s) {
+  if (G <= 0) return cudaSuccess;
+  model_probs_kernel<<<(unsigned)G, kSelThreads, 0, s>>>(counts, G, M, n_boot, alpha, seed, prob, lb, ub,
+                                                          reinterpret_cast<uint64_t*>(boot));
+  return cudaGetLastError();
 }
 
 __global__ void post_summary_kernel(const int64_t* aoff, const int64_t* idx, const double* theta, int64_t ld,
