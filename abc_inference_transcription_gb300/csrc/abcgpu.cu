@@ -1309,6 +1309,8 @@ int abc_data_stats(abc_ctx* c, const int32_t* u, const int32_t* l, int64_t G, in
   if (!c->cells_set) return fail(c, ABC_ERR_STATE, "abc_data_stats: call abc_set_cells first");
   if (!u || !l || !stats_out || G < 0 || n_boot < 0 || n_boot > 10000 || (se_out && n_boot < 2))
     return fail(c, ABC_ERR_INVALID, "abc_data_stats: bad arguments (standard errors need n_boot >= 2)");
+  if (c->C > data_stats_max_cells(c->cfg.n_ages, c->cfg.n_conds))
+    return fail(c, ABC_ERR_INVALID, "abc_data_stats: too many cells for the per-gene shared-memory table");
   const int64_t C = c->C;
   for (int64_t i = 0; i < G * C; ++i)
     if (u[i] < 0 || l[i] < 0 || u[i] > (1 << 20) || l[i] > (1 << 20))

@@ -188,6 +188,8 @@ struct DataStatsArgs {
   double* out;                // [G][n_boot + 1][K]
 };
 cudaError_t launch_data_stats(const DataStatsArgs& a, double* se, cudaStream_t s);
+// cells that fit the per-gene shared-memory table of launch_data_stats
+int64_t data_stats_max_cells(int n_ages, int n_conds);
 
 // model probabilities with bootstrap intervals and per-gene posterior summaries (posterior.cu)
 cudaError_t launch_model_probs(const int64_t* counts, int64_t G, int M, int n_boot, double alpha, uint64_t seed,
