@@ -20,6 +20,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "distance.cuh"
 #include "kernels.h"
 #include "model.cuh"
 
@@ -47,6 +48,14 @@ __device__ __forceinline__ double sample_cov(unsigned long long n, unsigned long
                                              unsigned long long sxy) {
   const __int128 num = (__int128)n * (__int128)sxy - (__int128)sx * (__int128)sy;
   return i128_to_double(num) / ((double)n * (double)(n - 1));
+}
+
+// the same with the denominator d2 = n (n - 1) and r2 = RN(1 / d2) given: the
+// quotient through div_rn (correctly rounded, equal to the IEEE division)
+__device__ __forceinline__ double sample_cov_r(unsigned long long n, unsigned long long sx, unsigned long long sy,
+                                               unsigned long long sxy, double d2, double r2) {
+  const __int128 num = (__int128)n * (__int128)sxy - (__int128)sx * (__int128)sy;
+  return div_rn(i128_to_double(num), d2, r2);
 }
 
 // Exact 64-bit sums from 32-bit shared-memory atomics (the 64-bit form is far
@@ -178,11 +187,14 @@ __global__ void data_stats_kernel(DataStatsArgs a, int64_t g0, int64_t ng, const
       if (S[0] == 0) {
         m1[ag] = m2[ag] = v1[ag] = v2[ag] = c12[ag] = 0.0;
       } else {
-        m1[ag] = (double)S[1] / (double)S[0];
-        m2[ag] = (double)S[2] / (double)S[0];
-        v1[ag] = sample_cov(S[0], S[1], S[1], S[3]);
-        v2[ag] = sample_cov(S[0], S[2], S[2], S[4]);
-        c12[ag] = sample_cov(S[0], S[1], S[2], S[5]);
+        // two reciprocals per group instead of five divisions
+        const double nd = (double)S[0], rn = 1.0 / nd;
+        m1[ag] = div_rn((double)S[1], nd, rn);
+        m2[ag] = div_rn((double)S[2], nd, rn);
+        const double d2 = nd * (double)(S[0] - 1), r2 = 1.0 / d2;
+        v1[ag] = sample_cov_r(S[0], S[1], S[1], S[3], d2, r2);
+        v2[ag] = sample_cov_r(S[0], S[2], S[2], S[4], d2, r2);
+        c12[ag] = sample_cov_r(S[0], S[1], S[2], S[5], d2, r2);
       }
     }
     // ratio of means (get_cond_specific_ratios)
