@@ -172,6 +172,7 @@ static DevCfg make_dcfg(const abc_config* cfg) {
   d.pulse_stat = cfg->pulse_stat_cond;
   d.chase_stat = cfg->chase_stat_cond;
   d.npar = 0;
+  dcfg_set_grid(d);
   return d;
 }
 

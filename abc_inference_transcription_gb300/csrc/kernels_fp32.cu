@@ -1,6 +1,7 @@
 // kernels_fp32.cu — production SSA launch: FP32 propensities, waiting times
 // and channel selection with fast intrinsics; compensated FP32 interval clock
-// re-anchored in FP64 at every breakpoint.  Built with FMA contraction on.
+// re-anchored at every breakpoint (integer breakpoint grid, or FP64 when the
+// configuration's times are not on one).  Built with FMA contraction on.
 #include "kernels.h"
 #include "ssa_fp32.cuh"
 
@@ -10,12 +11,12 @@ namespace abc {
 // 10 resident blocks of 128 threads per SM.
 static const int kVariantMinBlocks[kSsaVariants] = {8, 10};
 
-template <bool SPLICE>
+template <bool SPLICE, bool GRID>
 static cudaError_t launch_variant(const SsaArgs& b, int variant, int grid, cudaStream_t s) {
   if (variant == 1)
-    ssa_kernel_f32<SPLICE, 10><<<grid, 128, 0, s>>>(b);
+    ssa_kernel_f32<SPLICE, 10, GRID><<<grid, 128, 0, s>>>(b);
   else
-    ssa_kernel_f32<SPLICE, 8><<<grid, 128, 0, s>>>(b);
+    ssa_kernel_f32<SPLICE, 8, GRID><<<grid, 128, 0, s>>>(b);
   return cudaGetLastError();
 }
 
@@ -28,15 +29,20 @@ cudaError_t launch_ssa_fp32(const SsaArgs& a, int grid, cudaStream_t s, int vari
     k0 += 0x9E3779B9u;
     k1 += 0xBB67AE85u;
   }
-  return a.cfg.splicing ? launch_variant<true>(b, variant, grid, s) : launch_variant<false>(b, variant, grid, s);
+  // integer breakpoints when the configuration's times lie on a power-of-two grid
+  if (a.cfg.grid_ok)
+    return a.cfg.splicing ? launch_variant<true, true>(b, variant, grid, s)
+                          : launch_variant<false, true>(b, variant, grid, s);
+  return a.cfg.splicing ? launch_variant<true, false>(b, variant, grid, s)
+                        : launch_variant<false, false>(b, variant, grid, s);
 }
 
 int ssa_blocks_per_sm_fp32(int variant) {
   int n = 0;
   if (variant == 1)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssa_kernel_f32<false, 10>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssa_kernel_f32<false, 10, true>, 128, 0);
   else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssa_kernel_f32<false, 8>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssa_kernel_f32<false, 8, true>, 128, 0);
   return n > 0 ? n : kVariantMinBlocks[variant < 0 || variant >= kSsaVariants ? 0 : variant];
 }
 

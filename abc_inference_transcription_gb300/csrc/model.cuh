@@ -6,6 +6,7 @@
 //   statistics    abc_sim                               scripts/abc_simulation.jl:23-46
 //                 weighted_cov                          scripts/data_summary_statistics.jl:179-181
 #pragma once
+#include <cmath>
 #include "common.cuh"
 
 namespace abc {
@@ -22,7 +23,45 @@ struct DevCfg {
   double chase[kMaxConds];
   int64_t event_cap;
   int n_steps, n_ages, n_conds, splicing, scaling_column, pulse_stat, chase_stat, npar;
+  // Breakpoint grid (dcfg_set_grid): when every time above is an integer
+  // multiple of quantum = 2^-e, the same times in quanta, so that the
+  // production SSA places breakpoints with exact integer arithmetic.
+  int grid_ok;
+  float quantum;
+  int32_t t0_q, cycle_q, step_q;
+  int32_t ages_q[kMaxAges], pulse_q[kMaxConds], chase_q[kMaxConds];
 };
+
+// Host: find the coarsest quantum 2^-e (e = 0..20) of which t0, the cycle, the
+// age step, every age, pulse and chase are exact integer multiples, with every
+// breakpoint time (at most a few cycles) below 2^30 quanta; grid_ok = 0 if none.
+inline void dcfg_set_grid(DevCfg& d) {
+  d.grid_ok = 0;
+  double horizon = std::fabs(d.t0) + 2.0 * d.cycle;
+  for (int a = 0; a < d.n_ages; ++a) horizon = std::fmax(horizon, std::fabs(d.ages[a]) + std::fabs(d.t0));
+  for (int e = 0; e <= 20; ++e) {
+    const double sc = std::ldexp(1.0, e);
+    auto ok = [&](double t) {
+      const double x = t * sc;
+      return x == std::floor(x) && std::fabs(x) < 1073741824.0;
+    };
+    bool all = ok(d.t0) && ok(d.cycle) && ok(d.step_len) && horizon * sc < 1073741824.0;
+    for (int a = 0; a < d.n_ages && all; ++a) all = ok(d.ages[a]);
+    for (int j = 0; j < d.n_conds && all; ++j) all = ok(d.pulse[j]) && ok(d.chase[j]);
+    if (!all) continue;
+    d.grid_ok = 1;
+    d.quantum = (float)std::ldexp(1.0, -e);
+    d.t0_q = (int32_t)(d.t0 * sc);
+    d.cycle_q = (int32_t)(d.cycle * sc);
+    d.step_q = (int32_t)(d.step_len * sc);
+    for (int a = 0; a < kMaxAges; ++a) d.ages_q[a] = a < d.n_ages ? (int32_t)(d.ages[a] * sc) : 0;
+    for (int j = 0; j < kMaxConds; ++j) {
+      d.pulse_q[j] = j < d.n_conds ? (int32_t)(d.pulse[j] * sc) : 0;
+      d.chase_q[j] = j < d.n_conds ? (int32_t)(d.chase[j] * sc) : 0;
+    }
+    return;
+  }
+}
 
 // FP64 particle record (rates are 10^theta).
 struct PRec {

@@ -184,6 +184,7 @@ extern "C" int abc_simulate_noalloc(const abc_config* cfg, int model, int64_t n_
   d.pulse_stat = cfg->pulse_stat_cond;
   d.chase_stat = cfg->chase_stat_cond;
   d.npar = 5 + (model >= 3 ? cfg->n_steps - 1 : 0) + d.splicing + d.scaling_column;
+  dcfg_set_grid(d);
 
   SetupArgs sa;
   sa.cfg = d;

@@ -30,7 +30,8 @@ namespace abc {
 constexpr float kCountLimitF = 8388608.0f;  // 2^23
 
 struct LaneF {
-  double t_bp;          // start of the current interval
+  double t_bp;          // start of the current interval (FP64 breakpoints)
+  int tq;               // the same in quanta of the breakpoint grid (integer breakpoints)
   float el, comp;       // elapsed time in the interval, Kahan compensation
   float len;            // interval length
   float ph0;            // cycle phase at the interval start
@@ -60,11 +61,33 @@ __device__ __forceinline__ double f32_tend(const LaneF& s, const DevCfg& cfg) {
   return te;
 }
 
+// the same on the integer breakpoint grid (DevCfg::grid_ok): every time is
+// an exact integer number of quanta, so the interval end, its length and the
+// cycle phase equal the FP64 ones bit for bit, without FP64 instructions
+__device__ __forceinline__ int q_tend(const LaneF& s, const DevCfg& cfg) {
+  const int cs = cfg.t0_q + s.cyc * cfg.cycle_q;
+  int te = (s.k == cfg.n_steps - 1) ? cs + cfg.cycle_q : cs + (s.k + 1) * cfg.step_q;
+  const int tobs = cfg.ages_q[s.a];
+  const int texp = (tobs - cfg.pulse_q[s.j]) - cfg.chase_q[s.j];
+  if (s.lab == 0 && texp < te) te = texp;
+  if (s.lab == 1 && texp + cfg.pulse_q[s.j] < te) te = texp + cfg.pulse_q[s.j];
+  if (tobs < te) te = tobs;
+  return te;
+}
+
+template <bool GRID>
 __device__ __forceinline__ void f32_interval(LaneF& s, const DevCfg& cfg, float lam) {
-  const double cs = cfg.t0 + (double)s.cyc * cfg.cycle;
-  const double te = f32_tend(s, cfg);
-  s.len = (float)(te - s.t_bp);
-  s.ph0 = (float)(s.t_bp - cs);
+  if (GRID) {
+    const int cs = cfg.t0_q + s.cyc * cfg.cycle_q;
+    const int te = q_tend(s, cfg);
+    s.len = (float)(te - s.tq) * cfg.quantum;
+    s.ph0 = (float)(s.tq - cs) * cfg.quantum;
+  } else {
+    const double cs = cfg.t0 + (double)s.cyc * cfg.cycle;
+    const double te = f32_tend(s, cfg);
+    s.len = (float)(te - s.t_bp);
+    s.ph0 = (float)(s.t_bp - cs);
+  }
   s.el = 0.0f;
   s.comp = 0.0f;
   s.lam_cur = (s.lab == 1) ? lam : 0.0f;
@@ -126,7 +149,7 @@ __device__ __forceinline__ float f32_halve(float nf, uint32_t& blk, const LaneF&
 // MINB: resident 128-thread blocks per SM the register allocation targets
 // (8: no spills; 10: 48 registers with a few spills) -- chosen at run time by
 // the autotuner (abc_autotune).
-template <bool SPLICE, int MINB>
+template <bool SPLICE, int MINB, bool GRID>
 __global__ void __launch_bounds__(128, MINB) ssa_kernel_f32(SsaArgs A) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -186,6 +209,7 @@ __global__ void __launch_bounds__(128, MINB) ssa_kernel_f32(SsaArgs A) {
           s.cyc = 0;
           s.lab = 0;
           s.t_bp = cfg.t0;
+          s.tq = cfg.t0_q;
           s.block = 0;
           const U4 w = main_block(s, A.rk);
           s.block = 1;
@@ -203,7 +227,7 @@ __global__ void __launch_bounds__(128, MINB) ssa_kernel_f32(SsaArgs A) {
           q.gam = F.gam[0];
           q.amax = F.amax[0];
           q.alp = F.alp[0];
-          f32_interval(s, cfg, lam);
+          f32_interval<GRID>(s, cfg, lam);
           if (!(s.uu < kCountLimitF) || !(s.us < kCountLimitF)) err |= STF_OVERFLOW;
           active = true;
         }
@@ -252,15 +276,24 @@ __global__ void __launch_bounds__(128, MINB) ssa_kernel_f32(SsaArgs A) {
     const float nc = (tt - s.el) - y;
     if (!((tt - nc) < s.len)) {
       // ---- breakpoint (interval end reached, or no reaction possible)
-      s.t_bp = f32_tend(s, cfg);
-      bool fin = s.t_bp == cfg.ages[s.a];
-      if (!fin) {
+      bool fin, at_step;
+      if (GRID) {
+        s.tq = q_tend(s, cfg);
+        fin = s.tq == cfg.ages_q[s.a];
+        const int texp = (cfg.ages_q[s.a] - cfg.pulse_q[s.j]) - cfg.chase_q[s.j];
+        while (!fin && s.lab < 2 && s.tq == (s.lab == 0 ? texp : texp + cfg.pulse_q[s.j])) s.lab++;
+        const int cs = cfg.t0_q + s.cyc * cfg.cycle_q;
+        at_step = s.tq == ((s.k == cfg.n_steps - 1) ? cs + cfg.cycle_q : cs + (s.k + 1) * cfg.step_q);
+      } else {
+        s.t_bp = f32_tend(s, cfg);
+        fin = s.t_bp == cfg.ages[s.a];
         const double texp = (cfg.ages[s.a] - cfg.pulse[s.j]) - cfg.chase[s.j];
-        while (s.lab < 2 && s.t_bp == (s.lab == 0 ? texp : texp + cfg.pulse[s.j])) s.lab++;
+        while (!fin && s.lab < 2 && s.t_bp == (s.lab == 0 ? texp : texp + cfg.pulse[s.j])) s.lab++;
         const double cs = cfg.t0 + (double)s.cyc * cfg.cycle;
-        const double step_edge =
-            (s.k == cfg.n_steps - 1) ? cs + cfg.cycle : cs + (double)(s.k + 1) * cfg.step_len;
-        if (s.t_bp == step_edge) {
+        at_step = s.t_bp == ((s.k == cfg.n_steps - 1) ? cs + cfg.cycle : cs + (double)(s.k + 1) * cfg.step_len);
+      }
+      if (!fin) {
+        if (at_step) {
           s.k++;
           if (s.k == cfg.n_steps) {
             s.k = 0;
@@ -277,7 +310,7 @@ __global__ void __launch_bounds__(128, MINB) ssa_kernel_f32(SsaArgs A) {
           q.amax = F.amax[s.k];
           q.alp = F.alp[s.k];
         }
-        f32_interval(s, cfg, lam);
+        f32_interval<GRID>(s, cfg, lam);
         if (!(s.uu < kCountLimitF) || !(s.lu < kCountLimitF) || !(s.us < kCountLimitF) || !(s.ls < kCountLimitF)) {
           err |= STF_OVERFLOW;
           fin = true;
