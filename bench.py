@@ -430,7 +430,7 @@ def main():
     d_stats = torch.empty((P_rank, K), dtype=torch.float64, device="cuda")
     torch.cuda.synchronize()
     # autotuner: kernel variant timed on a sample of the batch (model 1 rows)
-    n_tune = min(args.per_model, 1000)
+    n_tune = min(args.per_model, 2000)
     variant, tune_ms = ctx.autotune(1, theta[:n_tune, :5], seed=7)
     ctx.profile(True)
 

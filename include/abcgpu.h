@@ -186,8 +186,10 @@ int abc_last_counters(const abc_ctx* ctx, int64_t* events, int64_t* rejections);
 int abc_profile(abc_ctx* ctx, int enable);
 /* Autotuner (no reference counterpart; the reference tunes nothing): times the
  * production SSA kernel variants (register allocation for 8 or 10 resident
- * blocks per SM) on a sample of particles and keeps the fastest for this
- * context.  ms_out: kernel milliseconds per variant (2 entries, may be NULL). */
+ * blocks per SM) on a sample of particles, twice each in alternating order,
+ * and keeps the fastest for this context (variant 0, the one without register
+ * spills, unless another is more than 2 % faster).  ms_out: the faster kernel
+ * milliseconds of each variant (2 entries, may be NULL). */
 int abc_autotune(abc_ctx* ctx, int model, const double* theta, int64_t n_particles, uint64_t seed,
                  double* ms_out, int* chosen);
 int abc_set_variant(abc_ctx* ctx, int variant);
