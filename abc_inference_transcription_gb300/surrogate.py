@@ -5,7 +5,7 @@ summary statistics.  It is trained on SSA output the pipeline itself
 generates; screening keeps a prior draw for exact simulation when its
 predicted expected error is within a gene's threshold plus a calibrated
 margin for some gene, or when the ensemble members disagree.  The exact SSA
-and the FP64-checked acceptance stay the judge: the screen only decides which
+and the FP64-checked acceptance decide acceptance: the screen only decides which
 draws are simulated.
 """
 from __future__ import annotations

@@ -36,7 +36,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N_CELLS = 2000
-OPS_PER_EVENT = 60          # algorithmic instruction count per fired event
+# algorithmic operations per fired event: half a Philox4x32-10 block (10 rounds x
+# 6 integer operations / 2), two uniforms, one log, one divide, ~9 propensity and
+# channel-selection operations, the clock add and compare, the state update
+OPS_PER_EVENT = 60
 LANES_PER_SM = 128
 SMS = 152
 PER_MODEL_DEFAULT = 4000
