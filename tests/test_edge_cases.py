@@ -142,3 +142,23 @@ def test_indices_only_selection_refuses_error_fetch(Ctx):
         assert err is None and off[-1] == 4 * 20
         with pytest.raises(RuntimeError, match="ABC_ERR_STATE"):
             ctx._fetch(4, int(off[-1]), True)
+
+
+@pytest.mark.parametrize("errors", (True, False))
+def test_selection_extreme_magnitudes(Ctx, orc, errors):
+    """Statistics and data far outside the certified FP32 path's range
+    (|x| > 2^60 or < 2^-60, a denominator below 2^-120) take its FP64
+    fallback; sets and order still equal the oracle's."""
+    data, se, stats = _problem(600, 8, 12, 17)
+    scale = np.array([1e20, 1e-20, 1.0, 3e18, 1e-19, 1.0, 1.0, 1e15])      # per gene
+    data = data * scale[:, None]
+    se = se * scale[:, None]
+    se[5] = 0.0
+    data[5, :6] = 0.0                                                        # eps = 1e-4 denominators
+    stats = np.concatenate([stats * s for s in (1e20, 1e-20, 1.0)])[::3]    # particles at three scales
+    stats[::7, 3] = 1e-200
+    with Ctx(make_config("hour"), None) as ctx:
+        for mode in (0, 2):
+            ctx.set_distance_mode(mode)
+            for sel, x in ((0, 4.8), (1, 0.05), (1, 0.5)):
+                _check(ctx, orc, data, se, stats, sel, x, errors)
