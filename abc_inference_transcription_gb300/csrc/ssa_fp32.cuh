@@ -232,8 +232,9 @@ __global__ void __launch_bounds__(128, MINB) ssa_kernel_f32(SsaArgs A) {
           active = true;
         }
       }
+      // done only changes here, so the warp's exit test runs only after a refill
+      if (__all_sync(FULL, done)) break;
     }
-    if (__all_sync(FULL, done)) break;
     if (!active) continue;
 
     // ---- one iteration: propensities, Philox block, waiting time
