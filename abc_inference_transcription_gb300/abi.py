@@ -73,6 +73,16 @@ def nstats(n_ages: int, n_conds: int) -> int:
     return 4 * n_ages + 3 * n_conds
 
 
+def breakpoint_grid(cfg: AbcConfig) -> float | None:
+    """The power-of-two quantum on which every time of cfg lies (the production
+    SSA then places breakpoints with integer arithmetic), or None."""
+    q = C.c_double(0.0)
+    st = load_library().abc_breakpoint_grid(C.byref(cfg), C.byref(q))
+    if st < 0:
+        raise AbcError(st, "invalid configuration")
+    return q.value if st == 1 else None
+
+
 def num_params(cfg: AbcConfig, model: int) -> int:
     """theta columns: get_vary_map (scripts/model.jl:30-43) + lambda + extensions."""
     if model not in (1, 2, 3, 4, 5):
@@ -156,6 +166,7 @@ def _declare(lib: C.CDLL) -> None:
         "abc_accept_fetch": (C.c_int, [vp, i64p, i64p, dp]),
         "abc_select_counters": (C.c_int, [vp, i64p, i64p]),
         "abc_set_select_errors": (C.c_int, [vp, C.c_int]),
+        "abc_breakpoint_grid": (C.c_int, [C.POINTER(AbcConfig), dp]),
         "abc_write_particles": (C.c_int, [C.c_char_p, C.c_int, C.c_int64, i64p, i64p]),
         "abc_write_matrix": (C.c_int, [C.c_char_p, C.c_int, C.c_int64, C.c_int64, dp, C.c_int64]),
         "abc_format_double": (C.c_int, [C.c_double, C.c_char_p, C.c_int]),
@@ -207,7 +218,7 @@ ABI_SYMBOLS = [
     "abc_synchronize", "abc_simulate_batch", "abc_simulate_batch_device", "abc_simulate_noalloc", "abc_simulate_cells", "abc_last_counters",
     "abc_profile", "abc_profile_read", "abc_autotune", "abc_set_variant", "abc_errors",
     "abc_errors_select", "abc_errors_select_thr", "abc_errors_select_device", "abc_accept_fetch",
-    "abc_select_counters", "abc_select_profile_read", "abc_set_select_errors", "abc_write_particles", "abc_write_matrix",
+    "abc_select_counters", "abc_select_profile_read", "abc_set_select_errors", "abc_breakpoint_grid", "abc_write_particles", "abc_write_matrix",
     "abc_format_double", "abc_read_particles", "abc_set_distance_mode", "abc_get_distance_mode",
     "abc_errors_candidate", "abc_model_probs", "abc_posterior_summary",
     "abc_moment_simulate", "abc_data_stats", "abc_set_graph", "abc_graph_counters",

@@ -242,6 +242,16 @@ int abc_destroy(abc_ctx* c) {
 
 const char* abc_last_error(const abc_ctx* c) { return c ? c->err.c_str() : "null context"; }
 
+int abc_breakpoint_grid(const abc_config* cfg, double* quantum) {
+  if (!cfg) return ABC_ERR_INVALID;
+  std::string msg;
+  const int st = validate_config(cfg, msg);
+  if (st) return st;
+  const DevCfg d = make_dcfg(cfg);
+  if (quantum) *quantum = d.grid_ok ? (double)d.quantum : 0.0;
+  return d.grid_ok ? 1 : 0;
+}
+
 int abc_num_params(const abc_ctx* c, int model) {
   if (!c) return ABC_ERR_INVALID;
   return npar_of(&c->cfg, model);

@@ -184,6 +184,12 @@ int abc_last_counters(const abc_ctx* ctx, int64_t* events, int64_t* rejections);
  * abc_profile_read returns, for the last synchronized simulate call, the
  * milliseconds spent in [setup, SSA, capture+statistics] kernels. */
 int abc_profile(abc_ctx* ctx, int enable);
+/* Whether the configuration's times (t0, cycle, age step, ages, pulses,
+ * chases) are all integer multiples of a power-of-two quantum, in which case
+ * the production SSA places breakpoints with integer arithmetic instead of
+ * FP64: returns 1 (and *quantum, may be NULL) or 0; ABC_ERR_INVALID for an
+ * invalid configuration.  Host only.  No reference counterpart. */
+int abc_breakpoint_grid(const abc_config* cfg, double* quantum);
 /* Autotuner (no reference counterpart; the reference tunes nothing): times the
  * production SSA kernel variants (register allocation for 8 or 10 resident
  * blocks per SM) on a sample of particles, twice each in alternating order,

@@ -99,3 +99,17 @@ def test_product_path_has_no_oracle_dependency():
         for f in files:
             if f.endswith((".py", ".cu", ".cuh", ".h")):
                 assert not bad.search(open(os.path.join(root, f)).read()), f
+
+
+def test_breakpoint_grid_detection(built):
+    """The integer breakpoint path of the production SSA applies when every
+    time of the configuration is a multiple of a power-of-two quantum."""
+    from abc_inference_transcription_gb300 import abi
+    assert abi.breakpoint_grid(make_config("hour")) == 0.25       # pulses of 15 min in hours
+    assert abi.breakpoint_grid(make_config("min")) == 1.0         # whole minutes
+    cfg = make_config("hour")
+    cfg.pulse[0] = 0.1                                            # not a dyadic multiple
+    assert abi.breakpoint_grid(cfg) is None
+    cfg = make_config("hour")
+    cfg.cycle = 21.0                                              # age step 4.2 h
+    assert abi.breakpoint_grid(cfg) is None

@@ -104,3 +104,4 @@ def test_selection_lists_to_particles_file(F, orc, tmp_path):
     F.write_particles(tmp_path / "particles_const.txt", off, idx)
     o2, i2 = F.read_particles(tmp_path / "particles_const.txt")
     assert np.array_equal(o2, roff) and np.array_equal(i2, ridx)
+
