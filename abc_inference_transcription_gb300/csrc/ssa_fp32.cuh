@@ -35,6 +35,7 @@ struct LaneF {
   float el, comp;       // elapsed time in the interval, Kahan compensation
   float len;            // interval length
   float ph0;            // cycle phase at the interval start
+  float at0, at1;       // thinned transcription rate at0 + at1 x (elapsed time), scaling exponent 0 or 1
   float lam_cur;        // labelling probability in this interval
   float uu, lu, us, ls; // molecule counts (exact integers in FP32)
   int k, cyc, lab, G;
@@ -76,7 +77,8 @@ __device__ __forceinline__ int q_tend(const LaneF& s, const DevCfg& cfg) {
 }
 
 template <bool GRID>
-__device__ __forceinline__ void f32_interval(LaneF& s, const DevCfg& cfg, float lam) {
+__device__ __forceinline__ void f32_interval(LaneF& s, const DevCfg& cfg, float lam, float alp, float scal,
+                                             float invT) {
   if (GRID) {
     const int cs = cfg.t0_q + s.cyc * cfg.cycle_q;
     const int te = q_tend(s, cfg);
@@ -91,6 +93,9 @@ __device__ __forceinline__ void f32_interval(LaneF& s, const DevCfg& cfg, float 
   s.el = 0.0f;
   s.comp = 0.0f;
   s.lam_cur = (s.lab == 1) ? lam : 0.0f;
+  // alpha size^s with size = 1 + phase / T is linear in the elapsed time for s in {0, 1}
+  s.at1 = alp * scal * invT;
+  s.at0 = alp * fmaf(scal, s.ph0 * invT, 1.0f);
 }
 
 // Philox4x32-10 with precomputed round keys rk[2r], rk[2r+1].
@@ -227,7 +232,7 @@ __global__ void __launch_bounds__(128, MINB) ssa_kernel_f32(SsaArgs A) {
           q.gam = F.gam[0];
           q.amax = F.amax[0];
           q.alp = F.alp[0];
-          f32_interval<GRID>(s, cfg, lam);
+          f32_interval<GRID>(s, cfg, lam, q.alp, scal, invT);
           if (!(s.uu < kCountLimitF) || !(s.us < kCountLimitF)) err |= STF_OVERFLOW;
           active = true;
         }
@@ -311,7 +316,7 @@ __global__ void __launch_bounds__(128, MINB) ssa_kernel_f32(SsaArgs A) {
           q.amax = F.amax[s.k];
           q.alp = F.alp[s.k];
         }
-        f32_interval<GRID>(s, cfg, lam);
+        f32_interval<GRID>(s, cfg, lam, q.alp, scal, invT);
         if (!(s.uu < kCountLimitF) || !(s.lu < kCountLimitF) || !(s.us < kCountLimitF) || !(s.ls < kCountLimitF)) {
           err |= STF_OVERFLOW;
           fin = true;
@@ -332,12 +337,12 @@ __global__ void __launch_bounds__(128, MINB) ssa_kernel_f32(SsaArgs A) {
     s.comp = nc;
     const float r = u23(wc) * a0;
     const bool b1 = r >= c1, b2 = r >= c2, b3 = r >= c3, b4 = r >= c4;
-    const float size = fmaf(s.ph0 + (s.el - s.comp), invT, 1.0f);
-    // size^s: linear (exact) for s in {0, 1}, the general power only for lanes
-    // with another exponent (a warp-uniform skip for the reference's models)
-    float sz = fmaf(scal, size - 1.0f, 1.0f);
-    if (!scal01) sz = exp2f(scal * __log2f(size));
-    const float at = q.alp * sz;
+    // alpha size^s: the per-interval linear form for s in {0, 1}, the general
+    // power only for lanes with another exponent (a warp-uniform skip for the
+    // reference's models)
+    const float dt = s.el - s.comp;
+    float at = fmaf(s.at1, dt, s.at0);
+    if (!scal01) at = q.alp * exp2f(scal * __log2f(fmaf(s.ph0 + dt, invT, 1.0f)));
     // thinning uniform from the 9 low bits of both words (18 bits), x bound
     const uint32_t th = ((wt & 0x1FFu) << 9) | (wc & 0x1FFu);
     const float v = (__uint_as_float(0x3F800000u | (th << 5)) - 1.0f) * q.amax;
