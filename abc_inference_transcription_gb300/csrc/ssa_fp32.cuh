@@ -36,6 +36,7 @@ struct LaneF {
   float len;            // interval length
   float ph0;            // cycle phase at the interval start
   float at0, at1;       // thinned transcription rate at0 + at1 x (elapsed time), scaling exponent 0 or 1
+  float koff_amax;      // k_off + alpha_max of the current age step (the cumulative sum when G = 1)
   float lam_cur;        // labelling probability in this interval
   float uu, lu, us, ls; // molecule counts (exact integers in FP32)
   int k, cyc, lab, G;
@@ -232,6 +233,7 @@ __global__ void __launch_bounds__(128, MINB) ssa_kernel_f32(SsaArgs A) {
           q.gam = F.gam[0];
           q.amax = F.amax[0];
           q.alp = F.alp[0];
+          s.koff_amax = koff + q.amax;
           f32_interval<GRID>(s, cfg, lam, q.alp, scal, invT);
           if (!(s.uu < kCountLimitF) || !(s.us < kCountLimitF)) err |= STF_OVERFLOW;
           active = true;
@@ -243,11 +245,10 @@ __global__ void __launch_bounds__(128, MINB) ssa_kernel_f32(SsaArgs A) {
     if (!active) continue;
 
     // ---- one iteration: propensities, Philox block, waiting time
-    const float a_on = s.G ? 0.0f : q.kon;
-    const float a_off = s.G ? koff : 0.0f;
-    const float a_tx = s.G ? q.amax : 0.0f;
+    // cumulative propensities: one of k_on, k_off is zero, so c2 and c3 are
+    // selections (k_off + alpha_max is summed once per age step)
     float c4, c5 = 0.f, c6 = 0.f, a_last, a0;
-    const float c1 = a_on, c2 = c1 + a_off, c3 = c2 + a_tx;
+    const float c1 = s.G ? 0.0f : q.kon, c2 = s.G ? koff : q.kon, c3 = s.G ? s.koff_amax : q.kon;
     if (!SPLICE) {
       a_last = q.gam * s.lu;
       c4 = fmaf(q.gam, s.uu, c3);
@@ -315,6 +316,7 @@ __global__ void __launch_bounds__(128, MINB) ssa_kernel_f32(SsaArgs A) {
           q.gam = F.gam[s.k];
           q.amax = F.amax[s.k];
           q.alp = F.alp[s.k];
+          s.koff_amax = koff + q.amax;
         }
         f32_interval<GRID>(s, cfg, lam, q.alp, scal, invT);
         if (!(s.uu < kCountLimitF) || !(s.lu < kCountLimitF) || !(s.us < kCountLimitF) || !(s.ls < kCountLimitF)) {
