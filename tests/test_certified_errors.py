@@ -95,3 +95,58 @@ def test_certified_error_within_bound(orc, case):
     if case == "generic":
         # the bound is not loose by orders of magnitude (else the selection would recheck too much)
         assert np.max(dev / bound(got[ok])) > 1e-2, np.max(dev / bound(got[ok]))
+
+
+def _certified_order(v, x, thr, clip=10.0):
+    """The selection's decision logic restated: sort by certified values v
+    (ties by index), flag positions whose interval [v - B, v + B] touches a
+    neighbour's, the clip or the threshold, give flagged positions their exact
+    value x, and sort each run of consecutive flagged positions in place."""
+    n = v.shape[0]
+    order = np.lexsort((np.arange(n), v))
+    vs, idx = v[order].copy(), order.copy()
+    B = bound(vs)
+    flag = np.zeros(n, bool)
+    touch = vs[:-1] + B[:-1] >= vs[1:] - B[1:]
+    flag[:-1] |= touch
+    flag[1:] |= touch
+    flag |= np.abs(vs - clip) <= B
+    flag |= np.abs(vs - thr) <= B
+    vs[flag] = x[idx[flag]]
+    i = 0
+    while i < n:
+        if not flag[i]:
+            i += 1
+            continue
+        j = i
+        while j < n and flag[j]:
+            j += 1
+        run = np.lexsort((idx[i:j], vs[i:j]))
+        vs[i:j], idx[i:j] = vs[i:j][run], idx[i:j][run]
+        i = j
+    return idx, vs
+
+
+def test_certified_order_logic_equals_exact_order():
+    """Adversarial certified values (at the edges of their bounds), exact ties,
+    dense clusters, values at the clip and at the threshold: the decision
+    logic gives the exact (err, index) order, and the set below the threshold
+    is exact."""
+    rng = np.random.default_rng(11)
+    for trial in range(200):
+        n = int(rng.integers(2, 400))
+        x = np.round(rng.uniform(0, 12, n), int(rng.integers(2, 8)))        # exact errors, many ties
+        x = np.minimum(x, 10.0)                                              # the clip
+        x[rng.random(n) < 0.1] = 10.0
+        if trial % 3 == 0:                                                   # a dense cluster
+            x[: n // 2] = 3.0 + rng.uniform(-1e-6, 1e-6, n // 2)
+        # certified values anywhere within the bound, often at its edges:
+        # |v - x| <= B(x) (1 - 2e-6) <= B(v), the kernel's guarantee
+        B = bound(x) * (1.0 - 2e-6)
+        edge = rng.choice([-1.0, 1.0, 0.0], n) if trial % 2 else rng.uniform(-1, 1, n)
+        v = x + edge * B
+        thr = float(rng.choice([3.0, 5.0, 10.0, x[rng.integers(0, n)]]))
+        idx, vs = _certified_order(v, x, thr)
+        want = np.lexsort((np.arange(n), x))
+        assert np.array_equal(idx, want), trial
+        assert set(np.flatnonzero(x <= thr)) == set(idx[: int((x <= thr).sum())]), trial
