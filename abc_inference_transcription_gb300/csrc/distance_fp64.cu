@@ -4,6 +4,7 @@
 // per-gene grouping and (err, index) sort of accepted particles
 // (scripts/accepted_particles.jl:20-26: findall + sortperm).
 #include <algorithm>
+#include <atomic>
 
 #include "bitonic.cuh"
 #include "distance.cuh"
@@ -584,7 +585,7 @@ cudaError_t launch_dist_group(const Cand* cand, int64_t n, int64_t G, int64_t* g
 static cudaError_t launch_segsort(const int64_t* goff, int64_t G, int32_t* sp, double* se64, const int* dirty,
                                   cudaStream_t s) {
   constexpr int smem = kSortSmem * (int)(sizeof(uint64_t) + sizeof(int32_t));
-  static bool attr = false;
+  static std::atomic<bool> attr{false};  // the attribute call is idempotent; shared by all contexts
   if (!attr) {
     cudaError_t err = cudaFuncSetAttribute(segsort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (err) return err;

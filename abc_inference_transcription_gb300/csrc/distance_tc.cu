@@ -28,6 +28,7 @@
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstring>
 
@@ -521,7 +522,7 @@ bool make_map(CUtensorMap* map, const float* base, int64_t rows, int64_t cols, i
 
 template <int NH>
 cudaError_t launch_nh(const float* A, const float* B, const TcArgs& args, int grid, cudaStream_t s) {
-  static bool attr = false;
+  static std::atomic<bool> attr{false};  // the attribute call is idempotent; shared by all contexts
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(dist_tc_kernel<NH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)Cfg<NH>::kSmem);

@@ -17,6 +17,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstring>
 
 #include "kernels.h"
@@ -200,7 +201,7 @@ bool make_map3(CUtensorMap* map, const __nv_bfloat16* base, int64_t K, int64_t l
 
 template <int EPI>
 cudaError_t launch_epi(const CUtensorMap& ma, const CUtensorMap& mb, const TcGemm& g, int members, cudaStream_t s) {
-  static bool attr = false;
+  static std::atomic<bool> attr{false};  // the attribute call is idempotent; shared by all contexts
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(mlp_tc_kernel<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
     if (e != cudaSuccess) return e;

@@ -5,6 +5,8 @@
 // FP64, built with -fmad=false: results are bit-identical to the C oracle.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -301,7 +303,7 @@ cudaError_t launch_posterior_summary(const int64_t* aoff, const int64_t* idx, in
   if (total > 0) {
     post_gather_kernel<<<(unsigned)G, 256, 0, s>>>(aoff, idx, theta, ld, npar, total, scratch);
     constexpr int smem = kPostSmem * (int)sizeof(uint64_t);
-    static bool attr = false;
+    static std::atomic<bool> attr{false};  // the attribute call is idempotent; shared by all contexts
     if (!attr) {
       cudaError_t e = cudaFuncSetAttribute(post_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
       if (e != cudaSuccess) return e;
