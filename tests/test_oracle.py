@@ -249,3 +249,30 @@ def test_mlp_reference_gradients_finite_differences():
             fd = (mlp_ref.loss_and_grads(pp, d, th, st, *args, rounding=False)[0] -
                   mlp_ref.loss_and_grads(pm, d, th, st, *args, rounding=False)[0]) / (2 * h)
             assert abs(fd - g[i]) <= 1e-6 + 1e-4 * abs(fd), (name, i, fd, g[i])
+
+
+def test_accept_oracle_matches_numpy_restatement(orc):
+    """Random error matrices with ties and NaN: eps mode is findall(err <= eps)
+    followed by a stable sortperm (scripts/accepted_particles.jl:20-26), top-q
+    the ceil(q P) smallest finite errors ordered by (err, index); 1-based."""
+    rng = np.random.default_rng(4)
+    for trial in range(30):
+        P, G = int(rng.integers(1, 300)), int(rng.integers(1, 6))
+        err = np.round(rng.uniform(0, 10, (P, G)), int(rng.integers(0, 3)))   # many ties
+        err[rng.random((P, G)) < 0.1] = np.nan
+        for mode, x in ((0, float(rng.uniform(0, 10))), (1, float(rng.uniform(0.01, 1.0)))):
+            off, idx = orc.accept(err, mode, x)
+            want_off, want_idx = [0], []
+            for g in range(G):
+                e = err[:, g]
+                if mode == 0:
+                    v = np.flatnonzero(e <= x)
+                    sel = v[np.argsort(e[v], kind="stable")]
+                else:
+                    k = int(np.ceil(x * P))
+                    fin = np.flatnonzero(~np.isnan(e))
+                    sel = fin[np.argsort(e[fin], kind="stable")][:k]
+                want_idx.extend((sel + 1).tolist())
+                want_off.append(len(want_idx))
+            assert off.tolist() == want_off, (trial, mode)
+            assert idx.tolist() == want_idx, (trial, mode)
