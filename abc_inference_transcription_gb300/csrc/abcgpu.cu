@@ -432,6 +432,7 @@ static int enqueue_simulate(abc_ctx* c, int model, const int32_t* d_models, cons
     sa.rec = c->d_rec.p;
     sa.recf = c->d_recf.p;
     sa.status = c->d_status.p;
+    sa.fp32 = fp64 ? 0 : 1;
     CK(prof_mark(c));
     CK(launch_setup(sa, c->stream));
     CK(launch_work_order(c->d_rec.p, n, c->d_ohist.p, c->d_order.p, c->stream));

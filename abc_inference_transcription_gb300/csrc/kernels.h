@@ -32,6 +32,7 @@ struct SetupArgs {
   PRec* rec;
   PRecF* recf;
   int* status;
+  int fp32 = 0;              // production mode: FP32 rates beyond its range are an error
 };
 
 struct PriorArgs {

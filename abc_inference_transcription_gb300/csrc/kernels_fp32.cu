@@ -11,13 +11,21 @@ namespace abc {
 // 10 resident blocks of 128 threads per SM.
 static const int kVariantMinBlocks[kSsaVariants] = {8, 10};
 
-template <bool SPLICE, bool GRID>
+template <bool SPLICE, bool GRID, bool GENSCAL>
 static cudaError_t launch_variant(const SsaArgs& b, int variant, int grid, cudaStream_t s) {
   if (variant == 1)
-    ssa_kernel_f32<SPLICE, 10, GRID><<<grid, 128, 0, s>>>(b);
+    ssa_kernel_f32<SPLICE, 10, GRID, GENSCAL><<<grid, 128, 0, s>>>(b);
   else
-    ssa_kernel_f32<SPLICE, 8, GRID><<<grid, 128, 0, s>>>(b);
+    ssa_kernel_f32<SPLICE, 8, GRID, GENSCAL><<<grid, 128, 0, s>>>(b);
   return cudaGetLastError();
+}
+
+template <bool SPLICE, bool GRID>
+static cudaError_t launch_scal(const SsaArgs& b, int variant, int grid, cudaStream_t s) {
+  // a scaling column in theta gives each particle its own size exponent;
+  // without one the exponent is 0 or 1 and the rate is linear in time
+  return b.cfg.scaling_column ? launch_variant<SPLICE, GRID, true>(b, variant, grid, s)
+                              : launch_variant<SPLICE, GRID, false>(b, variant, grid, s);
 }
 
 cudaError_t launch_ssa_fp32(const SsaArgs& a, int grid, cudaStream_t s, int variant) {
@@ -31,18 +39,16 @@ cudaError_t launch_ssa_fp32(const SsaArgs& a, int grid, cudaStream_t s, int vari
   }
   // integer breakpoints when the configuration's times lie on a power-of-two grid
   if (a.cfg.grid_ok)
-    return a.cfg.splicing ? launch_variant<true, true>(b, variant, grid, s)
-                          : launch_variant<false, true>(b, variant, grid, s);
-  return a.cfg.splicing ? launch_variant<true, false>(b, variant, grid, s)
-                        : launch_variant<false, false>(b, variant, grid, s);
+    return a.cfg.splicing ? launch_scal<true, true>(b, variant, grid, s) : launch_scal<false, true>(b, variant, grid, s);
+  return a.cfg.splicing ? launch_scal<true, false>(b, variant, grid, s) : launch_scal<false, false>(b, variant, grid, s);
 }
 
 int ssa_blocks_per_sm_fp32(int variant) {
   int n = 0;
   if (variant == 1)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssa_kernel_f32<false, 10, true>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssa_kernel_f32<false, 10, true, false>, 128, 0);
   else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssa_kernel_f32<false, 8, true>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssa_kernel_f32<false, 8, true, false>, 128, 0);
   return n > 0 ? n : kVariantMinBlocks[variant < 0 || variant >= kSsaVariants ? 0 : variant];
 }
 

@@ -86,6 +86,15 @@ __global__ void setup_kernel(SetupArgs A) {
   F.lam = (float)R.lam;
   F.beta = (float)R.beta;
   F.scal = (float)R.scal;
+  if (A.fp32) {
+    // rates beyond the FP32 range would stall the production kernel's clock
+    bool ok = F.koff < 1e30f && F.beta < 1e30f;
+    for (int k = 0; k < kMaxSteps; ++k) ok = ok && F.kon[k] < 1e30f && F.alp[k] < 1e30f && F.gam[k] < 1e30f;
+    if (!ok) {
+      atomicOr(A.status, STF_NONFINITE);
+      memset(&F, 0, sizeof(F));
+    }
+  }
   A.recf[p] = F;
 }
 
@@ -99,8 +108,85 @@ cudaError_t launch_setup(const SetupArgs& a, cudaStream_t s) {
 // ---------------------------------------------------------------------------
 // SSA, FP64 oracle mode.
 // ---------------------------------------------------------------------------
+// Persistent: every lane owns one trajectory at a time and pulls the next
+// (particle, cell) item from the global counter (warp-aggregated atomics).
+__global__ void __launch_bounds__(128) ssa_kernel_fp64(SsaArgs A) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int64_t cap = A.cfg.event_cap > 0 ? A.cfg.event_cap : kDefaultEventCap;
+  Traj s;
+  bool active = false, done = false;
+  unsigned long long tot_ev = 0, tot_rej = 0;
+  int err = 0;
+  while (true) {
+    const bool need = !active && !done;
+    const unsigned mask = __ballot_sync(FULL, need);
+    if (mask) {
+      const int leader = __ffs(mask) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(A.counter, (unsigned long long)__popc(mask));
+      base = __shfl_sync(FULL, base, leader);
+      if (need) {
+        const unsigned long long item = base + (unsigned long long)__popc(mask & ((1u << lane) - 1u));
+        if (item >= (unsigned long long)A.n_items) {
+          done = true;
+        } else {
+          traj_init(s, A, (int64_t)item);
+          active = true;
+        }
+      }
+    }
+    if (__all_sync(FULL, done)) break;
+    if (active) {
+      const PRec& R = A.rec[s.plocal];
+#pragma unroll 1
+      for (int it = 0; it < kQuantum; ++it) {
+        uint32_t ch;
+        bool fin = step_fp64(s, R, A.cfg, ch);
+        if (ch == CH_REJ) {
+          tot_rej++;
+        } else if (ch != CH_NULL) {
+          s.ev++;
+          if (s.ev > cap) {
+            err |= STF_EVENT_CAP;
+            fin = true;
+          }
+        }
+        if (s.uu >= kOverflowCount || s.lu >= kOverflowCount || s.us >= kOverflowCount ||
+            s.ls >= kOverflowCount) {
+          err |= STF_OVERFLOW;
+          fin = true;
+        }
+        if (s.stall > kMaxStall) {
+          err |= STF_NONFINITE;
+          fin = true;
+        }
+        if (fin) {
+          A.counts[s.out] = make_int2(s.uu + s.us, s.lu + s.ls);
+          if (A.events) A.events[s.out] = s.ev;
+          if (A.hash) A.hash[s.out] = s.hash;
+          tot_ev += (unsigned long long)s.ev;
+          active = false;
+          break;
+        }
+      }
+    }
+  }
+  // warp totals -> one atomic per warp
+  for (int o = 16; o > 0; o >>= 1) {
+    tot_ev += __shfl_xor_sync(FULL, tot_ev, o);
+    tot_rej += __shfl_xor_sync(FULL, tot_rej, o);
+    err |= __shfl_xor_sync(FULL, err, o);
+  }
+  if (lane == 0) {
+    atomicAdd(&A.totals[0], tot_ev);
+    atomicAdd(&A.totals[1], tot_rej);
+    if (err) atomicOr(A.status, err);
+  }
+}
+
 cudaError_t launch_ssa_fp64(const SsaArgs& a, int grid, cudaStream_t s) {
-  ssa_kernel<true><<<grid, 128, 0, s>>>(a);
+  ssa_kernel_fp64<<<grid, 128, 0, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -188,7 +274,7 @@ cudaError_t launch_stats(const StatsArgs& a, cudaStream_t s) {
 
 int ssa_blocks_per_sm_fp64() {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssa_kernel<true>, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssa_kernel_fp64, 128, 0);
   return n;
 }
 

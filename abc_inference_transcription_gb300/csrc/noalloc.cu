@@ -196,6 +196,7 @@ extern "C" int abc_simulate_noalloc(const abc_config* cfg, int model, int64_t n_
   sa.rec = d_rec;
   sa.recf = d_recf;
   sa.status = status;
+  sa.fp32 = cfg->precision == ABC_FP32 ? 1 : 0;
   NA_CK(launch_setup(sa, stream));
 
   int dev = 0, sms = 0;

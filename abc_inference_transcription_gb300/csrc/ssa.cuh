@@ -55,6 +55,7 @@ struct SsaArgs {
   unsigned long long* totals;  // [0] fired events, [1] thinning rejections
   int* status;
   int want_hash;
+  int chunk = 1;             // production kernel: consecutive items a lane takes per pull
   uint32_t rk[20];           // Philox round keys (seed + r * Weyl), filled by the FP32 launcher
 };
 
@@ -231,215 +232,10 @@ __device__ __forceinline__ bool step_fp64(Traj& s, const PRec& R, const DevCfg& 
   return false;
 }
 
-// One iteration in FP32 (propensities, waiting time and selection in FP32,
-// clock in FP64).  Uniforms: 24-bit U1 in (0,1), 24-bit U2 in [0,1).
-struct RatesF {
-  float kon, gam, amax, alp;  // current age step
-  float koff, lam, beta, scal;
-};
-
-__device__ __forceinline__ float powf_fast(float x, float s) {
-  if (s == 1.0f) return x;
-  if (s == 0.0f) return 1.0f;
-  return exp2f(s * __log2f(x));
-}
-
-__device__ __forceinline__ bool step_fp32(Traj& s, const RatesF& q, const DevCfg& cfg, float invT,
-                                          uint32_t& ch) {
-  float a_on = s.G ? 0.0f : q.kon;
-  float a_off = s.G ? q.koff : 0.0f;
-  float a_tx = s.G ? q.amax : 0.0f;
-  float c1 = a_on;
-  float c2 = c1 + a_off;
-  float c3 = c2 + a_tx;
-  float c4, c5, c6, a_last, a0;
-  if (!cfg.splicing) {
-    float a_du = q.gam * (float)s.uu;
-    a_last = q.gam * (float)s.lu;
-    c4 = c3 + a_du;
-    c5 = c4;
-    c6 = c4;
-    a0 = c4 + a_last;
-  } else {
-    float a_su = q.beta * (float)s.uu;
-    float a_sl = q.beta * (float)s.lu;
-    float a_du = q.gam * (float)s.us;
-    a_last = q.gam * (float)s.ls;
-    c4 = c3 + a_su;
-    c5 = c4 + a_sl;
-    c6 = c5 + a_du;
-    a0 = c6 + a_last;
-  }
-  uint32_t w0, w1;
-  rng_pair(s.rng, w0, w1);
-  ch = CH_NULL;
-  if (!(a0 > 0.0f)) return traj_breakpoint(s, cfg);
-  float U1 = fmaf((float)(w0 >> 8), 5.9604644775390625e-08f, 2.98023223876953125e-08f);
-  float tau = __fdividef(-__logf(U1), a0);
-  double tn = s.t + (double)tau;
-  if (tn >= s.t_end) return traj_breakpoint(s, cfg);
-  s.stall = (tn == s.t) ? s.stall + 1 : 0;
-  s.t = tn;
-  float r = ((float)(w1 >> 8) * 5.9604644775390625e-08f) * a0;
-  if (r < c1) {
-    s.G = 1;
-    ch = CH_ON;
-  } else if (r < c2) {
-    s.G = 0;
-    ch = CH_OFF;
-  } else if (r < c3) {
-    float v = r - c2;
-    float size = 1.0f + (float)(s.t - s.cycle_start) * invT;
-    float at = q.alp * powf_fast(size, q.scal);
-    if (v < at) {
-      float lam_cur = (s.lab_state == 1) ? q.lam : 0.0f;
-      if (v < at * lam_cur) {
-        s.lu++;
-        ch = CH_TXL;
-      } else {
-        s.uu++;
-        ch = CH_TXU;
-      }
-    } else {
-      ch = CH_REJ;
-    }
-  } else if (!cfg.splicing) {
-    if (r < c4) {
-      s.uu--;
-      ch = CH_DEGU;
-    } else if (a_last > 0.0f) {
-      s.lu--;
-      ch = CH_DEGL;
-    }
-  } else {
-    if (r < c4) {
-      s.uu--;
-      s.us++;
-      ch = CH_SPLU;
-    } else if (r < c5) {
-      s.lu--;
-      s.ls++;
-      ch = CH_SPLL;
-    } else if (r < c6) {
-      s.us--;
-      ch = CH_DEGU;
-    } else if (a_last > 0.0f) {
-      s.ls--;
-      ch = CH_DEGL;
-    }
-  }
-  return false;
-}
-
-__device__ __forceinline__ void load_rates(RatesF& q, const PRecF& F, int k) {
-  q.kon = F.kon[k];
-  q.gam = F.gam[k];
-  q.amax = F.amax[k];
-  q.alp = F.alp[k];
-}
-__device__ __forceinline__ void load_particle(RatesF& q, const PRecF& F) {
-  q.koff = F.koff;
-  q.lam = F.lam;
-  q.beta = F.beta;
-  q.scal = F.scal;
-}
-
-// Persistent driver.  FP64 = true: oracle mode; false: production mode.
-// Iterations between work refills are grouped in quanta of kQuantum so the
-// warp votes are amortised.
+// Persistent driver of the FP64 oracle mode.  Iterations between work
+// refills are grouped in quanta of kQuantum so the warp votes are amortised.
 constexpr int kQuantum = 16;
 constexpr int64_t kDefaultEventCap = (int64_t)1 << 28;
 constexpr int kOverflowCount = 1 << 30;
-
-template <bool FP64>
-__global__ void __launch_bounds__(128) ssa_kernel(SsaArgs A) {
-  const unsigned FULL = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
-  const float invT = (float)(1.0 / A.cfg.cycle);
-  const int64_t cap = A.cfg.event_cap > 0 ? A.cfg.event_cap : kDefaultEventCap;
-  Traj s;
-  RatesF q;
-  bool active = false, done = false;
-  int kprev = -1;
-  unsigned long long tot_ev = 0, tot_rej = 0;
-  int err = 0;
-  while (true) {
-    const bool need = !active && !done;
-    const unsigned mask = __ballot_sync(FULL, need);
-    if (mask) {
-      const int leader = __ffs(mask) - 1;
-      unsigned long long base = 0;
-      if (lane == leader) base = atomicAdd(A.counter, (unsigned long long)__popc(mask));
-      base = __shfl_sync(FULL, base, leader);
-      if (need) {
-        const unsigned long long item = base + (unsigned long long)__popc(mask & ((1u << lane) - 1u));
-        if (item >= (unsigned long long)A.n_items) {
-          done = true;
-        } else {
-          traj_init(s, A, (int64_t)item);
-          if (!FP64) load_particle(q, A.recf[s.plocal]);
-          active = true;
-          kprev = -1;
-        }
-      }
-    }
-    if (__all_sync(FULL, done)) break;
-    if (active) {
-      const PRec& R = A.rec[s.plocal];
-#pragma unroll 1
-      for (int it = 0; it < kQuantum; ++it) {
-        uint32_t ch;
-        bool fin;
-        if (FP64) {
-          fin = step_fp64(s, R, A.cfg, ch);
-        } else {
-          if (s.k != kprev) {
-            load_rates(q, A.recf[s.plocal], s.k);
-            kprev = s.k;
-          }
-          fin = step_fp32(s, q, A.cfg, invT, ch);
-          if (A.want_hash) s.hash = (s.hash ^ (uint64_t)ch) * kFnvPrime;
-        }
-        if (ch == CH_REJ) {
-          tot_rej++;
-        } else if (ch != CH_NULL) {
-          s.ev++;
-          if (s.ev > cap) {
-            err |= STF_EVENT_CAP;
-            fin = true;
-          }
-        }
-        if (s.uu >= kOverflowCount || s.lu >= kOverflowCount || s.us >= kOverflowCount ||
-            s.ls >= kOverflowCount) {
-          err |= STF_OVERFLOW;
-          fin = true;
-        }
-        if (s.stall > kMaxStall) {
-          err |= STF_NONFINITE;
-          fin = true;
-        }
-        if (fin) {
-          A.counts[s.out] = make_int2(s.uu + s.us, s.lu + s.ls);
-          if (A.events) A.events[s.out] = s.ev;
-          if (A.hash) A.hash[s.out] = s.hash;
-          tot_ev += (unsigned long long)s.ev;
-          active = false;
-          break;
-        }
-      }
-    }
-  }
-  // warp totals -> one atomic per warp
-  for (int o = 16; o > 0; o >>= 1) {
-    tot_ev += __shfl_xor_sync(FULL, tot_ev, o);
-    tot_rej += __shfl_xor_sync(FULL, tot_rej, o);
-    err |= __shfl_xor_sync(FULL, err, o);
-  }
-  if (lane == 0) {
-    atomicAdd(&A.totals[0], tot_ev);
-    atomicAdd(&A.totals[1], tot_rej);
-    if (err) atomicOr(A.status, err);
-  }
-}
 
 }  // namespace abc
