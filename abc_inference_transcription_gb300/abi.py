@@ -156,6 +156,8 @@ def _declare(lib: C.CDLL) -> None:
         "abc_profile": (C.c_int, [vp, C.c_int]),
         "abc_autotune": (C.c_int, [vp, C.c_int, dp, i64, u64, dp, C.POINTER(C.c_int)]),
         "abc_set_variant": (C.c_int, [vp, C.c_int]),
+        "abc_autotune_batch": (C.c_int, [vp, i32p, dp, i64, i64, u64, dp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "abc_set_work_chunk": (C.c_int, [vp, C.c_int]),
         "abc_profile_read": (C.c_int, [vp, dp]),
         "abc_errors": (C.c_int, [vp, dp, dp, i64, C.c_int, C.c_int, i32p, dp, i64, dp]),
         "abc_errors_select": (C.c_int, [vp, dp, dp, i64, C.c_int, C.c_int, i32p, dp, i64, C.c_int,
@@ -216,7 +218,8 @@ ABI_SYMBOLS = [
     "abc_create", "abc_destroy", "abc_last_error", "abc_num_params", "abc_num_stats",
     "abc_stream", "abc_set_cells", "abc_sample_prior", "abc_sample_prior_device", "abc_simulate", "abc_simulate_device",
     "abc_synchronize", "abc_simulate_batch", "abc_simulate_batch_device", "abc_simulate_noalloc", "abc_simulate_cells", "abc_last_counters",
-    "abc_profile", "abc_profile_read", "abc_autotune", "abc_set_variant", "abc_errors",
+    "abc_profile", "abc_profile_read", "abc_autotune", "abc_autotune_batch", "abc_set_variant",
+    "abc_set_work_chunk", "abc_errors",
     "abc_errors_select", "abc_errors_select_thr", "abc_errors_select_device", "abc_accept_fetch",
     "abc_select_counters", "abc_select_profile_read", "abc_set_select_errors", "abc_breakpoint_grid", "abc_write_particles", "abc_write_matrix",
     "abc_format_double", "abc_read_particles", "abc_set_distance_mode", "abc_get_distance_mode",

@@ -40,7 +40,15 @@ struct DBuf {
   }
 };
 
-constexpr size_t kChunkBytes = size_t(2) << 30;  // counts buffer budget per simulate chunk
+// counts buffer budget per simulate chunk: 10^6 particles x 2,000 cells run as
+// one persistent launch (16 GB of the GB300's HBM), so the heaviest
+// trajectories of the whole batch start first
+constexpr size_t kChunkBytes = size_t(16) << 30;
+// the production kernel's work cursor is 32-bit: items (particles x cells) per launch below 2^31
+constexpr int64_t kMaxItemsPerLaunch = (int64_t(1) << 31) - 1;
+// work chunks (consecutive items per lane per pull) the batch autotuner times
+constexpr int kTuneChunks[] = {1, 4, 16};
+constexpr int kNumTuneChunks = 3;
 
 }  // namespace
 
@@ -71,6 +79,7 @@ struct abc_ctx {
   DBuf<int> d_status;
   int64_t last_events = 0, last_rej = 0;
   int variant = 0;  // production SSA kernel variant chosen by abc_autotune
+  int work_chunk = 1;  // items a lane takes per pull of the production kernel (abc_set_work_chunk)
   bool graph_mode = false;           // simulate chain as a CUDA graph (abc_set_graph)
   cudaGraphExec_t gexec = nullptr;
   int64_t graph_instantiations = 0, graph_updates = 0;
@@ -390,6 +399,7 @@ static cudaError_t prof_mark(abc_ctx* c) {
 static int prepare_simulate(abc_ctx* c, int64_t P, bool want_cells, int64_t* chunk_out) {
   const int64_t C = c->C;
   int64_t chunk = std::max<int64_t>(1, (int64_t)(kChunkBytes / (sizeof(int2) * (size_t)C)));
+  chunk = std::min<int64_t>(chunk, std::max<int64_t>(1, kMaxItemsPerLaunch / std::max<int64_t>(C, 1)));
   if (want_cells) chunk = P;  // per-cell outputs are requested for small P only
   chunk = std::min<int64_t>(chunk, std::max<int64_t>(P, 1));
   CK(c->d_rec.ensure(chunk));
@@ -457,6 +467,7 @@ static int enqueue_simulate(abc_ctx* c, int model, const int32_t* d_models, cons
     ss.totals = c->d_misc.p + 1;
     ss.status = c->d_status.p;
     ss.want_hash = want_cells ? 1 : 0;
+    ss.chunk = c->work_chunk;
     const int64_t warps_needed = (ss.n_items + 31) / 32;
     int64_t grid = (int64_t)std::max(1, bps) * c->sms;
     grid = std::min<int64_t>(grid, (warps_needed + 3) / 4);
@@ -687,6 +698,47 @@ int abc_simulate_cells(abc_ctx* c, int model, const double* theta, int64_t P, ui
   return st;
 }
 
+// Times the production kernel for every (register variant, work chunk) pair
+// on a sample already on the device (d_models NULL: one model), twice each in
+// alternating order, keeping each pair's faster SSA-kernel time; the context
+// keeps the fastest pair, unless it is within 2 % of the first pair (variant
+// 0, the spill-free allocation, with the first chunk).  ms_out[v * n_chunks + i].
+static int tune_impl(abc_ctx* c, int model, const int32_t* d_models, const double* d_theta, int64_t ld, int64_t P,
+                     uint64_t seed, const int* chunks, int n_chunks, double* ms_out, int* chosen_v, int* chosen_c) {
+  const bool prof = c->prof;
+  c->prof = true;
+  const int n_cfg = kSsaVariants * n_chunks;
+  std::vector<double> t((size_t)n_cfg, 1e300);
+  for (int rep = 0; rep < 2; ++rep) {
+    for (int i = 0; i < n_cfg; ++i) {
+      const int k = rep == 0 ? i : n_cfg - 1 - i;
+      c->variant = k / n_chunks;
+      c->work_chunk = chunks[k % n_chunks];
+      int st = enqueue_simulate(c, model, d_models, d_theta, ld, P, seed, 0, c->d_stats.p, false);
+      if (!st) st = finish_status(c);
+      if (st) {
+        c->prof = prof;
+        c->variant = 0;
+        c->work_chunk = chunks[0];
+        return st;
+      }
+      t[k] = std::min(t[k], (double)c->phase_ms[1]);
+    }
+  }
+  int best = 0;
+  for (int k = 1; k < n_cfg; ++k)
+    if (t[k] < t[best]) best = k;
+  if (t[best] > 0.98 * t[0]) best = 0;
+  if (ms_out)
+    for (int k = 0; k < n_cfg; ++k) ms_out[k] = t[k];
+  c->prof = prof;
+  c->variant = best / n_chunks;
+  c->work_chunk = chunks[best % n_chunks];
+  if (chosen_v) *chosen_v = c->variant;
+  if (chosen_c) *chosen_c = c->work_chunk;
+  return ABC_OK;
+}
+
 int abc_autotune(abc_ctx* c, int model, const double* theta, int64_t P, uint64_t seed, double* ms_out,
                  int* chosen) {
   if (!c) return ABC_ERR_INVALID;
@@ -702,35 +754,37 @@ int abc_autotune(abc_ctx* c, int model, const double* theta, int64_t P, uint64_t
   CK(c->d_theta.ensure((size_t)P * npar));
   CK(c->d_stats.ensure((size_t)P * K));
   CK(cudaMemcpyAsync(c->d_theta.p, theta, sizeof(double) * P * npar, cudaMemcpyHostToDevice, c->stream));
-  const bool prof = c->prof;
-  c->prof = true;
-  // every variant twice, in alternating order, keeping each one's faster time
-  // (first-launch and ordering effects); another variant replaces variant 0
-  // (the one without register spills) only when it is more than 2 % faster
-  double t[kSsaVariants];
-  for (int v = 0; v < kSsaVariants; ++v) t[v] = 1e300;
-  for (int rep = 0; rep < 2; ++rep) {
-    for (int i = 0; i < kSsaVariants; ++i) {
-      const int v = rep == 0 ? i : kSsaVariants - 1 - i;
-      c->variant = v;
-      st = enqueue_simulate(c, model, nullptr, c->d_theta.p, npar, P, seed, 0, c->d_stats.p, false);
-      if (!st) st = finish_status(c);
-      if (st) {
-        c->prof = prof;
-        c->variant = 0;
-        return st;
-      }
-      t[v] = std::min(t[v], (double)c->phase_ms[1]);
-    }
+  const int keep_chunk = c->work_chunk;
+  return tune_impl(c, model, nullptr, c->d_theta.p, npar, P, seed, &keep_chunk, 1, ms_out, chosen, nullptr);
+}
+
+int abc_autotune_batch(abc_ctx* c, const int32_t* models, const double* theta, int64_t ld_theta, int64_t P,
+                       uint64_t seed, double* ms_out, int* chosen_variant, int* chosen_chunk) {
+  if (!c) return ABC_ERR_INVALID;
+  int st = check_sim_args(c, 1, P, 0);
+  if (st) return st;
+  if (P < 1 || !theta || !models) return fail(c, ABC_ERR_INVALID, "abc_autotune_batch: needs a sample");
+  if (ld_theta < npar_max(&c->cfg)) return fail(c, ABC_ERR_INVALID, "ld_theta below the largest npar");
+  for (int64_t p = 0; p < P; ++p)
+    if (models[p] < 1 || models[p] > 5) return fail(c, ABC_ERR_INVALID, "model ids must be 1..5");
+  if (c->cfg.precision != ABC_FP32) {
+    if (chosen_variant) *chosen_variant = 0;
+    if (chosen_chunk) *chosen_chunk = c->work_chunk;
+    return ABC_OK;
   }
-  int best_v = 0;
-  for (int v = 1; v < kSsaVariants; ++v)
-    if (t[v] < 0.98 * t[best_v]) best_v = v;
-  if (ms_out)
-    for (int v = 0; v < kSsaVariants; ++v) ms_out[v] = t[v];
-  c->prof = prof;
-  c->variant = best_v;
-  if (chosen) *chosen = best_v;
+  const int K = ABC_NSTATS(c->cfg.n_ages, c->cfg.n_conds);
+  CK(c->d_models.ensure((size_t)P));
+  CK(c->d_theta.ensure((size_t)P * ld_theta));
+  CK(c->d_stats.ensure((size_t)P * K));
+  CK(cudaMemcpyAsync(c->d_models.p, models, sizeof(int32_t) * P, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->d_theta.p, theta, sizeof(double) * P * ld_theta, cudaMemcpyHostToDevice, c->stream));
+  return tune_impl(c, 0, c->d_models.p, c->d_theta.p, ld_theta, P, seed, kTuneChunks, kNumTuneChunks, ms_out,
+                   chosen_variant, chosen_chunk);
+}
+
+int abc_set_work_chunk(abc_ctx* c, int chunk) {
+  if (!c || chunk < 1 || chunk > 1024) return ABC_ERR_INVALID;
+  c->work_chunk = chunk;
   return ABC_OK;
 }
 

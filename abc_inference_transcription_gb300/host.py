@@ -142,8 +142,22 @@ class Context:
         self._check(self.lib.abc_autotune(self.h, model, ptr(th), th.shape[0], seed, ptr(ms), C.byref(chosen)))
         return chosen.value, ms.tolist()
 
+    def autotune_batch(self, models: np.ndarray, theta: np.ndarray, seed: int = 1) -> tuple[int, int, list[float]]:
+        """Time (register variant x work chunk) on a mixed-model sample and keep the
+        fastest pair: returns (variant, chunk, ms[variant * 3 + chunk index])."""
+        m = np.ascontiguousarray(models, np.int32)
+        th = np.ascontiguousarray(theta, np.float64)
+        ms = np.zeros(6)
+        v, ch = C.c_int(), C.c_int()
+        self._check(self.lib.abc_autotune_batch(self.h, ptr(m, C.c_int32), ptr(th), th.shape[1], th.shape[0], seed,
+                                                ptr(ms), C.byref(v), C.byref(ch)))
+        return v.value, ch.value, ms.tolist()
+
     def set_variant(self, variant: int) -> None:
         self._check(self.lib.abc_set_variant(self.h, variant))
+
+    def set_work_chunk(self, chunk: int) -> None:
+        self._check(self.lib.abc_set_work_chunk(self.h, chunk))
 
     def profile(self, enable: bool = True) -> None:
         self._check(self.lib.abc_profile(self.h, int(enable)))

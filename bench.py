@@ -1,23 +1,30 @@
 #!/usr/bin/env python3
 """Benchmark of the ABC simulation hot path on GB300.
 
-Workload (one step): the five-model ABC batch -- all 5 gene models mixed in
-one persistent FP32 SSA launch (FP64 clock), PER_MODEL particles per model x
-2,000 synthetic cells (1,200 pulse, 800 chase, Beta(4,16) capture), the
-reference time grid (cycle 20 h, 5 age groups, 11 labelling conditions),
-followed by binomial capture and the 53 summary statistics per particle.
-Metric: fired SSA events per second.  A fresh random stream (seed) per step.
+Workload (one step): the five-model ABC batch of 10^6 particles (2 x 10^5 per
+model: constant, constant non-scaling, and k_on / alpha / gamma varying over
+the 5 age groups) x 2,000 synthetic cells (1,200 pulse, 800 chase, Beta(4,16)
+capture), the reference time grid (cycle 20 h, 5 age groups, 11 labelling
+conditions), in one persistent FP32 SSA launch, then binomial capture and the
+53 summary statistics per particle.  Metric: fired SSA events per second.
+Each step is one call of the public host API (abc_simulate_batch: host theta
+in, host statistics out) with a fresh random stream (seed).
 
-  value       device-timed (CUDA events on the library's stream), inputs
-              resident in HBM; the per-cell count buffer (> 129 MB L2) is
-              rewritten every step, so no L2 flush is needed.
-  e2e         the same step through the public host API (abc_simulate_batch
-              with host theta / host statistics, copies inside the timed region).
+  value       events / device time of the step's kernels (setup, work order,
+              SSA, capture + statistics; CUDA events on the library's stream),
+              inputs resident in HBM; the per-cell count buffer (16 GB, > L2)
+              is rewritten every step, so no L2 flush is needed.
+  e2e         the same steps' events / their wall time, host<->device copies
+              of theta and statistics included.
   roofline    SSA kernel against the instruction-issue roofline (algorithmic
               ops per event x events / SSA kernel time vs 152 SMs x 128 lanes x
-              max SM clock); capture+statistics kernel against HBM bandwidth.
+              max SM clock).
   cpu_baseline  the FP64 CPU SSA (oracle port, OpenMP over host cores) on a
               bounded sample of the same particles.
+
+Sections after the headline (flags turn them off / on): the P x G distance
+and top-q acceptance at 5 x 10^6 x 2,000 with an FP64-oracle equality check,
+the moment ODE, and surrogate-screened vs plain ABC.
 
 --impl reference: the CPU implementation alone (rank 0), same metric/config.
 """
@@ -42,7 +49,11 @@ N_CELLS = 2000
 OPS_PER_EVENT = 60
 LANES_PER_SM = 128
 SMS = 152
-PER_MODEL_DEFAULT = 4000
+PER_MODEL_DEFAULT = 200_000  # 10^6 particles over the five models
+# DRAM bytes per (particle, cell) trajectory of the production SSA kernel,
+# measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum) on a
+# 10^4-particle x 2,000-cell launch whose count buffer exceeds L2; None until measured
+SSA_DRAM_BYTES_PER_TRAJECTORY = None
 
 
 def parse():
@@ -53,15 +64,19 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--per-model", type=int, default=PER_MODEL_DEFAULT)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-distance", action="store_true", help="skip the P x G distance section")
-    ap.add_argument("--no-abc", action="store_true", help="skip the plain vs screened ABC section")
+    ap.add_argument("--no-abc", action="store_true", help="skip the plain vs screened ABC section (few genes)")
+    ap.add_argument("--abc-wide", action="store_true",
+                    help="also run screened vs plain ABC at 8, 50 and 2,000 genes (top 1 %%)")
     ap.add_argument("--no-moment", action="store_true", help="skip the moment-ODE section")
-    ap.add_argument("--no-graph", action="store_true", help="skip the CUDA-graph timing of the step")
+    ap.add_argument("--no-graph", action="store_true", help="skip the CUDA-graph check of the chain")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (variant 0, chunk 1)")
     ap.add_argument("--dist-particles", type=int, default=5_000_000)
     ap.add_argument("--genes", type=int, default=2000)
-    ap.add_argument("--section", default="all", choices=["all", "distance", "moment"],
-                    help="'distance' / 'moment' run only that section and print its object")
+    ap.add_argument("--oracle-genes", type=int, default=64,
+                    help="genes of the distance section whose accepted lists are checked against the FP64 oracle")
+    ap.add_argument("--section", default="all", choices=["all", "distance", "moment", "abc"],
+                    help="'distance' / 'moment' / 'abc' run only that section and print its object")
     return ap.parse_args()
 
 
@@ -72,6 +87,11 @@ def load_peaks():
         return pk, "measured"
     except Exception:
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def workload_name(per_model: int) -> str:
+    return (f"five-model ABC batch: 5 x {per_model} particles x {N_CELLS} cells, reference time grid (h), "
+            "factor prior, SSA + capture + 53 statistics")
 
 
 def workload(per_model: int, seed0: int, offset: int):
@@ -157,7 +177,7 @@ def cpu_ssa_rate(cfg, cells, theta, models, seconds: float, threads: int):
     cfg64.precision = FP64
     P = theta.shape[0]
     per_model = P // 5
-    order = np.concatenate([[m * per_model + i for m in range(5)] for i in range(per_model)])
+    order = (np.arange(5)[None, :] * per_model + np.arange(per_model)[:, None]).ravel()
     # increments of 10 particles (2 per model) until the time budget is spent
     n, ev, dt = 0, 0, 0.0
     while n < P and dt < seconds:
@@ -175,7 +195,7 @@ def cpu_ssa_rate(cfg, cells, theta, models, seconds: float, threads: int):
     return ev / dt, n, dt, ev
 
 
-def distance_bench(P: int, G: int, K: int, q: float, seed: int, cpu_seconds: float):
+def distance_bench(P: int, G: int, K: int, q: float, seed: int, cpu_seconds: float, oracle_genes: int = 0):
     """Rejection error matrix + top-q acceptance at P x K x G with FP32
     candidate passes and FP64 rechecks; statistics stand-ins are log-normal
     perturbations of 256 base vectors (a K = 72 width has no reference
@@ -211,6 +231,34 @@ def distance_bench(P: int, G: int, K: int, q: float, seed: int, cpu_seconds: flo
         fast_ms, passes = ctx.select_profile()
         cands, rechecked = ctx.select_counters()
         mode_used = ctx.distance_mode()[1]
+        # the same selection keeping the FP64 error of every accepted pair
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        off_e, idx_e, err_e = ctx.select_device(data, se, stats.data_ptr(), P, 1, q, errors=True)
+        torch.cuda.synchronize()
+        dt_e = time.perf_counter() - t0
+        # accepted lists of the first genes against the FP64 oracle (errors of
+        # all P particles, compute_errors.jl:30-43, then accepted_particles.jl:20-29)
+        oracle_chk = None
+        if oracle_genes > 0:
+            from oracle import oracle as orc
+            orc.build()
+            ng = min(oracle_genes, G)
+            st_h = stats.cpu().numpy()
+            t0 = time.perf_counter()
+            e_orc = orc.errors(data[:ng], se[:ng], st_h, n_threads=os.cpu_count() or 1)
+            o_off, o_idx = orc.accept(e_orc, 1, q)
+            t_orc = time.perf_counter() - t0
+            n_o = int(o_off[ng])
+            gene = np.repeat(np.arange(ng), np.diff(o_off))
+            same_i = bool(np.array_equal(off[:ng + 1], o_off) and np.array_equal(idx[:off[ng]], o_idx))
+            same_e = bool(np.array_equal(off_e[:ng + 1], o_off) and np.array_equal(idx_e[:off_e[ng]], o_idx))
+            same_err = bool(same_e and np.array_equal(err_e[:n_o], e_orc[o_idx - 1, gene]))
+            oracle_chk = {"genes": ng, "particles": P, "accepted_pairs": n_o,
+                          "identical_indices_only_path": same_i, "identical_fp64_error_path": same_e,
+                          "fp64_errors_bit_identical": same_err, "oracle_seconds": t_orc,
+                          "oracle_cores": os.cpu_count()}
+            del st_h, e_orc
         # downstream of the acceptance: posterior summaries of the 10^7 accepted
         # pairs (theta on the device) and model probabilities for the genes
         theta = torch.randn((P, 9), device="cuda", dtype=torch.float64, generator=g)
@@ -266,7 +314,9 @@ def distance_bench(P: int, G: int, K: int, q: float, seed: int, cpu_seconds: flo
     out = {"workload": f"P={P} particles x K={K} statistics x G={G} genes, top {q:g} per gene",
            "pairs_per_s": P * G / dt, "seconds": dt, "accepted": int(off[-1]), "accepted_expected": k * G,
            "candidates": cands, "fp64_rechecked": rechecked, "candidate_passes": passes,
-           "distance_mode": mode_used, "downstream": down}
+           "distance_mode": mode_used, "downstream": down,
+           "fp64_error_path": {"seconds": dt_e, "pairs_per_s": P * G / dt_e, "accepted": int(off_e[-1])},
+           "oracle_check": oracle_chk}
     if mode_used in (1, 2):
         # tcgen05 TF32 MMAs issued per pass: 128 x 256 tiles, depth KA per term, 1 or 3 terms
         ka = -(-2 * K // 32) * 32
@@ -383,14 +433,32 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded prior draws, synthetic cells)",
-        "config": {"workload": f"five-model SSA batch, {args.per_model} particles/model x {N_CELLS} cells, "
-                               "reference time grid (h)", "cells": N_CELLS},
+        "config": {"workload": workload_name(args.per_model), "particles_per_step": 5 * per_model,
+                   "cells": N_CELLS},
         "cpu_baseline": {"value": value, "unit": "events/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference is Julia (not installed); this is the FP64 C restatement of its simulation, "
                 "the exact SSA of the same reaction network",
     }
     print(json.dumps(line))
+
+
+def screened_sections(args):
+    """Surrogate-screened vs plain ABC (the benchmark spec's learned pre-screen)."""
+    from abc_inference_transcription_gb300 import pipeline
+    out = {}
+    # a few genes at a small quantile: the regime where the screen can drop
+    # most draws (top 0.2 % of 10^5 plain draws; four independent sets of 4
+    # genes, one surrogate)
+    out["abc_screened_small_q"] = pipeline.run(genes=(4, 4, 4, 4), per_model_train=40000, per_model_plain=20000,
+                                               screen_factor=10, q=0.002, seed=2, epochs=40)
+    if args.abc_wide:
+        # accepted pairs per second, plain vs screened, top 1 % per gene, for 8,
+        # 50 and the full gene set (the screen's gain falls with the number of
+        # genes a draw must be far from)
+        out["abc_screened"] = pipeline.run(genes=(8, 50, args.genes), per_model_train=20000, per_model_plain=2000,
+                                           screen_factor=10, q=0.01, seed=1, epochs=40)
+    return out
 
 
 def main():
@@ -405,14 +473,17 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    if args.section in ("distance", "moment"):
+    if args.section != "all":
         if rank == 0:
             import __graft_entry__
             __graft_entry__.build()
             if args.section == "distance":
-                print(json.dumps(distance_bench(args.dist_particles, args.genes, 72, 0.001, 5, args.cpu_seconds)))
-            else:
+                print(json.dumps(distance_bench(args.dist_particles, args.genes, 72, 0.001, 5, args.cpu_seconds,
+                                                args.oracle_genes)))
+            elif args.section == "moment":
                 print(json.dumps(moment_bench(40000, args.cpu_seconds)))
+            else:
+                print(json.dumps(screened_sections(args)))
         return
     dist = None
     if world > 1:
@@ -426,23 +497,24 @@ def main():
 
     P_rank = 5 * args.per_model
     cfg, cells, ctx, theta, models = workload(args.per_model, 11, rank * P_rank)
-    ld = theta.shape[1]
     K = ctx.K
-    d_theta = torch.from_numpy(theta).cuda()
-    d_models = torch.from_numpy(models).cuda()
-    d_stats = torch.empty((P_rank, K), dtype=torch.float64, device="cuda")
-    torch.cuda.synchronize()
-    # autotuner: kernel variant timed on a sample of the batch (model 1 rows)
-    n_tune = min(args.per_model, 2000)
-    variant, tune_ms = ctx.autotune(1, theta[:n_tune, :5], seed=7)
+    # autotuner: (register variant x work chunk) on an evenly spaced sample of the batch
+    tune = None
+    if not args.no_tune:
+        n_tune = min(P_rank, 2000)
+        rows = np.linspace(0, P_rank - 1, n_tune).astype(np.int64)
+        variant, chunk, tune_ms = ctx.autotune_batch(models[rows], theta[rows], seed=7)
+        tune = {"chosen_variant": variant, "chosen_chunk": chunk, "variants": [0, 1], "chunks": [1, 4, 16],
+                "ssa_ms": tune_ms, "sample": f"{n_tune} particles spaced evenly over the batch"}
     ctx.profile(True)
 
     def step(seed):
-        ctx.simulate_batch_device(d_models.data_ptr(), d_theta.data_ptr(), ld, P_rank, seed, d_stats.data_ptr(),
-                                  offset=rank * P_rank)
-        ctx.synchronize()
+        """One call of the public host API: host theta in, host statistics out."""
+        t0 = time.perf_counter()
+        st = ctx.simulate_batch(models, theta, seed, offset=rank * P_rank)
+        wall = time.perf_counter() - t0
         ev, rej = ctx.last_counters()
-        return ev, rej, ctx.phase_ms()
+        return ev, rej, np.array(ctx.phase_ms()), wall, st
 
     for w in range(args.warmup):
         step(500 + w)
@@ -456,67 +528,53 @@ def main():
     e0.record(stream)
     tot_ev = tot_rej = 0
     phase = np.zeros(3)
+    wall = 0.0
+    st_host = None
     for k in range(args.steps):
-        ev, rej, ph = step(1000 + k)
+        ev, rej, ph, w_s, st_host = step(1000 + k)
         tot_ev += ev
         tot_rej += rej
-        phase += np.array(ph)
+        phase += ph
+        wall += w_s
     e1.record(stream)
     torch.cuda.synchronize()
     clocks = sampler.stop()
     t_ms = e0.elapsed_time(e1)
+    compute_s = phase.sum() / 1e3
     if dist:
-        t = torch.tensor([t_ms], device="cuda", dtype=torch.float64)
+        t = torch.tensor([t_ms, compute_s, wall], device="cuda", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_ms = float(t.item())
+        t_ms, compute_s, wall = (float(x) for x in t.tolist())
         e = torch.tensor([tot_ev], device="cuda", dtype=torch.float64)
         dist.all_reduce(e, op=dist.ReduceOp.SUM)
         tot_ev_all = float(e.item())
     else:
         tot_ev_all = float(tot_ev)
-    value = tot_ev_all / (t_ms / 1e3)
+    value = tot_ev_all / compute_s
+    e2e = {"value": tot_ev_all / wall, "unit": "events/s", "h2d_bytes_per_step": int(theta.nbytes + models.nbytes),
+           "d2h_bytes_per_step": int(st_host.nbytes), "seconds": wall,
+           "path": "abc_simulate_batch (C ABI) with host theta and host statistics, the timed steps themselves"}
 
-    # the same steps with the chain (setup -> work order -> SSA -> capture +
-    # statistics) as one CUDA graph, updated in place per seed
+    # the chain (setup -> work order -> SSA -> capture + statistics) as one CUDA
+    # graph, against plain launches, on a sub-batch of the same particles
     graph = None
     if not args.no_graph:
+        sub = np.linspace(0, P_rank - 1, min(P_rank, 20000)).astype(np.int64)
         ctx.profile(False)
-        ctx.set_graph(True)
-        step(700)
-        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        g0.record(stream)
-        ng = min(args.steps, 3)
-        for k in range(ng):
-            step(1000 + k)
-        g1.record(stream)
-        torch.cuda.synchronize()
+        res = {}
+        for mode in (False, True):
+            ctx.set_graph(mode)
+            ctx.simulate_batch(models[sub], theta[sub], 700, offset=rank * P_rank)
+            t0 = time.perf_counter()
+            res[mode] = ctx.simulate_batch(models[sub], theta[sub], 701, offset=rank * P_rank)
+            res[(mode, "s")] = time.perf_counter() - t0
         gi, gu = ctx.graph_counters()
-        graph = {"ms_per_step": g0.elapsed_time(g1) / ng, "plain_ms_per_step": t_ms / args.steps,
-                 "instantiations": gi, "in_place_updates": gu, "steps": ng}
         ctx.set_graph(False)
         ctx.profile(True)
-
-    # e2e through the host API
-    e2e = None
-    if not args.no_e2e:
-        st_host = np.zeros((P_rank, K))
-        ctx.simulate_batch(models, theta, 900, offset=rank * P_rank)  # warm host path
-        t0 = time.perf_counter()
-        ev_e2e = 0
-        for k in range(args.steps):
-            st_host = ctx.simulate_batch(models, theta, 1000 + k, offset=rank * P_rank)
-            ev_e2e += ctx.last_counters()[0]
-        dt = time.perf_counter() - t0
-        if dist:
-            t = torch.tensor([dt], device="cuda", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            dt = float(t.item())
-            e = torch.tensor([ev_e2e], device="cuda", dtype=torch.float64)
-            dist.all_reduce(e, op=dist.ReduceOp.SUM)
-            ev_e2e = float(e.item())
-        e2e = {"value": ev_e2e / dt, "unit": "events/s", "h2d_bytes_per_step": int(theta.nbytes + models.nbytes),
-               "d2h_bytes_per_step": int(st_host.nbytes)}
+        graph = {"particles": int(sub.shape[0]), "graph_seconds": res[(True, "s")],
+                 "plain_seconds": res[(False, "s")], "identical_statistics": bool(
+                     np.array_equal(res[True], res[False], equal_nan=True)),
+                 "instantiations": gi, "in_place_updates": gu}
 
     if rank != 0:
         if dist:
@@ -527,8 +585,8 @@ def main():
     ssa_s = phase[1] / 1e3
     achieved_ev = tot_ev / ssa_s
     peak_ev = SMS * LANES_PER_SM * sm_max * 1e6 / OPS_PER_EVENT
-    stats_bytes = args.steps * (P_rank * N_CELLS * 8 + P_rank * K * 8)
-    stats_gbs = stats_bytes / (phase[2] / 1e3) / 1e9
+    trajectories = P_rank * N_CELLS
+    traffic = None if SSA_DRAM_BYTES_PER_TRAJECTORY is None else SSA_DRAM_BYTES_PER_TRAJECTORY * trajectories
     cpu = None
     try:
         if args.cpu_seconds <= 0:
@@ -542,32 +600,31 @@ def main():
     line = {
         "metric": "SSA events/s", "value": value, "unit": "events/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (FP64 clock)", "data": "synthetic (seeded prior draws, synthetic cells)",
-        "config": {"workload": f"five-model SSA batch: 5 x {args.per_model} particles x {N_CELLS} cells, "
-                               "reference time grid (h), factor prior, capture + 53 statistics",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded prior draws, synthetic cells)",
+        "config": {"workload": workload_name(args.per_model),
                    "particles_per_step": P_rank * world, "cells": N_CELLS, "parallelism": f"particle shards x{world}",
-                   "l2": "per-cell count buffer (P x C x 8 B) exceeds L2 and is rewritten every step"},
+                   "l2": "per-cell count buffer (P x C x 8 B = 16 GB at 10^6 particles) exceeds L2 and is "
+                         "rewritten every step"},
         "events_per_step": tot_ev_all / args.steps, "thinning_rejections": tot_rej,
-        "particles_per_s": P_rank * world * args.steps / (t_ms / 1e3),
-        "phase_ms_per_step": {"setup": phase[0] / args.steps, "ssa": phase[1] / args.steps,
+        "particles_per_s": P_rank * world * args.steps / compute_s,
+        "phase_ms_per_step": {"setup_and_work_order": phase[0] / args.steps, "ssa": phase[1] / args.steps,
                               "capture_stats": phase[2] / args.steps},
         "roofline": {"bound": "issue", "achieved": achieved_ev / 1e9, "peak": peak_ev / 1e9, "unit": "Gevents/s",
-                     "frac": achieved_ev / peak_ev, "traffic": None,
+                     "frac": achieved_ev / peak_ev, "traffic": traffic,
                      "basis": f"{OPS_PER_EVENT} algorithmic ops/event, {SMS} SMs x {LANES_PER_SM} lanes x "
-                              f"{sm_max:.0f} MHz ({peak_src} sm_max)"},
-        "roofline_stats": {"bound": "hbm", "achieved": stats_gbs, "peak": float(peaks.get("hbm_gbs", 6800.0)),
-                           "unit": "GB/s", "frac": stats_gbs / float(peaks.get("hbm_gbs", 6800.0)),
-                           "traffic": None, "peak_source": peak_src},
+                              f"{sm_max:.0f} MHz ({peak_src} sm_max); traffic = DRAM bytes per launch, "
+                              "per-trajectory figure from ncu x trajectories"},
         "cpu_baseline": cpu,
         "e2e": e2e,
-        "gpu_launches": 5 * args.steps,  # setup, 2 work-order kernels, SSA, capture+statistics
-        "autotune": {"chosen_variant": variant, "ssa_ms_per_variant": tune_ms, "sample": f"{n_tune} particles"},
+        "gpu_launches": 5 * args.steps,  # per step: setup, 2 work-order kernels, SSA, capture+statistics
+        "autotune": tune,
         "cuda_graph": graph,
         "clocks": clocks,
     }
     if not args.no_distance:
         try:
-            line["distance"] = distance_bench(args.dist_particles, args.genes, 72, 0.001, 5, args.cpu_seconds)
+            line["distance"] = distance_bench(args.dist_particles, args.genes, 72, 0.001, 5, args.cpu_seconds,
+                                              args.oracle_genes)
         except Exception as exc:
             line["distance"] = {"error": repr(exc)}
     if not args.no_moment:
@@ -577,20 +634,9 @@ def main():
             line["moment_ode"] = {"error": repr(exc)}
     if not args.no_abc:
         try:
-            from abc_inference_transcription_gb300 import pipeline
-            # accepted pairs per second, plain vs surrogate-screened, top 1 % per gene,
-            # for 8, 50 and the full gene set (the screen's gain falls with the
-            # number of genes a draw must be far from)
-            line["abc_screened"] = pipeline.run(genes=(8, 50, args.genes), per_model_train=20000,
-                                                per_model_plain=2000, screen_factor=10, q=0.01, seed=1, epochs=40)
-            # a few genes at a small quantile: the regime where the screen can
-            # drop most draws (top 0.2 % of 10^5 plain draws; four independent
-            # sets of 4 genes, one surrogate)
-            line["abc_screened_small_q"] = pipeline.run(genes=(4, 4, 4, 4), per_model_train=40000,
-                                                        per_model_plain=20000, screen_factor=10, q=0.002, seed=2,
-                                                        epochs=40)
+            line.update(screened_sections(args))
         except Exception as exc:
-            line["abc_screened"] = {"error": repr(exc)}
+            line["abc_screened_small_q"] = {"error": repr(exc)}
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

@@ -198,7 +198,20 @@ int abc_breakpoint_grid(const abc_config* cfg, double* quantum);
  * milliseconds of each variant (2 entries, may be NULL). */
 int abc_autotune(abc_ctx* ctx, int model, const double* theta, int64_t n_particles, uint64_t seed,
                  double* ms_out, int* chosen);
+/* Autotuner over the kernel's two tunable axes, on a mixed-model sample
+ * (rows padded to ld_theta, as abc_simulate_batch; no reference
+ * counterpart): register variant (8 or 10 resident blocks per SM) x work
+ * chunk (1, 4 or 16 consecutive (particle, cell) items per lane and pull),
+ * each pair timed twice in alternating order; the context keeps the fastest
+ * pair unless it is within 2 % of (variant 0, chunk 1).  ms_out: 6 entries,
+ * ms_out[variant * 3 + chunk index] (may be NULL). */
+int abc_autotune_batch(abc_ctx* ctx, const int32_t* models, const double* theta, int64_t ld_theta,
+                       int64_t n_particles, uint64_t seed, double* ms_out, int* chosen_variant,
+                       int* chosen_chunk);
 int abc_set_variant(abc_ctx* ctx, int variant);
+/* Work items (consecutive cells of a particle) a lane of the production
+ * kernel takes per pull from the work counter, 1..1024 (default 1). */
+int abc_set_work_chunk(abc_ctx* ctx, int chunk);
 int abc_profile_read(const abc_ctx* ctx, double* ms_out);
 
 /* Error matrix, compute_trunc_errors / nlsqerror_part (scripts/compute_errors.jl:30-70):

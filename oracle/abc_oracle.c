@@ -1076,31 +1076,48 @@ static int cmp_pair(const void* x, const void* y) {
   return (a->i < b->i) ? -1 : (a->i > b->i);
 }
 
+/* Per gene (accepted_particles.jl:20-29): the particles with err <= eps (mode
+ * 0) or the ceil(q P) smallest finite errors (mode 1), sorted by (err, index),
+ * 1-based.  The list lengths need no sort, so offsets are counted first; the
+ * lists are then filled one gene per thread (idx == NULL: offsets only). */
 int64_t orc_accept(const double* err, int64_t P, int64_t G, int mode, double eps_or_q,
                    int64_t* offsets, int64_t* idx, int64_t cap) {
-  pair_t* buf = (pair_t*)malloc(sizeof(pair_t) * (size_t)(P > 0 ? P : 1));
-  int64_t total = 0;
-  int64_t kq = (int64_t)ceil(eps_or_q * (double)P);
+  const int64_t kq = (int64_t)ceil(eps_or_q * (double)P);
   offsets[0] = 0;
   for (int64_t g = 0; g < G; ++g) {
     int64_t n = 0;
     for (int64_t p = 0; p < P; ++p) {
-      double e = err[p * G + g];
+      const double e = err[p * G + g];
       if (e != e) continue;
       if (mode == 0 && !(e <= eps_or_q)) continue;
-      buf[n].e = e;
-      buf[n].i = p;
       n++;
     }
-    qsort(buf, (size_t)n, sizeof(pair_t), cmp_pair);
     if (mode == 1 && n > kq) n = kq;
-    for (int64_t q = 0; q < n; ++q) {
-      if (total + q < cap) idx[total + q] = buf[q].i + 1;
-    }
-    total += n;
-    offsets[g + 1] = total;
+    offsets[g + 1] = offsets[g] + n;
   }
-  free(buf);
+  const int64_t total = offsets[G];
+  if (!idx) return total;
+#pragma omp parallel
+  {
+    pair_t* buf = (pair_t*)malloc(sizeof(pair_t) * (size_t)(P > 0 ? P : 1));
+#pragma omp for schedule(dynamic, 1)
+    for (int64_t g = 0; g < G; ++g) {
+      int64_t n = 0;
+      for (int64_t p = 0; p < P; ++p) {
+        const double e = err[p * G + g];
+        if (e != e) continue;
+        if (mode == 0 && !(e <= eps_or_q)) continue;
+        buf[n].e = e;
+        buf[n].i = p;
+        n++;
+      }
+      qsort(buf, (size_t)n, sizeof(pair_t), cmp_pair);
+      const int64_t len = offsets[g + 1] - offsets[g];
+      for (int64_t q = 0; q < len; ++q)
+        if (offsets[g] + q < cap) idx[offsets[g] + q] = buf[q].i + 1;
+    }
+    free(buf);
+  }
   return total;
 }
 
