@@ -7,6 +7,7 @@
 #include <atomic>
 
 #include "bitonic.cuh"
+#include "smem_attr.h"
 #include "distance.cuh"
 #include "kernels.h"
 
@@ -585,12 +586,9 @@ cudaError_t launch_dist_group(const Cand* cand, int64_t n, int64_t G, int64_t* g
 static cudaError_t launch_segsort(const int64_t* goff, int64_t G, int32_t* sp, double* se64, const int* dirty,
                                   cudaStream_t s) {
   constexpr int smem = kSortSmem * (int)(sizeof(uint64_t) + sizeof(int32_t));
-  static std::atomic<bool> attr{false};  // the attribute call is idempotent; shared by all contexts
-  if (!attr) {
-    cudaError_t err = cudaFuncSetAttribute(segsort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (err) return err;
-    attr = true;
-  }
+  static std::atomic<uint64_t> attr{0};  // devices where the limit is set, shared by all contexts
+  cudaError_t err = set_smem_once(attr, segsort_kernel, smem);
+  if (err) return err;
   segsort_kernel<<<(unsigned)G, 1024, smem, s>>>(goff, sp, se64, dirty);
   return cudaGetLastError();
 }

@@ -33,6 +33,7 @@
 #include <cstring>
 
 #include "distance.cuh"
+#include "smem_attr.h"
 #include "kernels.h"
 #include "tcgen05.cuh"
 
@@ -522,13 +523,9 @@ bool make_map(CUtensorMap* map, const float* base, int64_t rows, int64_t cols, i
 
 template <int NH>
 cudaError_t launch_nh(const float* A, const float* B, const TcArgs& args, int grid, cudaStream_t s) {
-  static std::atomic<bool> attr{false};  // the attribute call is idempotent; shared by all contexts
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(dist_tc_kernel<NH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)Cfg<NH>::kSmem);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  static std::atomic<uint64_t> attr{0};  // devices where the limit is set, shared by all contexts
+  cudaError_t e = set_smem_once(attr, dist_tc_kernel<NH>, (int)Cfg<NH>::kSmem);
+  if (e != cudaSuccess) return e;
   CUtensorMap ma, mb;
   const int64_t ld = (int64_t)NH * args.KA;
   if (!make_map(&ma, A, args.P, ld, BM) || !make_map(&mb, B, args.G, ld, BN)) return cudaErrorInvalidValue;

@@ -14,9 +14,11 @@
 //                          (scripts/model_probs.jl:54-61), posterior estimates
 //                          (scripts/posterior_kinetics.jl:72-75).
 // Floats are written in the shortest form that reads back to the same double,
-// in Julia's spelling: a ".0" on integral values, exponents as "e-5", NaN,
-// Inf and -Inf.  Host code only; no GPU is involved.
+// in Julia's spelling: fixed notation for 1e-4 <= |x| < 1e6 with a ".0" on
+// integral values, otherwise an unpadded exponent ("1.0e-5", "1.234567e6"),
+// NaN, Inf and -Inf.  Host code only; no GPU is involved.
 #include <charconv>
+#include <cstdlib>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -27,7 +29,12 @@
 
 namespace {
 
-// Julia-style shortest decimal of x into buf; returns the length
+// Julia-style shortest decimal of x into buf; returns the length.  The digits
+// are the shortest that read back to the same double; the notation follows
+// Julia's float printing: with the decimal point pt places after the first
+// digit's position (x = 0.d1d2... x 10^pt), fixed notation when -4 < pt <= 6
+// (1e-4 <= |x| < 1e6: 100000.0, 0.0001, 0.00025, 123456.7), otherwise one
+// digit, a point and an unpadded exponent (1.0e6, 1.234567e6, 1.0e-5).
 int format_double(double x, char* buf) {
   if (std::isnan(x)) {
     std::memcpy(buf, "NaN", 3);
@@ -42,34 +49,46 @@ int format_double(double x, char* buf) {
     return 4;
   }
   char tmp[64];
-  const auto res = std::to_chars(tmp, tmp + sizeof(tmp), x);
+  const auto res = std::to_chars(tmp, tmp + sizeof(tmp), x, std::chars_format::scientific);
   const int n = (int)(res.ptr - tmp);
-  // split mantissa / exponent
-  int epos = -1;
-  for (int i = 0; i < n; ++i)
-    if (tmp[i] == 'e') {
-      epos = i;
-      break;
+  tmp[n] = '\0';  // to_chars does not terminate; atoi below needs it
+  int i = 0, o = 0;
+  if (tmp[i] == '-') {
+    buf[o++] = '-';
+    ++i;
+  }
+  char dig[32];
+  int nd = 0;
+  for (; i < n && tmp[i] != 'e'; ++i)
+    if (tmp[i] != '.') dig[nd++] = tmp[i];
+  int e10 = 0;
+  if (i < n) e10 = std::atoi(tmp + i + 1);
+  const int pt = e10 + 1;
+  if (-4 < pt && pt <= 6) {
+    if (pt <= 0) {
+      buf[o++] = '0';
+      buf[o++] = '.';
+      for (int k = 0; k < -pt; ++k) buf[o++] = '0';
+      for (int k = 0; k < nd; ++k) buf[o++] = dig[k];
+    } else if (pt < nd) {
+      for (int k = 0; k < pt; ++k) buf[o++] = dig[k];
+      buf[o++] = '.';
+      for (int k = pt; k < nd; ++k) buf[o++] = dig[k];
+    } else {
+      for (int k = 0; k < nd; ++k) buf[o++] = dig[k];
+      for (int k = nd; k < pt; ++k) buf[o++] = '0';
+      buf[o++] = '.';
+      buf[o++] = '0';
     }
-  const int mlen = epos < 0 ? n : epos;
-  bool has_dot = false;
-  for (int i = 0; i < mlen; ++i) has_dot = has_dot || tmp[i] == '.';
-  int o = 0;
-  std::memcpy(buf, tmp, mlen);
-  o = mlen;
-  if (!has_dot) {
-    buf[o++] = '.';
-    buf[o++] = '0';
+    return o;
   }
-  if (epos >= 0) {
-    buf[o++] = 'e';
-    int i = epos + 1;
-    if (tmp[i] == '+') ++i;
-    if (tmp[i] == '-') buf[o++] = tmp[i++];
-    while (i < n - 1 && tmp[i] == '0') ++i;  // no zero padding of the exponent
-    while (i < n) buf[o++] = tmp[i++];
-  }
-  return o;
+  buf[o++] = dig[0];
+  buf[o++] = '.';
+  if (nd == 1) buf[o++] = '0';
+  for (int k = 1; k < nd; ++k) buf[o++] = dig[k];
+  buf[o++] = 'e';
+  const auto r2 = std::to_chars(buf + o, buf + o + 8, pt - 1);
+  return (int)(r2.ptr - buf);
 }
 
 int format_int(long long v, char* buf) {

@@ -21,6 +21,7 @@
 #include <cstring>
 
 #include "kernels.h"
+#include "smem_attr.h"
 #include "mlp.cuh"
 #include "tcgen05.cuh"
 
@@ -201,12 +202,9 @@ bool make_map3(CUtensorMap* map, const __nv_bfloat16* base, int64_t K, int64_t l
 
 template <int EPI>
 cudaError_t launch_epi(const CUtensorMap& ma, const CUtensorMap& mb, const TcGemm& g, int members, cudaStream_t s) {
-  static std::atomic<bool> attr{false};  // the attribute call is idempotent; shared by all contexts
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(mlp_tc_kernel<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  static std::atomic<uint64_t> attr{0};  // devices where the limit is set, shared by all contexts
+  cudaError_t e = set_smem_once(attr, mlp_tc_kernel<EPI>, kSmem);
+  if (e != cudaSuccess) return e;
   const int n_mt = (g.M + BM - 1) / BM;
   dim3 grid((unsigned)((g.N + BN - 1) / BN), (unsigned)(n_mt * g.k_split), (unsigned)members);
   mlp_tc_kernel<EPI><<<grid, 128, kSmem, s>>>(ma, mb, g);

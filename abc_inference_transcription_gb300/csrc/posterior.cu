@@ -8,6 +8,7 @@
 #include <atomic>
 
 #include "common.cuh"
+#include "smem_attr.h"
 #include "kernels.h"
 
 namespace abc {
@@ -303,12 +304,9 @@ cudaError_t launch_posterior_summary(const int64_t* aoff, const int64_t* idx, in
   if (total > 0) {
     post_gather_kernel<<<(unsigned)G, 256, 0, s>>>(aoff, idx, theta, ld, npar, total, scratch);
     constexpr int smem = kPostSmem * (int)sizeof(uint64_t);
-    static std::atomic<bool> attr{false};  // the attribute call is idempotent; shared by all contexts
-    if (!attr) {
-      cudaError_t e = cudaFuncSetAttribute(post_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-      if (e != cudaSuccess) return e;
-      attr = true;
-    }
+    static std::atomic<uint64_t> attr{0};  // devices where the limit is set, shared by all contexts
+    cudaError_t e = set_smem_once(attr, post_select_kernel, smem);
+    if (e != cudaSuccess) return e;
     post_select_kernel<<<(unsigned)(G * npar), kSelThreads, smem, s>>>(aoff, total, G, scratch, q, q4);
   }
   const int64_t n = G * npar;

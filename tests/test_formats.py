@@ -17,6 +17,11 @@ def F(built):
 def test_float_spelling_and_round_trip(F):
     assert [F.format_double(x) for x in (1.0, 0.1, 1e-5, 123456.0, 1e16, -0.0, np.nan, np.inf, -np.inf)] == \
         ["1.0", "0.1", "1.0e-5", "123456.0", "1.0e16", "-0.0", "NaN", "Inf", "-Inf"]
+    # Julia switches to exponent notation outside 1e-4 <= |x| < 1e6
+    assert [F.format_double(x) for x in (1e5, 1e-4, 2.5e-4, 999999.0, 1e6, 1234567.0, -0.00012, 123456.7, 0.5e-4,
+                                         3.0e-300, 12.5)] == \
+        ["100000.0", "0.0001", "0.00025", "999999.0", "1.0e6", "1.234567e6", "-0.00012", "123456.7", "5.0e-5",
+         "3.0e-300", "12.5"]
     rng = np.random.default_rng(1)
     xs = np.concatenate([rng.normal(size=2000) * 10.0 ** rng.integers(-300, 300, 2000),
                          rng.integers(-10 ** 6, 10 ** 6, 500).astype(float), [5e-324, 1.7976931348623157e308]])
