@@ -69,7 +69,7 @@ class AbcPrior(C.Structure):
 
 
 def nstats(n_ages: int, n_conds: int) -> int:
-    """4A + 3J, scripts/compute_errors.jl:148."""
+    """4A + 3J, scripts/compute_errors.jl:51."""
     return 4 * n_ages + 3 * n_conds
 
 

@@ -20,7 +20,7 @@ REF_PULSE_H = [0.25, 0.5, 0.75, 1.0, 2.0, 3.0, 22.0, 22.0, 22.0, 22.0, 22.0]
 REF_CHASE_H = [0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 1.0, 2.0, 4.0, 6.0]
 N_PULSE_CONDS = 6
 TAU = [(2 * k + 1) / (2 * 5) for k in range(5)]  # load_process_data.jl:52
-# reference statistic families (compute_errors.jl:152-154): sizes for A=5, J=11
+# reference statistic families (compute_errors.jl:55-57): sizes for A=5, J=11
 REF_FAMILIES = [5, 5, 5, 5, 11, 11, 11]
 
 

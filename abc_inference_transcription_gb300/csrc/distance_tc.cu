@@ -468,7 +468,7 @@ __global__ void tc_prep_genes_kernel(const double* data, const double* se, int64
 }
 
 // Y_g = K X_g - c_g rounded up; X < 0 accepts no pair.  Errors are clipped at
-// 10 (scripts/compute_errors.jl:159-161), so X >= 10 accepts every finite pair,
+// 10 (scripts/compute_errors.jl:62-64), so X >= 10 accepts every finite pair,
 // however large its unclipped error.
 __global__ void tc_y_kernel(const float* X, const double* cg64, int64_t G, int K, float* Y) {
   const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;

@@ -110,7 +110,7 @@ __device__ __forceinline__ U4 philox_rk(U4 c, const uint32_t* rk) {
 }
 
 // Block `block` of the main stream, counter (block, ST_SSA << 30, cell,
-// particle): round 1 needs only the product of the block word, the rest of
+// particle): the first Philox round needs only the product of the block word, the rest of
 // it (r1x, r1y, r1z) is fixed per trajectory.
 __device__ __forceinline__ U4 main_block(uint32_t block, uint32_t r1x, uint32_t r1y, uint32_t r1z,
                                          const uint32_t* rk) {

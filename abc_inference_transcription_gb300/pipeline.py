@@ -72,7 +72,7 @@ def make_genes(stats: np.ndarray, G: int, rng: np.random.Generator):
     return data, se
 
 
-CLIP = 10.0  # errors are clipped at 10 (scripts/compute_errors.jl:159-161)
+CLIP = 10.0  # errors are clipped at 10 (scripts/compute_errors.jl:62-64)
 
 
 def thresholds_from_lists(off: np.ndarray, err: np.ndarray) -> np.ndarray:

@@ -444,7 +444,7 @@ def run_reference(args):
 
 
 def screened_sections(args):
-    """Surrogate-screened vs plain ABC (the benchmark spec's learned pre-screen)."""
+    """Surrogate-screened vs plain ABC (the learned pre-screen of prior draws)."""
     from abc_inference_transcription_gb300 import pipeline
     out = {}
     # a few genes at a small quantile: the regime where the screen can drop

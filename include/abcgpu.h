@@ -11,7 +11,7 @@
  *     or traps; abc_last_error() returns a message for the last failure.
  *   - Matrices are ROW-MAJOR with the row index first ("P x npar" means row p
  *     holds particle p).  A Julia caller passes the transpose of its
- *     column-major matrix (identical memory), see INTEGRATION.md.
+ *     column-major matrix (identical memory).
  *   - Particle indices returned by the acceptance step are 1-based (reference
  *     convention, scripts/accepted_particles.jl:20-26).
  *   - Host pointers unless the function name ends in _device.
@@ -34,7 +34,7 @@ extern "C" {
 #define ABC_MAX_PARAMS 32
 #define ABC_MAX_FAMILIES 16
 
-/* Statistics per particle in the reference layout (scripts/compute_errors.jl:148,152-154):
+/* Statistics per particle in the reference layout (scripts/compute_errors.jl:51,55-57):
  * pulse_mean[A], pulse_ff[A], chase_mean[A], chase_ff[A], ratio[J], mean_corr[J], corr_mean[J]. */
 #define ABC_NSTATS(A, J) (4 * (A) + 3 * (J))
 
@@ -61,7 +61,7 @@ typedef enum abc_model {
 
 typedef enum abc_precision {
   ABC_FP64 = 0, /* oracle mode: bit-exact with the FP64 CPU oracle */
-  ABC_FP32 = 1  /* production mode: FP32 propensities, FP64 clock */
+  ABC_FP32 = 1  /* production mode: FP32 propensities and interval clock, exact breakpoints */
 } abc_precision;
 
 /* Time grid, labelling conditions and model options (all times in the unit of
@@ -104,7 +104,7 @@ const char* abc_last_error(const abc_ctx* ctx);
 /* Number of theta columns for a model under this context's configuration
  * (get_vary_map, scripts/model.jl:30-43, plus the optional extensions). */
 int abc_num_params(const abc_ctx* ctx, int model);
-/* Number of statistics per particle, 4A + 3J (scripts/compute_errors.jl:148). */
+/* Number of statistics per particle, 4A + 3J (scripts/compute_errors.jl:51). */
 int abc_num_stats(const abc_ctx* ctx);
 /* cudaStream_t used by the context, as void*. */
 void* abc_stream(abc_ctx* ctx);

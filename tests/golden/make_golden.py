@@ -1,8 +1,8 @@
 """Generate the golden fixtures from the reference's shipped data.
 
-Run in a checkout that has the reference project at REF (default
-/root/reference); the outputs are committed so that tests never read the
-reference at run time:
+Run with the reference project's checkout as the argument,
+  python tests/golden/make_golden.py <path to the reference project>
+the outputs are committed so that tests never read the reference at run time:
 
   recovered_statistics.npz  theta_MAP rows (data/posterior_estimates/map_sets_<model>.txt)
                             and the moments the reference computed for them without
@@ -10,7 +10,7 @@ reference at run time:
                             written by scripts/recover_statistics.jl:49-68)
   summary_stats.npz         data-side statistics and standard errors of the first
                             N_GENES genes (data/summary_stats/*.txt, 53 per gene in the
-                            family order of scripts/compute_errors.jl:152-153)
+                            family order of scripts/compute_errors.jl:55-57)
   capture_efficiencies.npy  the 5,422 per-cell capture efficiencies (data/capture_efficiencies.txt)
 """
 from __future__ import annotations
@@ -20,7 +20,6 @@ import sys
 
 import numpy as np
 
-REF = os.environ.get("ABC_REFERENCE", "/root/reference")
 HERE = os.path.dirname(os.path.abspath(__file__))
 MODELS = ["const", "const_const", "kon", "alpha", "gamma"]
 COND_IDS = ["pulse_15", "pulse_30", "pulse_45", "pulse_60", "pulse_120", "pulse_180",
@@ -31,7 +30,9 @@ N_GENES = 256
 
 
 def main() -> None:
-    data = os.path.join(REF, "data")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path to the reference project>")
+    data = os.path.join(sys.argv[1], "data")
     if not os.path.isdir(data):
         sys.exit(f"reference data not found under {data}")
     out = {}
