@@ -446,8 +446,6 @@ static int enqueue_simulate(abc_ctx* c, int model, const int32_t* d_models, cons
     CK(prof_mark(c));
     CK(launch_setup(sa, c->stream));
     CK(launch_work_order(c->d_rec.p, n, c->d_ohist.p, c->d_order.p, c->stream));
-    CK(prof_mark(c));
-    CK(cudaMemsetAsync(c->d_misc.p, 0, sizeof(unsigned long long), c->stream));
     SsaArgs ss;
     ss.cfg = sa.cfg;
     ss.rec = c->d_rec.p;
@@ -468,6 +466,10 @@ static int enqueue_simulate(abc_ctx* c, int model, const int32_t* d_models, cons
     ss.status = c->d_status.p;
     ss.want_hash = want_cells ? 1 : 0;
     ss.chunk = c->work_chunk;
+    // production mode: the trajectories' initial states, drawn in FP64 before the SSA
+    if (!fp64) CK(launch_init_states(ss, c->sms, c->stream));
+    CK(prof_mark(c));
+    CK(cudaMemsetAsync(c->d_misc.p, 0, sizeof(unsigned long long), c->stream));
     const int64_t warps_needed = (ss.n_items + 31) / 32;
     int64_t grid = (int64_t)std::max(1, bps) * c->sms;
     grid = std::min<int64_t>(grid, (warps_needed + 3) / 4);

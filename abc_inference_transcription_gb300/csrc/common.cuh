@@ -324,6 +324,53 @@ ABC_HD int64_t btrd(Rng& rr, int64_t n, double p) {
   }
 }
 
+// log(k!) from the Stirling series with the tabulated correction above.
+ABC_HD double logfact(double k) {
+  return (((k + 0.5) * xlog(k + 1.0) - (k + 1.0)) + 0.9189385332046728) + stirling_fc(k);
+}
+
+// Poisson(lam): inversion by sequential search below lam = 10, otherwise
+// PTRS, the transformed rejection with squeeze of W. Hormann, "The
+// transformed rejection method for generating Poisson random variables",
+// Insurance: Mathematics and Economics 12 (1993) 39-45.  Both loops are
+// bounded (the acceptance rate of PTRS is about 0.9 per try).
+ABC_HD int64_t poisson(Rng& r, double lam) {
+  if (!(lam > 0.0)) return 0;
+  uint32_t w0, w1;
+  if (lam < 10.0) {
+    rng_pair(r, w0, w1);
+    double u = u52(w0, w1);
+    double f = xexp(-lam);
+    int64_t k = 0;
+    while (u >= f && k < 1000) {
+      u = u - f;
+      k = k + 1;
+      f = f * (lam / (double)k);
+    }
+    return k;
+  }
+  const double slam = sqrt(lam);
+  const double loglam = xlog(lam);
+  const double b = 0.931 + 2.53 * slam;
+  const double a = -0.059 + 0.02483 * b;
+  const double inv_alpha = 1.1239 + 1.1328 / (b - 3.4);
+  const double vr = 0.9277 - 3.6224 / (b - 2.0);
+  for (int it = 0; it < 1000; ++it) {
+    rng_pair(r, w0, w1);
+    const double U = u52(w0, w1) - 0.5;
+    rng_pair(r, w0, w1);
+    const double V = u52open(w0, w1);
+    const double us = 0.5 - fabs(U);
+    const double kd = floor((((2.0 * a) / us + b) * U + lam) + 0.43);
+    if (us >= 0.07 && V <= vr) return (int64_t)kd;
+    if (kd < 0.0 || (us < 0.013 && V > us)) continue;
+    const double lhs = xlog((V * inv_alpha) / (a / (us * us) + b));
+    const double rhs = (kd * loglam - lam) - logfact(kd);
+    if (lhs <= rhs) return (int64_t)kd;
+  }
+  return (int64_t)floor(lam + 0.5);
+}
+
 ABC_HD int64_t binomial(Rng& r, int64_t n, double p) {
   if (n <= 0 || !(p > 0.0)) return 0;
   if (p >= 1.0) return n;

@@ -204,6 +204,11 @@ cudaError_t launch_posterior_summary(const int64_t* aoff, const int64_t* idx, in
 cudaError_t launch_prior(const PriorArgs& a, cudaStream_t s);
 cudaError_t launch_setup(const SetupArgs& a, cudaStream_t s);
 cudaError_t launch_ssa_fp64(const SsaArgs& a, int grid, cudaStream_t s);
+// Initial state of every (particle, cell) trajectory of a production-SSA
+// launch, in FP64 exactly as the oracle mode draws it: counts[item] =
+// (first mRNA count, gene state).  The production kernel reads it at the
+// trajectory start and overwrites it with the final counts.
+cudaError_t launch_init_states(const SsaArgs& a, int sms, cudaStream_t s);
 constexpr int kSsaVariants = 2;
 cudaError_t launch_ssa_fp32(const SsaArgs& a, int grid, cudaStream_t s, int variant = 0);
 cudaError_t launch_stats(const StatsArgs& a, cudaStream_t s);

@@ -71,7 +71,7 @@ __global__ void setup_kernel(SetupArgs A) {
     atomicOr(A.status, STF_NONFINITE);
     // a harmless record: the trajectory sees no reactions
     for (int k = 0; k < kMaxSteps; ++k) R.kon[k] = R.alp[k] = R.gam[k] = R.amax[k] = 0.0;
-    R.koff = R.lam = R.beta = R.scal = R.g0 = R.u0 = R.s0 = 0.0;
+    R.koff = R.lam = R.beta = R.scal = R.g0 = R.u0 = R.s0 = R.c0 = R.v0 = 0.0;
     R.cost = 1.0;
   }
   A.rec[p] = R;
@@ -187,6 +187,43 @@ __global__ void __launch_bounds__(128) ssa_kernel_fp64(SsaArgs A) {
 
 cudaError_t launch_ssa_fp64(const SsaArgs& a, int grid, cudaStream_t s) {
   ssa_kernel_fp64<<<grid, 128, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// One thread per trajectory: the gene state from the first word of the
+// trajectory's main stream and the moment-matched first mRNA count
+// (initial_count, auxiliary stream), the draws traj_init makes.  Runs on
+// the FP64 pipe at full occupancy instead of inside the production kernel's
+// divergent refill path.
+__global__ void __launch_bounds__(256) init_state_kernel(SsaArgs A) {
+  const int64_t n = A.n_items;
+  for (int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; item < n;
+       item += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t pl = item / A.n_cells;
+    const int64_t ci = item - pl * A.n_cells;
+    const PRec& R = A.rec[pl];
+    const uint32_t cell = A.cell_id[ci], particle = (uint32_t)(A.p_offset + pl);
+    Rng r;
+    rng_init(r, A.seed, ST_SSA, cell, particle);
+    uint32_t w0, w1;
+    rng_pair(r, w0, w1);
+    const int G = ((double)w0 * ABC_TWO_M32 < R.g0) ? 1 : 0;
+    int64_t u;
+    if (A.cfg.splicing) {
+      u = (int64_t)floor(R.u0 + 0.5);
+    } else {
+      Rng aux;
+      rng_init(aux, A.seed, ST_AUX, cell, particle);
+      u = initial_count(R, G, w1, aux);
+    }
+    A.counts[item] = make_int2((int)(u < 2147483647 ? u : 2147483647), G);
+  }
+}
+
+cudaError_t launch_init_states(const SsaArgs& a, int sms, cudaStream_t s) {
+  if (a.n_items <= 0) return cudaSuccess;
+  const int64_t want = (a.n_items + 255) / 256, cap = (int64_t)sms * 16;
+  init_state_kernel<<<(unsigned)(want < cap ? want : cap), 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 

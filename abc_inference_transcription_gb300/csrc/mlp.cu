@@ -99,8 +99,9 @@ __global__ void mlp_gather_kernel(const float* xn, const float* yn, int64_t N, i
 // Gaussian negative log-likelihood on standardised targets; dY = dL/dY / count.
 constexpr float kLvMin = -9.0f, kLvMax = 9.0f;
 
-__global__ void mlp_loss_kernel(const float* Y, const float* T, int B, int K, int out_pad, float inv_count,
-                                __nv_bfloat16* dY, __nv_bfloat16* dYT, int ldT, float* loss, int64_t sY, int64_t sT) {
+__global__ void __launch_bounds__(256) mlp_loss_kernel(const float* Y, const float* T, int B, int K, int out_pad,
+                                                       float inv_count, __nv_bfloat16* dY, __nv_bfloat16* dYT, int ldT,
+                                                       float* loss_part, int64_t sY, int64_t sT) {
   const int e = blockIdx.y;
   float local = 0.0f;
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < B * out_pad; idx += gridDim.x * blockDim.x) {
@@ -132,8 +133,37 @@ __global__ void mlp_loss_kernel(const float* Y, const float* T, int B, int K, in
     dY[e * sY + idx] = gb;
     dYT[(int64_t)e * out_pad * ldT + (int64_t)c * ldT + i] = gb;
   }
+  // block sum in a fixed order: warps by shuffles, then warp 0 over the warp sums
+  __shared__ float wsum[8];
   for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(&loss[e], local * inv_count);
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = local;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.0f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += wsum[w];
+    loss_part[e * gridDim.x + blockIdx.x] = t * inv_count;
+  }
+}
+
+// loss[e] += sum of the member's block partials, in block order (the epoch
+// loss accumulates over the batches in stream order)
+__global__ void mlp_loss_sum_kernel(const float* loss_part, int n_blocks, float* loss) {
+  const int e = blockIdx.x;
+  if (threadIdx.x != 0) return;
+  float t = 0.0f;
+  for (int b = 0; b < n_blocks; ++b) t += loss_part[e * n_blocks + b];
+  loss[e] += t;
+}
+
+// out[z][off + i] = sum over the used reduction splits of part[split][z][off + i], in split order
+__global__ void mlp_split_sum_kernel(const float* part, int used, int64_t sSplit, int64_t sMember, int64_t off,
+                                     int64_t n, float* out) {
+  const int z = blockIdx.y;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float acc = 0.0f;
+    for (int sp = 0; sp < used; ++sp) acc += part[sp * sSplit + z * sMember + off + i];
+    out[z * sMember + off + i] = acc;
+  }
 }
 
 // db[n] = sum_i dZ[i][n] for every member
@@ -288,15 +318,19 @@ cudaError_t mlp_forward(const MlpDims& d, int members, int B, const __nv_bfloat1
 
 // Backward pass: dY (bf16 [members][B][out_pad]) and dY^T ([members][out_pad][ldT])
 // -> parameter gradients Gf (fp32, zeroed here).  dW_l = A_{l-1}^T dZ_l from the
-// transposed copies (reduction over the batch split across CTAs, atomically
-// accumulated); dZ_l = (dZ_{l+1} W_{l+1}^T) silu'(Z_l) with its transposed copy.
+// transposed copies (reduction over the batch split across CTAs, each split
+// writing its own slice of Gpart, the slices summed in split order so that a
+// training run is reproducible bit for bit); dZ_l = (dZ_{l+1} W_{l+1}^T)
+// silu'(Z_l) with its transposed copy.
 cudaError_t mlp_backward(const MlpDims& d, int members, int B, const __nv_bfloat16* X0T, const __nv_bfloat16* Wh,
                          const float* Z, const __nv_bfloat16* AhT, const __nv_bfloat16* dY, const __nv_bfloat16* dYT,
                          __nv_bfloat16* dZa, __nv_bfloat16* dZb, __nv_bfloat16* dZTa, __nv_bfloat16* dZTb, int ldT,
-                         float* Gf, int* err, cudaStream_t s) {
+                         float* Gf, float* Gpart, int* err, cudaStream_t s) {
   const int H = d.H;
   const int64_t sZ = 3 * (int64_t)B * H, sL = (int64_t)B * H, sLT = (int64_t)H * ldT, sP = d.n_params;
-  const int splits = std::max(1, std::min(16, B / 128));
+  const int splits = mlp_wgrad_splits(B);
+  const int nk = (B + 63) / 64, per = (nk + splits - 1) / splits;
+  const int used = (nk + per - 1) / per;  // splits that receive reduction chunks
   cudaError_t e = cudaMemsetAsync(Gf, 0, sizeof(float) * d.n_params * members, s);
   if (e) return e;
   auto wgrad = [&](const TcOperand& A, const TcOperand& Bg, int M, int N, int64_t off) {
@@ -305,11 +339,17 @@ cudaError_t mlp_backward(const MlpDims& d, int members, int B, const __nv_bfloat
     g.N = N;
     g.K = B;
     g.k_split = splits;
-    g.outf = Gf + off;
+    g.outf = Gpart + off;
     g.sOutf = sP;
+    g.sSplit = sP * members;
     g.ldf = N;
     g.err = err;
-    return mlp_tc_gemm(EPI_ATOMIC, A, Bg, g, members, s);
+    cudaError_t r = mlp_tc_gemm(EPI_PARTIAL, A, Bg, g, members, s);
+    if (r != cudaSuccess) return r;
+    const int64_t n = (int64_t)M * N;
+    mlp_split_sum_kernel<<<dim3((unsigned)std::min<int64_t>((n + 255) / 256, 1024), members), 256, 0, s>>>(
+        Gpart, used, sP * members, sP, off, n, Gf);
+    return cudaGetLastError();
   };
   // layer 4: dW4 = A3^T dY (M = H, N = out_pad), db4 = colsum(dY)
   {
@@ -369,11 +409,12 @@ cudaError_t mlp_backward(const MlpDims& d, int members, int B, const __nv_bfloat
 }
 
 cudaError_t mlp_loss(const MlpDims& d, int members, int B, int valid_rows, const float* Y, const float* T,
-                     __nv_bfloat16* dY, __nv_bfloat16* dYT, int ldT, float* loss, cudaStream_t s) {
+                     __nv_bfloat16* dY, __nv_bfloat16* dYT, int ldT, float* loss, float* loss_part, cudaStream_t s) {
   const float inv = 1.0f / (float)(std::max(1, valid_rows) * d.K);
-  dim3 grid(std::min(1024, (B * d.out_pad + 255) / 256), members);
-  mlp_loss_kernel<<<grid, 256, 0, s>>>(Y, T, B, d.K, d.out_pad, inv, dY, dYT, ldT, loss, (int64_t)B * d.out_pad,
-                                       (int64_t)B * d.K);
+  const int nb = mlp_loss_blocks(B, d.out_pad);
+  mlp_loss_kernel<<<dim3(nb, members), 256, 0, s>>>(Y, T, B, d.K, d.out_pad, inv, dY, dYT, ldT, loss_part,
+                                                    (int64_t)B * d.out_pad, (int64_t)B * d.K);
+  mlp_loss_sum_kernel<<<members, 32, 0, s>>>(loss_part, nb, loss);
   return cudaGetLastError();
 }
 

@@ -45,7 +45,8 @@ inline MlpDims mlp_dims(int in_dim, int K) {
 enum MlpEpi : int {
   EPI_HIDDEN = 0,    // z = C + bias -> Zf32 (optional), act = silu(z) -> bf16 out
   EPI_LINEAR = 1,    // C + bias -> fp32 out
-  EPI_ATOMIC = 2,    // atomicAdd C into fp32 out (split-K over the batch)
+  EPI_PARTIAL = 2,   // C into fp32 out + split * sSplit: one slice per reduction split (split-K over
+                     // the batch), summed in split order afterwards, so the result does not depend on timing
   EPI_DSILU = 3      // bf16 out = C * silu'(Zprev)
 };
 
@@ -61,14 +62,15 @@ struct TcOperand {
 
 struct TcGemm {
   int M, N, K;
-  int k_split;   // reduction split over blockIdx.y (EPI_ATOMIC)
+  int k_split;   // reduction split over blockIdx.y (EPI_PARTIAL)
   int a_shared;  // one A for every member
   const float* bias;
   int64_t sBias;
   const float* zprev;  // EPI_DSILU: pre-activation [M][ldz]
   int64_t sZ;
   int ldz;
-  float* outf;         // EPI_HIDDEN (optional), EPI_LINEAR, EPI_ATOMIC: [M][ldf]
+  float* outf;         // EPI_HIDDEN (optional), EPI_LINEAR, EPI_PARTIAL: [M][ldf]
+  int64_t sSplit;      // EPI_PARTIAL: stride between the slices of the reduction splits
   int64_t sOutf;
   int ldf;
   __nv_bfloat16* outh;   // EPI_HIDDEN, EPI_DSILU: [M][ldh]
@@ -79,6 +81,14 @@ struct TcGemm {
   int ldhT;
   int* err;              // nonzero: a bounded wait ran out
 };
+
+// reduction splits of the weight-gradient GEMMs for a batch of B rows, and
+// blocks of the loss kernel (sizes of the partial-sum buffers)
+inline int mlp_wgrad_splits(int B) { return B / 128 < 1 ? 1 : (B / 128 > 16 ? 16 : B / 128); }
+inline int mlp_loss_blocks(int B, int out_pad) {
+  const int n = (B * out_pad + 255) / 256;
+  return n < 1024 ? n : 1024;
+}
 
 cudaError_t mlp_tc_gemm(int epi, const TcOperand& A, const TcOperand& B, const TcGemm& g, int members,
                         cudaStream_t s);

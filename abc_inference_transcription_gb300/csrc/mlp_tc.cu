@@ -7,7 +7,7 @@
 // with the 128-byte swizzle) into a 3-stage ring; one lane of warp 1 issues
 // tcgen05.mma.kind::f16 (M = N = 128, K = 16); all four warps then read their
 // 32 accumulator rows with tcgen05.ld and apply the fused epilogue (bias +
-// SiLU, bias, atomic accumulation, or the SiLU derivative), writing the
+// SiLU, bias, one partial sum per reduction split, or the SiLU derivative), writing the
 // row-major result and, where the backward pass needs it, the transposed
 // BF16 copy.  Waits are bounded (about one second); a wait that runs out sets
 // the error word, and the CTA drains its copies and MMAs before it frees its
@@ -156,8 +156,8 @@ __global__ void __launch_bounds__(128, 1)
           if (g.outhT) g.outhT[z * g.sOuthT + (int64_t)n * g.ldhT + m] = h;
         } else if (EPI == EPI_LINEAR) {
           g.outf[z * g.sOutf + (int64_t)m * g.ldf + n] = a + (bias ? bias[n] : 0.0f);
-        } else if (EPI == EPI_ATOMIC) {
-          atomicAdd(&g.outf[z * g.sOutf + (int64_t)m * g.ldf + n], a);
+        } else if (EPI == EPI_PARTIAL) {
+          g.outf[split * g.sSplit + z * g.sOutf + (int64_t)m * g.ldf + n] = a;
         } else {
           const float zp = g.zprev[z * g.sZ + (int64_t)m * g.ldz + n];
           const float sg = sigm(zp);
@@ -225,7 +225,7 @@ cudaError_t mlp_tc_gemm(int epi, const TcOperand& A, const TcOperand& B, const T
   switch (epi) {
     case EPI_HIDDEN: return launch_epi<EPI_HIDDEN>(ma, mb, g, members, s);
     case EPI_LINEAR: return launch_epi<EPI_LINEAR>(ma, mb, g, members, s);
-    case EPI_ATOMIC: return launch_epi<EPI_ATOMIC>(ma, mb, g, members, s);
+    case EPI_PARTIAL: return launch_epi<EPI_PARTIAL>(ma, mb, g, members, s);
     default: return launch_epi<EPI_DSILU>(ma, mb, g, members, s);
   }
 }

@@ -68,6 +68,7 @@ struct PRec {
   double kon[kMaxSteps], alp[kMaxSteps], gam[kMaxSteps], amax[kMaxSteps];
   double koff, lam, beta, scal;
   double g0, u0, s0;  // means at the start of a cycle (SSA initial state)
+  double c0, v0;      // Cov(G, u) and Var u there (no splicing)
   double cost;        // expected fired events per trajectory (work estimate)
 };
 
@@ -143,6 +144,109 @@ ABC_HD void initial_means(const DevCfg& cfg, PRec& R) {
   R.s0 = s;
 }
 
+// ---------------------------------------------------------------------------
+// Initial state without splicing: the periodic solution, at the start of a
+// cycle (after division), of the unlabelled moments x = (E G, E u, Cov(G,u),
+// Var u) of the reaction network (model.jl:67-86 with lambda = 0) under the
+// division map (model.jl:98-111: Cov/2, Var/4 + E/4, E/2), i.e. the state
+// transient_phase converges to (model.jl:114-142).
+//   E G' = kon - (kon + koff) E G
+//   E u' = alpha(t) E G - gamma E u
+//   C'   = alpha(t) E G (1 - E G) - (kon + koff + gamma) C
+//   V'   = alpha(t) E G + gamma E u + 2 alpha(t) C - 2 gamma V
+// Exponential sub-steps (16 per age step) with the sources averaged over the
+// sub-step.  E G is periodic by itself; with it fixed, the cycle map of
+// (E u, C, V) is affine with a lower-triangular matrix, solved directly.
+// ---------------------------------------------------------------------------
+ABC_HD void moment_cycle(const DevCfg& cfg, const PRec& R, double* x) {
+  const int S = cfg.n_steps;
+  const double T = cfg.cycle;
+  const double h = (T / (double)S) / (double)kIcSub;
+  double g = x[0], m = x[1], c = x[2], v = x[3];
+  for (int k = 0; k < S; ++k) {
+    const double kG = R.kon[k] + R.koff;
+    const double Ginf = R.kon[k] / kG;
+    const double gam = R.gam[k];
+    double eG, phG, em, phm, ec, phc, ev, phv;
+    phi_pair(kG * h, eG, phG);
+    phi_pair(gam * h, em, phm);
+    phi_pair((kG + gam) * h, ec, phc);
+    phi_pair((2.0 * gam) * h, ev, phv);
+    for (int i = 0; i < kIcSub; ++i) {
+      const double ph = ((double)(k * kIcSub + i) + 0.5) * h;
+      const double a = R.alp[k] * xpow(1.0 + ph / T, R.scal);
+      const double Gavg = Ginf + (g - Ginf) * phG;
+      const double gn = Ginf + (g - Ginf) * eG;
+      const double mn = m * em + ((a * Gavg) * h) * phm;
+      const double cn = c * ec + ((a * (Gavg * (1.0 - Gavg))) * h) * phc;
+      const double src = (a * Gavg + gam * (0.5 * (m + mn))) + (2.0 * a) * (0.5 * (c + cn));
+      const double vn = v * ev + (src * h) * phv;
+      g = gn;
+      m = mn;
+      c = cn;
+      v = vn;
+    }
+  }
+  x[0] = g;
+  x[1] = m * 0.5;
+  x[2] = c * 0.5;
+  x[3] = v * 0.25 + m * 0.25;
+}
+
+ABC_HD void initial_moments(const DevCfg& cfg, PRec& R) {
+  double z[4] = {0.0, 0.0, 0.0, 0.0}, e[4] = {1.0, 0.0, 0.0, 0.0};
+  moment_cycle(cfg, R, z);
+  moment_cycle(cfg, R, e);
+  double g = z[0] / (1.0 - (e[0] - z[0]));
+  if (!(g > 0.0)) g = 0.0;
+  if (g > 1.0) g = 1.0;
+  double b[4] = {g, 0.0, 0.0, 0.0}, bm[4] = {g, 1.0, 0.0, 0.0};
+  double bc[4] = {g, 0.0, 1.0, 0.0}, bv[4] = {g, 0.0, 0.0, 1.0};
+  moment_cycle(cfg, R, b);
+  moment_cycle(cfg, R, bm);
+  moment_cycle(cfg, R, bc);
+  moment_cycle(cfg, R, bv);
+  const double mmm = bm[1] - b[1], mcc = bc[2] - b[2];
+  const double mvm = bm[3] - b[3], mvc = bc[3] - b[3], mvv = bv[3] - b[3];
+  double m = b[1] / (1.0 - mmm);
+  double c = b[2] / (1.0 - mcc);
+  double v = ((b[3] + mvm * m) + mvc * c) / (1.0 - mvv);
+  if (!(m > 0.0)) m = 0.0;
+  if (!(v > 0.0)) v = 0.0;
+  if (!(c == c)) c = 0.0;
+  R.g0 = g;
+  R.u0 = m;
+  R.s0 = 0.0;
+  R.c0 = c;
+  R.v0 = v;
+}
+
+// Unspliced count at the start of a trajectory, given the gene state G drawn
+// with probability g0: conditional mean E[u | G] = u0 + c0 / g0 (G = 1) or
+// u0 - c0 / (1 - g0) (G = 0), and within-state variance F E[u | G] with the
+// Fano factor F = (v0 - c0^2 / (g0 (1 - g0))) / u0, so that E u, Var u and
+// Cov(G, u) are those of the periodic solution.  Drawn as a zero-inflated
+// Poisson (0 with probability 1 - w, else Poisson(mu / w), w = mu / (mu + F - 1))
+// when F > 1, a Poisson(mu) otherwise.  wz: a 32-bit uniform word for the
+// zero inflation; aux: the trajectory's auxiliary stream.
+ABC_HD int64_t initial_count(const PRec& R, int G, uint32_t wz, Rng& aux) {
+  const double g = R.g0, m = R.u0, c = R.c0, v = R.v0;
+  double mu = m, vr = v;
+  if (g > 0.0 && g < 1.0) {
+    mu = G ? m + c / g : m - c / (1.0 - g);
+    vr = v - (c * c) / (g * (1.0 - g));
+  }
+  if (!(mu > 0.0)) return 0;
+  const double F = (m > 0.0 && vr > 0.0) ? vr / m : 0.0;
+  double lam = mu;
+  if (F > 1.0) {
+    const double w = mu / (mu + (F - 1.0));
+    if (!((double)wz * ABC_TWO_M32 < w)) return 0;
+    lam = mu / w;
+  }
+  return poisson(aux, lam);
+}
+
 // theta -> record; returns 0 or a negative abc_status.
 // with_ic: also the SSA initial state and work estimate (not needed by the moment ODE)
 ABC_HD int parse_theta(const DevCfg& cfg, int model, const double* th, PRec& R, bool with_ic = true) {
@@ -184,7 +288,11 @@ ABC_HD int parse_theta(const DevCfg& cfg, int model, const double* th, PRec& R, 
     if (!(R.kon[k] < INFINITY) || !(R.alp[k] < INFINITY) || !(R.gam[k] < INFINITY)) return -5;
   if (!(R.koff < INFINITY) || R.lam != R.lam || R.scal != R.scal || R.scal < 0.0) return -5;
   if (!with_ic) return 0;
-  initial_means(cfg, R);
+  R.c0 = R.v0 = 0.0;
+  if (cfg.splicing)
+    initial_means(cfg, R);
+  else
+    initial_moments(cfg, R);
   // work estimate: switching + transcription + decay events over the horizon
   double horizon = (double)(cfg.ages[0] - cfg.t0);
   double rate = 0.0;

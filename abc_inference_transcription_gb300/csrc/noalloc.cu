@@ -227,6 +227,8 @@ extern "C" int abc_simulate_noalloc(const abc_config* cfg, int model, int64_t n_
   ss.want_hash = 0;
   int64_t grid = std::min<int64_t>((int64_t)bps * sms, (ss.n_items + 127) / 128);
   grid = std::max<int64_t>(grid, 1);
+  // the production kernel takes each trajectory's initial state from the count array
+  if (!fp64) NA_CK(launch_init_states(ss, sms, stream));
   NA_CK(fp64 ? launch_ssa_fp64(ss, (int)grid, stream) : launch_ssa_fp32(ss, (int)grid, stream));
 
   StatsArgs sta;

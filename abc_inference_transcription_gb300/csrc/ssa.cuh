@@ -105,8 +105,16 @@ __device__ __forceinline__ void traj_init(Traj& s, const SsaArgs& A, int64_t ite
   uint32_t w0, w1;
   rng_pair(s.rng, w0, w1);
   s.G = ((double)w0 * ABC_TWO_M32 < R.g0) ? 1 : 0;
-  s.uu = (int)floor(R.u0 + 0.5);
-  s.us = cfg.splicing ? (int)floor(R.s0 + 0.5) : 0;
+  if (cfg.splicing) {
+    s.uu = (int)floor(R.u0 + 0.5);
+    s.us = (int)floor(R.s0 + 0.5);
+  } else {
+    // moment-matched draw from the periodic state (initial_count), auxiliary stream blocks 0, 1, ...
+    Rng aux;
+    rng_init(aux, A.seed, ST_AUX, A.cell_id[ci], (uint32_t)(A.p_offset + pl));
+    s.uu = (int)initial_count(R, s.G, w1, aux);
+    s.us = 0;
+  }
   s.lu = 0;
   s.ls = 0;
   s.hash = kFnvOff;

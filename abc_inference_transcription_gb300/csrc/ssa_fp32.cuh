@@ -463,10 +463,11 @@ __global__ void __launch_bounds__(128, MINB) ssa_kernel_f32(SsaArgs A) {
               s.tlab_end = texp + (T)cfg.pulse[j];
             }
             s.cs = t0;
-            const U4 w0 = main_block(0u, s.r1x, s.r1y, s.r1z, A.rk);
+            // initial state, drawn beforehand by init_state_kernel: (u, G)
+            const int2 st0 = A.counts[(int64_t)pl * A.n_cells + ci];
             s.block = 1;
-            s.G = ((double)w0.x * ABC_TWO_M32 < R.g0) ? 1.0f : 0.0f;
-            s.uu = floorf((float)R.u0 + 0.5f);
+            s.G = st0.y ? 1.0f : 0.0f;
+            s.uu = (float)st0.x;
             s.us = SPLICE ? floorf((float)R.s0 + 0.5f) : 0.0f;
             s.lu = 0.0f;
             s.ls = 0.0f;

@@ -31,9 +31,9 @@ cudaError_t mlp_forward(const MlpDims& d, int members, int B, const __nv_bfloat1
 cudaError_t mlp_backward(const MlpDims& d, int members, int B, const __nv_bfloat16* X0T, const __nv_bfloat16* Wh,
                          const float* Z, const __nv_bfloat16* AhT, const __nv_bfloat16* dY, const __nv_bfloat16* dYT,
                          __nv_bfloat16* dZa, __nv_bfloat16* dZb, __nv_bfloat16* dZTa, __nv_bfloat16* dZTb, int ldT,
-                         float* Gf, int* err, cudaStream_t s);
+                         float* Gf, float* Gpart, int* err, cudaStream_t s);
 cudaError_t mlp_loss(const MlpDims& d, int members, int B, int valid_rows, const float* Y, const float* T,
-                     __nv_bfloat16* dY, __nv_bfloat16* dYT, int ldT, float* loss, cudaStream_t s);
+                     __nv_bfloat16* dY, __nv_bfloat16* dYT, int ldT, float* loss, float* loss_part, cudaStream_t s);
 cudaError_t mlp_adam(const MlpDims& d, int members, float* P, const float* G, float* m, float* v,
                      __nv_bfloat16* Ph, __nv_bfloat16* PhT, float lr, int step, cudaStream_t s);
 cudaError_t mlp_combine(const MlpDims& d, int members, int N, const float* Y, const float* ymean, const float* ystd,
@@ -270,7 +270,8 @@ struct abc_surrogate {
   Buf<__nv_bfloat16> X0, Ah, dY, dZa, dZb;
   Buf<__nv_bfloat16> X0T, AhT, dYT, dZTa, dZTb;  // [features][ldT] copies for the weight gradients
   int ldT = 0;
-  Buf<float> loss;
+  Buf<float> loss, loss_part;  // per-member loss; per-block partial sums of the loss kernel
+  Buf<float> Gpart;            // weight-gradient partial sums, one slice per reduction split
   Buf<uint64_t> perm;
   // prediction scratch
   Buf<double> pm, pv, pd;
@@ -311,6 +312,8 @@ static int ensure_batch(abc_surrogate* s, int B) {
   SK(s->dZTa.ensure(E * d.H * lt));
   SK(s->dZTb.ensure(E * d.H * lt));
   SK(s->loss.ensure(E));
+  SK(s->loss_part.ensure(E * (size_t)mlp_loss_blocks(B, d.out_pad)));
+  SK(s->Gpart.ensure((size_t)mlp_wgrad_splits(B) * E * (size_t)d.n_params));
   SK(s->perm.ensure(2 * E));
   return ABC_OK;
 }
@@ -333,9 +336,9 @@ static int train_step(abc_surrogate* s, int B, int64_t base, int valid, int64_t 
   SK(mlp_gather(s->xn.p, s->yn.p, N, d, B, base, s->perm.p, E, s->X0.p, s->X0T.p, s->ldT, s->T.p, s->stream));
   SK(mlp_forward(d, E, B, s->X0.p, (int64_t)B * d.in_pad, s->PhT.p, s->P.p, s->Z.p, s->Ah.p, s->AhT.p, s->ldT,
                  s->Y.p, s->tcerr.p, s->stream));
-  SK(mlp_loss(d, E, B, valid, s->Y.p, s->T.p, s->dY.p, s->dYT.p, s->ldT, s->loss.p, s->stream));
+  SK(mlp_loss(d, E, B, valid, s->Y.p, s->T.p, s->dY.p, s->dYT.p, s->ldT, s->loss.p, s->loss_part.p, s->stream));
   SK(mlp_backward(d, E, B, s->X0T.p, s->Ph.p, s->Z.p, s->AhT.p, s->dY.p, s->dYT.p, s->dZa.p, s->dZb.p, s->dZTa.p,
-                  s->dZTb.p, s->ldT, s->G.p, s->tcerr.p, s->stream));
+                  s->dZTb.p, s->ldT, s->G.p, s->Gpart.p, s->tcerr.p, s->stream));
   return ABC_OK;
 }
 
@@ -386,6 +389,7 @@ int abc_surrogate_destroy(abc_surrogate* s) {
   s->ysf.release(); s->xm.release(); s->xs.release(); s->ym.release(); s->ys.release(); s->th64.release();
   s->st64.release(); s->xn.release(); s->yn.release(); s->T.release(); s->Z.release(); s->Y.release();
   s->X0.release(); s->Ah.release(); s->dY.release(); s->dZa.release(); s->dZb.release(); s->loss.release();
+  s->loss_part.release(); s->Gpart.release();
   s->perm.release(); s->pm.release(); s->pv.release(); s->pd.release(); s->pmf.release(); s->pvf.release();
   s->sw.release(); s->dw.release(); s->X.release(); s->gd.release(); s->gs.release(); s->keep.release();
   s->cnt.release();

@@ -607,7 +607,7 @@ def main():
                          "rewritten every step"},
         "events_per_step": tot_ev_all / args.steps, "thinning_rejections": tot_rej,
         "particles_per_s": P_rank * world * args.steps / compute_s,
-        "phase_ms_per_step": {"setup_and_work_order": phase[0] / args.steps, "ssa": phase[1] / args.steps,
+        "phase_ms_per_step": {"setup_work_order_initial_states": phase[0] / args.steps, "ssa": phase[1] / args.steps,
                               "capture_stats": phase[2] / args.steps},
         "roofline": {"bound": "issue", "achieved": achieved_ev / 1e9, "peak": peak_ev / 1e9, "unit": "Gevents/s",
                      "frac": achieved_ev / peak_ev, "traffic": traffic,
@@ -616,7 +616,7 @@ def main():
                               "per-trajectory figure from ncu x trajectories"},
         "cpu_baseline": cpu,
         "e2e": e2e,
-        "gpu_launches": 5 * args.steps,  # per step: setup, 2 work-order kernels, SSA, capture+statistics
+        "gpu_launches": 6 * args.steps,  # per step: setup, 2 work-order kernels, initial states, SSA, capture+statistics
         "autotune": tune,
         "cuda_graph": graph,
         "clocks": clocks,

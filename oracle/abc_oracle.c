@@ -44,7 +44,7 @@ void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
 /* Random stream of one trajectory: counter = (block lo, block hi | stream<<30,
  * cell, particle), key = seed.  Words are consumed in pairs; one Philox block
  * gives two pairs. */
-enum { ST_SSA = 0, ST_CAPTURE = 1, ST_PRIOR = 2 };
+enum { ST_SSA = 0, ST_CAPTURE = 1, ST_PRIOR = 2, ST_AUX = 3 };
 typedef struct {
   uint32_t k0, k1, cell, particle, tag;
   uint64_t block;
@@ -300,6 +300,60 @@ static int64_t binomial(orc_rng* r, int64_t n, double p) {
   return flip ? n - k : k;
 }
 
+/* log(k!) from the Stirling series with the tabulated correction. */
+static double logfact(double k) {
+  return (((k + 0.5) * orc_xlog(k + 1.0) - (k + 1.0)) + 0.9189385332046728) + fc(k);
+}
+
+/* Poisson(lam): inversion below lam = 10, otherwise PTRS (W. Hormann, "The
+ * transformed rejection method for generating Poisson random variables",
+ * Insurance: Mathematics and Economics 12 (1993) 39-45).  Same operation
+ * order as the GPU sampler. */
+static int64_t poisson(orc_rng* r, double lam) {
+  if (!(lam > 0.0)) return 0;
+  uint32_t w0, w1;
+  if (lam < 10.0) {
+    rng_pair(r, &w0, &w1);
+    double u = u52(w0, w1);
+    double f = orc_xexp(-lam);
+    int64_t k = 0;
+    while (u >= f && k < 1000) {
+      u = u - f;
+      k = k + 1;
+      f = f * (lam / (double)k);
+    }
+    return k;
+  }
+  const double slam = sqrt(lam);
+  const double loglam = orc_xlog(lam);
+  const double b = 0.931 + 2.53 * slam;
+  const double a = -0.059 + 0.02483 * b;
+  const double inv_alpha = 1.1239 + 1.1328 / (b - 3.4);
+  const double vr = 0.9277 - 3.6224 / (b - 2.0);
+  for (int it = 0; it < 1000; ++it) {
+    rng_pair(r, &w0, &w1);
+    const double U = u52(w0, w1) - 0.5;
+    rng_pair(r, &w0, &w1);
+    const double V = u52open(w0, w1);
+    const double us = 0.5 - fabs(U);
+    const double kd = floor((((2.0 * a) / us + b) * U + lam) + 0.43);
+    if (us >= 0.07 && V <= vr) return (int64_t)kd;
+    if (kd < 0.0 || (us < 0.013 && V > us)) continue;
+    const double lhs = orc_xlog((V * inv_alpha) / (a / (us * us) + b));
+    const double rhs = (kd * loglam - lam) - logfact(kd);
+    if (lhs <= rhs) return (int64_t)kd;
+  }
+  return (int64_t)floor(lam + 0.5);
+}
+
+int64_t orc_poisson(double lam, uint64_t seed, uint32_t stream, uint32_t cell, uint32_t particle,
+                    int64_t n_draws, int64_t* out) {
+  orc_rng r;
+  rng_init(&r, seed, stream, cell, particle);
+  for (int64_t i = 0; i < n_draws; ++i) out[i] = poisson(&r, lam);
+  return (int64_t)r.block;
+}
+
 int64_t orc_binomial(int64_t n, double p, uint64_t seed, uint32_t stream, uint32_t cell,
                      uint32_t particle, int64_t n_draws, int64_t* out) {
   orc_rng r;
@@ -322,6 +376,7 @@ typedef struct {
   int S;
   double kon[ABC_MAX_STEPS], alp[ABC_MAX_STEPS], gam[ABC_MAX_STEPS], amax[ABC_MAX_STEPS];
   double koff, lam, beta, scal, g0, u0, s0;
+  double c0, v0; /* Cov(G, u) and Var u at the start of a cycle (no splicing) */
 } rec_t;
 
 /* One cycle of the mean equations (G, first mRNA species, spliced species)
@@ -388,6 +443,97 @@ static void initial_means(const abc_config* cfg, rec_t* R) {
   R->s0 = s;
 }
 
+/* Periodic solution at the start of a cycle (after division) of the
+ * unlabelled moments x = (E G, E u, Cov(G,u), Var u) of model.jl:67-86 with
+ * lambda = 0, under the division map of model.jl:98-111 -- the state that
+ * transient_phase (model.jl:114-142) converges to.  Exponential sub-steps
+ * with sub-step-averaged sources; E G is periodic by itself, then the cycle
+ * map of (E u, C, V) is affine with a lower-triangular matrix. */
+static void moment_cycle(const abc_config* cfg, const rec_t* R, double x[4]) {
+  const int S = R->S;
+  const double T = cfg->cycle;
+  const double h = (T / (double)S) / (double)IC_SUB;
+  double g = x[0], m = x[1], c = x[2], v = x[3];
+  for (int k = 0; k < S; ++k) {
+    const double kG = R->kon[k] + R->koff;
+    const double Ginf = R->kon[k] / kG;
+    const double gam = R->gam[k];
+    double eG, phG, em, phm, ec, phc, ev, phv;
+    phi_pair(kG * h, &eG, &phG);
+    phi_pair(gam * h, &em, &phm);
+    phi_pair((kG + gam) * h, &ec, &phc);
+    phi_pair((2.0 * gam) * h, &ev, &phv);
+    for (int i = 0; i < IC_SUB; ++i) {
+      const double ph = ((double)(k * IC_SUB + i) + 0.5) * h;
+      const double a = R->alp[k] * xpow(1.0 + ph / T, R->scal);
+      const double Gavg = Ginf + (g - Ginf) * phG;
+      const double gn = Ginf + (g - Ginf) * eG;
+      const double mn = m * em + ((a * Gavg) * h) * phm;
+      const double cn = c * ec + ((a * (Gavg * (1.0 - Gavg))) * h) * phc;
+      const double src = (a * Gavg + gam * (0.5 * (m + mn))) + (2.0 * a) * (0.5 * (c + cn));
+      const double vn = v * ev + (src * h) * phv;
+      g = gn;
+      m = mn;
+      c = cn;
+      v = vn;
+    }
+  }
+  x[0] = g;
+  x[1] = m * 0.5;
+  x[2] = c * 0.5;
+  x[3] = v * 0.25 + m * 0.25;
+}
+
+static void initial_moments(const abc_config* cfg, rec_t* R) {
+  double z[4] = {0.0, 0.0, 0.0, 0.0}, e[4] = {1.0, 0.0, 0.0, 0.0};
+  moment_cycle(cfg, R, z);
+  moment_cycle(cfg, R, e);
+  double g = z[0] / (1.0 - (e[0] - z[0]));
+  if (!(g > 0.0)) g = 0.0;
+  if (g > 1.0) g = 1.0;
+  double b[4] = {g, 0.0, 0.0, 0.0}, bm[4] = {g, 1.0, 0.0, 0.0};
+  double bc[4] = {g, 0.0, 1.0, 0.0}, bv[4] = {g, 0.0, 0.0, 1.0};
+  moment_cycle(cfg, R, b);
+  moment_cycle(cfg, R, bm);
+  moment_cycle(cfg, R, bc);
+  moment_cycle(cfg, R, bv);
+  const double mmm = bm[1] - b[1], mcc = bc[2] - b[2];
+  const double mvm = bm[3] - b[3], mvc = bc[3] - b[3], mvv = bv[3] - b[3];
+  double m = b[1] / (1.0 - mmm);
+  double c = b[2] / (1.0 - mcc);
+  double v = ((b[3] + mvm * m) + mvc * c) / (1.0 - mvv);
+  if (!(m > 0.0)) m = 0.0;
+  if (!(v > 0.0)) v = 0.0;
+  if (!(c == c)) c = 0.0;
+  R->g0 = g;
+  R->u0 = m;
+  R->s0 = 0.0;
+  R->c0 = c;
+  R->v0 = v;
+}
+
+/* Initial unspliced count given the gene state G: conditional mean
+ * E[u | G] and within-state variance F E[u | G] of the periodic moments,
+ * drawn as a zero-inflated Poisson when F > 1 (0 with probability 1 - w, else
+ * Poisson(mu / w), w = mu / (mu + F - 1)), as a Poisson(mu) otherwise. */
+static int64_t initial_count(const rec_t* R, int G, uint32_t wz, orc_rng* aux) {
+  const double g = R->g0, m = R->u0, c = R->c0, v = R->v0;
+  double mu = m, vr = v;
+  if (g > 0.0 && g < 1.0) {
+    mu = G ? m + c / g : m - c / (1.0 - g);
+    vr = v - (c * c) / (g * (1.0 - g));
+  }
+  if (!(mu > 0.0)) return 0;
+  const double F = (m > 0.0 && vr > 0.0) ? vr / m : 0.0;
+  double lam = mu;
+  if (F > 1.0) {
+    const double w = mu / (mu + (F - 1.0));
+    if (!((double)wz * TWO_M32 < w)) return 0;
+    lam = mu / w;
+  }
+  return poisson(aux, lam);
+}
+
 static int parse_theta(const abc_config* cfg, int model, const double* th, rec_t* R) {
   const int S = cfg->n_steps;
   int i = 0;
@@ -414,7 +560,31 @@ static int parse_theta(const abc_config* cfg, int model, const double* th, rec_t
   for (int k = 0; k < S; ++k)
     if (!(R->kon[k] < INFINITY) || !(R->alp[k] < INFINITY) || !(R->gam[k] < INFINITY)) return ABC_ERR_NONFINITE;
   if (!(R->koff < INFINITY) || R->lam != R->lam || R->scal != R->scal || R->scal < 0.0) return ABC_ERR_NONFINITE;
-  initial_means(cfg, R);
+  R->c0 = R->v0 = 0.0;
+  if (cfg->splicing)
+    initial_means(cfg, R);
+  else
+    initial_moments(cfg, R);
+  return ABC_OK;
+}
+
+/* The SSA's initial state of n trajectories (cells 0..n-1 of one particle):
+ * the gene state and the first mRNA count, as sim_traj draws them. */
+int orc_initial_states(const abc_config* cfg, int model, const double* theta, uint64_t seed, uint32_t particle,
+                       int64_t n, int32_t* G_out, int64_t* u_out) {
+  rec_t R;
+  int st = parse_theta(cfg, model, theta, &R);
+  if (st) return st;
+  for (int64_t c = 0; c < n; ++c) {
+    orc_rng rng, aux;
+    rng_init(&rng, seed, ST_SSA, (uint32_t)c, particle);
+    rng_init(&aux, seed, ST_AUX, (uint32_t)c, particle);
+    uint32_t w0, w1;
+    rng_pair(&rng, &w0, &w1);
+    const int G = ((double)w0 * TWO_M32 < R.g0) ? 1 : 0;
+    G_out[c] = G;
+    u_out[c] = cfg->splicing ? (int64_t)floor(R.u0 + 0.5) : initial_count(&R, G, w1, &aux);
+  }
   return ABC_OK;
 }
 
@@ -429,6 +599,7 @@ int orc_setup(const abc_config* cfg, int model, const double* theta, double* rec
   for (int k = 0; k < S; ++k) rec_out[i++] = R.amax[k];
   rec_out[i++] = R.koff; rec_out[i++] = R.lam; rec_out[i++] = R.beta; rec_out[i++] = R.scal;
   rec_out[i++] = R.g0; rec_out[i++] = R.u0; rec_out[i++] = R.s0;
+  rec_out[i++] = R.c0; rec_out[i++] = R.v0;
   return ABC_OK;
 }
 
@@ -507,7 +678,8 @@ typedef struct {
   int err;
 } traj_out;
 
-static void sim_traj(const abc_config* cfg, const rec_t* R, int j, int a, orc_rng* rng, traj_out* o) {
+static void sim_traj(const abc_config* cfg, const rec_t* R, int j, int a, orc_rng* rng, orc_rng* aux,
+                     traj_out* o) {
   const double T = cfg->cycle;
   const int S = cfg->n_steps;
   const double step_len = T / (double)S;
@@ -526,7 +698,8 @@ static void sim_traj(const abc_config* cfg, const rec_t* R, int j, int a, orc_rn
   uint32_t w0, w1;
   rng_pair(rng, &w0, &w1);
   int G = ((double)w0 * TWO_M32 < R->g0) ? 1 : 0;
-  int64_t uu = (int64_t)floor(R->u0 + 0.5);
+  /* splicing option: the means; reference model: the moment-matched draw */
+  int64_t uu = sp ? (int64_t)floor(R->u0 + 0.5) : initial_count(R, G, w1, aux);
   int64_t us = sp ? (int64_t)floor(R->s0 + 0.5) : 0;
   int64_t lu = 0, ls = 0;
   uint64_t h = FNV_OFF;
@@ -739,7 +912,9 @@ int orc_simulate(const abc_config* cfg, int64_t C, const int32_t* cell_cond,
     orc_rng rng;
     traj_out o;
     rng_init(&rng, seed, ST_SSA, (uint32_t)c, (uint32_t)(particle_offset + p));
-    sim_traj(cfg, &R[p], cell_cond[c], cell_age[c], &rng, &o);
+    orc_rng aux; /* initial state: auxiliary stream, blocks 0, 1, ... */
+    rng_init(&aux, seed, ST_AUX, (uint32_t)c, (uint32_t)(particle_offset + p));
+    sim_traj(cfg, &R[p], cell_cond[c], cell_age[c], &rng, &aux, &o);
     if (o.err) status = o.err;
     if (o.u > 2147483647 || o.l > 2147483647) status = ABC_ERR_NONFINITE;
     orc_rng rc;

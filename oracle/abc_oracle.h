@@ -26,6 +26,9 @@ extern "C" {
 void    orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 double  orc_xlog(double x);
 double  orc_xexp(double x);
+/* n draws of Poisson(lam) from one stream (inversion below 10, PTRS above). */
+int64_t orc_poisson(double lam, uint64_t seed, uint32_t stream, uint32_t cell, uint32_t particle,
+                    int64_t n_draws, int64_t* out);
 int64_t orc_binomial(int64_t n, double p, uint64_t seed, uint32_t stream, uint32_t cell,
                      uint32_t particle, int64_t n_draws, int64_t* out);
 
@@ -38,6 +41,9 @@ int orc_sample_prior(const abc_config* cfg, int model, int64_t P, uint64_t seed,
 /* per-particle setup: rates and the initial means at the start of a cycle.
  * rec_out: 4*S + 7 doubles: kon[S], alp[S], gam[S], amax[S], koff, lam, beta, scal, g0, u0, s0 */
 int orc_setup(const abc_config* cfg, int model, const double* theta, double* rec_out);
+/* Initial (G, u) of trajectories of cells 0..n-1 of one particle, as the SSA draws them. */
+int orc_initial_states(const abc_config* cfg, int model, const double* theta, uint64_t seed, uint32_t particle,
+                       int64_t n, int32_t* G_out, int64_t* u_out);
 
 /* FP64 SSA + capture + statistics over P particles x C cells (OpenMP over
  * trajectories when n_threads > 1).  Any output may be NULL.

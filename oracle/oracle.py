@@ -45,9 +45,12 @@ def lib() -> C.CDLL:
         L.orc_binomial.argtypes = [C.c_int64, C.c_double, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
                                    C.c_int64, i64p]
         L.orc_binomial.restype = C.c_int64
+        L.orc_poisson.argtypes = [C.c_double, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int64, i64p]
+        L.orc_poisson.restype = C.c_int64
         L.orc_num_params.argtypes = [cfgp, C.c_int]
         L.orc_sample_prior.argtypes = [cfgp, C.c_int, C.c_int64, C.c_uint64, C.c_int64, C.POINTER(AbcPrior), dp]
         L.orc_setup.argtypes = [cfgp, C.c_int, dp, dp]
+        L.orc_initial_states.argtypes = [cfgp, C.c_int, dp, C.c_uint64, C.c_uint32, C.c_int64, i32p, i64p]
         L.orc_simulate.argtypes = [cfgp, C.c_int64, i32p, i32p, dp, dp, C.c_int, dp, C.c_int64, C.c_uint64,
                                    C.c_int64, C.c_int, i32p, i32p, i64p, u64p, i64p, dp]
         L.orc_stats_from_moments.argtypes = [cfgp, dp, dp, dp]
@@ -99,15 +102,31 @@ def binomial(n: int, p: float, n_draws: int, seed: int = 1, stream: int = 1, cel
     return out
 
 
+def poisson(lam: float, n_draws: int, seed: int = 1, stream: int = 3, cell: int = 0, particle: int = 0) -> np.ndarray:
+    out = np.zeros(n_draws, np.int64)
+    lib().orc_poisson(lam, seed, stream, cell, particle, n_draws, ptr(out, C.c_int64))
+    return out
+
+
 def sample_prior(cfg: AbcConfig, model: int, P: int, seed: int, prior: AbcPrior, offset: int = 0) -> np.ndarray:
     th = np.zeros((P, num_params(cfg, model)))
     _check(lib().orc_sample_prior(C.byref(cfg), model, P, seed, offset, C.byref(prior), ptr(th)), "sample_prior")
     return th
 
 
+def initial_states(cfg: AbcConfig, model: int, theta: np.ndarray, n: int, seed: int = 1, particle: int = 0):
+    """(G, u) at the start of n trajectories of one particle, as the SSA draws them."""
+    th = np.ascontiguousarray(theta, np.float64)
+    G = np.zeros(n, np.int32)
+    u = np.zeros(n, np.int64)
+    _check(lib().orc_initial_states(C.byref(cfg), model, ptr(th), seed, particle, n, ptr(G, C.c_int32),
+                                    ptr(u, C.c_int64)), "initial_states")
+    return G, u
+
+
 def setup(cfg: AbcConfig, model: int, theta: np.ndarray) -> np.ndarray:
     S = cfg.n_steps
-    rec = np.zeros(4 * S + 7)
+    rec = np.zeros(4 * S + 9)  # kon, alpha, gamma, amax per step; koff, lam, beta, scal, g0, u0, s0, c0, v0
     th = np.ascontiguousarray(theta, np.float64)
     _check(lib().orc_setup(C.byref(cfg), model, ptr(th), ptr(rec)), "setup")
     return rec

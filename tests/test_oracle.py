@@ -276,3 +276,93 @@ def test_accept_oracle_matches_numpy_restatement(orc):
                 want_off.append(len(want_idx))
             assert off.tolist() == want_off, (trial, mode)
             assert idx.tolist() == want_idx, (trial, mode)
+
+
+# --------------------------------------------------------------------------
+# SSA initial state: periodic moments and the moment-matched draw
+# --------------------------------------------------------------------------
+@pytest.mark.parametrize("lam", [0.3, 3.0, 9.99, 10.0, 37.5, 1000.0, 3e5])
+def test_poisson_sampler_exact_distribution(orc, lam):
+    """Inversion (lam < 10) and PTRS (lam >= 10) against the Poisson pmf: chi-square
+    over the bins with at least 20 expected draws, plus mean and variance."""
+    from scipy import stats
+    n = 200_000
+    x = orc.poisson(lam, n, seed=11)
+    assert abs(x.mean() - lam) < 5 * math.sqrt(lam / n)
+    assert abs(x.var() / lam - 1.0) < 5 * math.sqrt(2.0 / n) + 5.0 / (n * lam) ** 0.5
+    lo, hi = int(stats.poisson.ppf(1e-4, lam)), int(stats.poisson.ppf(1 - 1e-4, lam))
+    edges = np.unique(np.linspace(lo, hi + 1, min(hi - lo + 2, 60)).astype(np.int64))
+    obs = np.histogram(x, bins=np.concatenate([[-1], edges[1:-1], [np.iinfo(np.int64).max]]))[0]
+    cdf = stats.poisson.cdf(np.concatenate([edges[1:-1] - 1, [np.inf]]), lam)
+    exp = np.diff(np.concatenate([[0.0], cdf])) * n
+    keep = exp >= 20
+    chi2 = (((obs - exp) ** 2) / exp)[keep].sum()
+    assert stats.chi2.sf(chi2, keep.sum() - 1) > 1e-4, (chi2, keep.sum())
+
+
+def _periodic_moments_scipy(kon, koff, alpha, gamma, scal, T=20.0, S=5):
+    """Periodic (E G, E u, Cov(G,u), Var u) after division, by iterating the
+    cycle map integrated with LSODA at tight tolerance."""
+    from scipy.integrate import solve_ivp
+
+    def rhs(k):
+        def f(t, y):
+            g, m, c, v = y
+            a = alpha[k] * (1 + t / T) ** scal
+            return [kon[k] - (kon[k] + koff) * g, a * g - gamma[k] * m,
+                    a * g * (1 - g) - (kon[k] + koff + gamma[k]) * c,
+                    a * g + gamma[k] * m + 2 * a * c - 2 * gamma[k] * v]
+        return f
+    y = np.zeros(4)
+    for _ in range(400):
+        z = y.copy()
+        for k in range(S):
+            z = solve_ivp(rhs(k), (k * T / S, (k + 1) * T / S), z, method="LSODA", rtol=1e-11, atol=1e-10).y[:, -1]
+        z = np.array([z[0], z[1] / 2, z[2] / 2, z[3] / 4 + z[1] / 4])
+        if np.max(np.abs(z - y) / (np.abs(z) + 1e-9)) < 1e-11:
+            break
+        y = z
+    return z
+
+
+@pytest.mark.parametrize("model,rates", [(1, [0.5, 1.0, 20.0, 0.01, 0.7]), (2, [0.5, 1.0, 20.0, 0.01, 0.7]),
+                                         (1, [100.0, 300.0, 630.0, 3.0, 0.5]),
+                                         (5, [0.2, 0.05, 50.0, 0.01, 0.02, 0.1, 0.005, 0.03, 0.8]),
+                                         (3, [0.001, 0.01, 0.1, 1.0, 0.05, 0.5, 300.0, 0.002, 0.5])])
+def test_initial_moments_are_the_periodic_solution(orc, model, rates):
+    """The SSA's initial moments (periodic solution of the unlabelled moment
+    equations, model.jl:67-111, with the exponential sub-step integrator)
+    against LSODA at tight tolerance: within 5e-3 relative (second order in
+    the sub-step)."""
+    cfg = make_config("hour", precision=0)
+    r = rates
+    if model == 3:
+        kon, koff, al, ga = r[:5], r[5], [r[6]] * 5, [r[7]] * 5
+    elif model == 5:
+        kon, koff, al, ga = [r[0]] * 5, r[1], [r[2]] * 5, r[3:8]
+    else:
+        kon, koff, al, ga = [r[0]] * 5, r[1], [r[2]] * 5, [r[3]] * 5
+    rec = orc.setup(cfg, model, np.log10(rates))
+    got = rec[[-5, -4, -2, -1]]  # g0, u0, c0, v0
+    want = _periodic_moments_scipy(kon, koff, al, ga, 0.0 if model == 2 else 1.0)
+    assert np.all(np.abs(got - want) <= 5e-3 * np.abs(want) + 1e-9), (got, want)
+
+
+@pytest.mark.parametrize("rates", [[0.5, 1.0, 20.0, 0.01, 0.7], [100.0, 300.0, 630.0, 3.0, 0.5],
+                                   [0.02, 0.01, 300.0, 0.01, 0.5]])
+def test_initial_draw_matches_periodic_moments(orc, rates):
+    """The initial (G, u) the SSA draws reproduce E G, E u, Cov(G, u) and Var u of
+    the periodic solution (zero-inflated Poisson given G), within 4 standard errors."""
+    cfg = make_config("hour", precision=0)
+    th = np.log10(rates)
+    g0, u0, _, c0, v0 = orc.setup(cfg, 1, th)[-5:]
+    n = 400_000
+    G, u = orc.initial_states(cfg, 1, th, n, seed=3)
+    G = G.astype(float)
+    u = u.astype(float)
+    du = u - u.mean()
+    dg = G - G.mean()
+    checks = [(G.mean(), g0, G.var()), (u.mean(), u0, u.var()),
+              ((dg * du).mean(), c0, (dg * du).var()), (u.var(), v0, (du * du).var())]
+    for val, want, var in checks:
+        assert abs(val - want) <= 4 * math.sqrt(var / n) + 1e-9 * abs(want), (val, want, math.sqrt(var / n))

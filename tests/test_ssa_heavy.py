@@ -137,6 +137,9 @@ FP32_THETAS = [
     (5, [2.0, 1.0, 85.0, 2.0, 3.0, 1.0, 1.0, 1.5, 0.7]),
     (4, [0.5, 0.5, 400.0, 630.0, 320.0, 800.0, 500.0, 1.0, 0.6]),  # heavy: alpha ~ 10^2.5-10^2.9 / h
     (3, [0.1, 1.0, 3.0, 10.0, 0.3, 2.0, 630.0, 0.5, 0.8]),         # heavy, switching varies 100-fold
+    # slow decay (gamma = 10^-2 / h): the initial state's variance relaxes least over the three cycles
+    (1, [0.5, 1.0, 20.0, 0.01, 0.7]),
+    (1, [0.05, 0.02, 300.0, 0.01, 0.5]),
 ]
 
 
@@ -172,7 +175,9 @@ def test_ssa_fp32_statistics_within_3_mc_se(Ctx, orc, model, rates):
                 if var > 0:
                     z_mom.append((val - exact) / math.sqrt(var / n))
                 else:
-                    assert val == exact
+                    # every draw equal (e.g. no labelled molecule in a short pulse):
+                    # consistent when the exact value predicts a handful of nonzero draws at most
+                    assert n * abs(val - exact) < 5.0, (j, a, val, exact)
     z = np.concatenate([z_stat[np.isfinite(z_stat)], np.array(z_mom)])
     report = {"model": model, "theta": rates, "replicates": R, "cells_per_group": N,
               "max_abs_z_statistics": float(np.nanmax(np.abs(z_stat))),
@@ -180,7 +185,7 @@ def test_ssa_fp32_statistics_within_3_mc_se(Ctx, orc, model, rates):
               "frac_abs_z_above_3": float((np.abs(z) > 3).mean()), "comparisons": int(z.shape[0]),
               "rel_dev_by_family": family_deviation(mean, ode)}
     if os.environ.get("ABC_REPORT_DIR"):
-        with open(os.path.join(os.environ["ABC_REPORT_DIR"], f"fp32_stats_{model}_{int(rates[2])}.json"), "w") as f:
+        with open(os.path.join(os.environ["ABC_REPORT_DIR"], f"fp32_stats_{model}_{int(rates[2])}_{rates[-2]:g}.json"), "w") as f:
             json.dump(report, f)
     assert np.isfinite(z_stat).sum() >= 50, report
     assert (np.abs(z) > 3).mean() <= 0.01 and np.abs(z).max() <= 4.5, report

@@ -47,6 +47,25 @@ def test_gradients_match_fp64_reference(mods):
                 assert rel < 2e-2, (e, name, rel)
 
 
+def test_training_is_bit_reproducible(mods):
+    """Two trainings from the same seed and data give identical weights and
+    losses: the split-K weight gradients are summed per split in a fixed
+    order and the loss in a fixed block order, so no result depends on the
+    order in which CTAs finish."""
+    S, _ = mods
+    rng = np.random.default_rng(8)
+    in_dim, K, N = 6, 53, 9000
+    theta = rng.uniform(-3, 3, (N, in_dim))
+    stats = np.sinh(theta[:, :1] + rng.normal(0, 0.3, (N, K)))
+    out = []
+    for _ in range(2):
+        with S.Surrogate(in_dim, K, ensemble=2, seed=21) as sg:
+            loss = sg.train(theta, stats, epochs=3, batch=2048, lr=2e-3)
+            out.append((loss, sg.params()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+
+
 def _exact(ctx, theta, seed):
     return ctx.simulate(1, theta, seed=seed)
 
