@@ -69,13 +69,16 @@ def parse():
     ap.add_argument("--abc-wide", action="store_true",
                     help="also run screened vs plain ABC at 8, 50 and 2,000 genes (top 1 %%)")
     ap.add_argument("--no-moment", action="store_true", help="skip the moment-ODE section")
+    ap.add_argument("--config5", action="store_true",
+                    help="also run screened ABC at full scale: 2 x 10^6 training draws, 5 x 10^6 plain draws, "
+                         "5 x 10^7 screened draws per gene set (about 10 minutes)")
     ap.add_argument("--no-graph", action="store_true", help="skip the CUDA-graph check of the chain")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (variant 0, chunk 1)")
     ap.add_argument("--dist-particles", type=int, default=5_000_000)
     ap.add_argument("--genes", type=int, default=2000)
     ap.add_argument("--oracle-genes", type=int, default=64,
                     help="genes of the distance section whose accepted lists are checked against the FP64 oracle")
-    ap.add_argument("--section", default="all", choices=["all", "distance", "moment", "abc"],
+    ap.add_argument("--section", default="all", choices=["all", "distance", "moment", "abc", "config5"],
                     help="'distance' / 'moment' / 'abc' run only that section and print its object")
     return ap.parse_args()
 
@@ -461,6 +464,17 @@ def screened_sections(args):
     return out
 
 
+def config5_section():
+    """Surrogate-screened vs plain ABC at the workload's full scale: the
+    surrogate trained on 2 x 10^6 exact draws (held-out error and calibration
+    on 10^5 of the plain draws), 5 x 10^6 plain draws, and 5 x 10^7 screened
+    draws for each of two sets of 4 genes at top 0.2 %; for 2,000 genes only
+    the plain run's bound on any screen's gain."""
+    from abc_inference_transcription_gb300 import pipeline
+    return pipeline.run(genes=(4, 4), per_model_train=400_000, per_model_plain=1_000_000, screen_factor=10,
+                        q=0.002, seed=3, epochs=40, bound_genes=(2000,))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -482,8 +496,10 @@ def main():
                                                 args.oracle_genes)))
             elif args.section == "moment":
                 print(json.dumps(moment_bench(40000, args.cpu_seconds)))
-            else:
+            elif args.section == "abc":
                 print(json.dumps(screened_sections(args)))
+            else:
+                print(json.dumps(config5_section()))
         return
     dist = None
     if world > 1:
@@ -637,6 +653,11 @@ def main():
             line.update(screened_sections(args))
         except Exception as exc:
             line["abc_screened_small_q"] = {"error": repr(exc)}
+    if args.config5:
+        try:
+            line["config5"] = config5_section()
+        except Exception as exc:
+            line["config5"] = {"error": repr(exc)}
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

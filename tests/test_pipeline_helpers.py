@@ -50,3 +50,13 @@ def test_posterior_agreement_z_statistics():
     # genes with too few accepted particles in either run are skipped
     c = pl.posterior_agreement([np.zeros((5, 5))], [np.zeros((100, 5))])
     assert c == {"genes_compared": 0}
+
+
+def test_binomial_ci_clopper_pearson():
+    from abc_inference_transcription_gb300.pipeline import binomial_ci
+    lo, hi = binomial_ci(0, 100)
+    assert lo == 0.0 and abs(hi - (1 - 0.025 ** (1 / 100))) < 1e-12
+    lo, hi = binomial_ci(100, 100)
+    assert hi == 1.0 and abs(lo - 0.025 ** (1 / 100)) < 1e-12
+    lo, hi = binomial_ci(9, 300)
+    assert lo < 9 / 300 < hi and 0.01 < lo < 0.02 and 0.05 < hi < 0.06
