@@ -168,6 +168,7 @@ def _declare(lib: C.CDLL) -> None:
         "abc_accept_fetch": (C.c_int, [vp, i64p, i64p, dp]),
         "abc_select_counters": (C.c_int, [vp, i64p, i64p]),
         "abc_set_select_errors": (C.c_int, [vp, C.c_int]),
+        "abc_accept_errors": (C.c_int, [vp, dp]),
         "abc_breakpoint_grid": (C.c_int, [C.POINTER(AbcConfig), dp]),
         "abc_write_particles": (C.c_int, [C.c_char_p, C.c_int, C.c_int64, i64p, i64p]),
         "abc_write_matrix": (C.c_int, [C.c_char_p, C.c_int, C.c_int64, C.c_int64, dp, C.c_int64]),
@@ -221,7 +222,7 @@ ABI_SYMBOLS = [
     "abc_profile", "abc_profile_read", "abc_autotune", "abc_autotune_batch", "abc_set_variant",
     "abc_set_work_chunk", "abc_errors",
     "abc_errors_select", "abc_errors_select_thr", "abc_errors_select_device", "abc_accept_fetch",
-    "abc_select_counters", "abc_select_profile_read", "abc_set_select_errors", "abc_breakpoint_grid", "abc_write_particles", "abc_write_matrix",
+    "abc_select_counters", "abc_select_profile_read", "abc_set_select_errors", "abc_accept_errors", "abc_breakpoint_grid", "abc_write_particles", "abc_write_matrix",
     "abc_format_double", "abc_read_particles", "abc_set_distance_mode", "abc_get_distance_mode",
     "abc_errors_candidate", "abc_model_probs", "abc_posterior_summary",
     "abc_moment_simulate", "abc_data_stats", "abc_set_graph", "abc_graph_counters",

@@ -115,6 +115,9 @@ struct abc_ctx {
   bool sel_ready = false;
   bool sel_errors = true;        // selections keep the FP64 error of every accepted pair
   bool sel_errors_exact = true;  // the last selection's stored errors are FP64
+  DistInputs sel_in;             // inputs of the last selection (device buffers; stats as given)
+  DBuf<int32_t> d_asp, d_asg;    // accepted pairs for abc_accept_errors
+  DBuf<double> d_aerr;
   DBuf<float4> d_ffg;
   DBuf<int32_t> d_pos;
   DBuf<uint8_t> d_flag;
@@ -1058,6 +1061,7 @@ static int select_impl(abc_ctx* c, const double* data, const double* se, int64_t
   DistInputs in;
   int st = load_dist_inputs(c, data, se, G, K, n_fam, fam, stats, P, in, stats_on_device);
   if (st) return st;
+  c->sel_in = in;
   CK(c->d_thr.ensure((size_t)G));
   if (mode == 2) CK(cudaMemcpyAsync(c->d_thr.p, thr, sizeof(double) * G, cudaMemcpyHostToDevice, c->stream));
   CK(c->d_X.ensure((size_t)G));
@@ -1267,6 +1271,26 @@ int abc_accept_fetch(abc_ctx* c, int64_t* gene_offsets, int64_t* particle_idx, d
         return fail(c, ABC_ERR_STATE, "the selection kept no FP64 errors (abc_set_select_errors(ctx, 0)); pass err = NULL");
       CK(cudaMemcpyAsync(err, c->d_out_err.p, sizeof(double) * c->sel_total, cudaMemcpyDeviceToHost, c->stream));
     }
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return ABC_OK;
+}
+
+int abc_accept_errors(abc_ctx* c, double* err) {
+  if (!c) return ABC_ERR_INVALID;
+  if (!c->sel_ready) return fail(c, ABC_ERR_STATE, "no selection result: call abc_errors_select first");
+  if (c->sel_total <= 0) return ABC_OK;
+  if (!err) return fail(c, ABC_ERR_INVALID, "null output");
+  if (c->sel_errors_exact) {
+    CK(cudaMemcpyAsync(err, c->d_out_err.p, sizeof(double) * c->sel_total, cudaMemcpyDeviceToHost, c->stream));
+  } else {
+    const size_t n = (size_t)c->sel_total;
+    CK(c->d_asp.ensure(n));
+    CK(c->d_asg.ensure(n));
+    CK(c->d_aerr.ensure(n));
+    CK(launch_accepted_errors(c->sel_in, c->d_aoff.p, c->d_out_idx.p, c->sel_G, 0, c->sel_total, c->d_asp.p,
+                              c->d_asg.p, c->d_aerr.p, c->stream));
+    CK(cudaMemcpyAsync(err, c->d_aerr.p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
   }
   CK(cudaStreamSynchronize(c->stream));
   return ABC_OK;

@@ -710,6 +710,25 @@ cudaError_t launch_dist_compact(const int64_t* goff, const int32_t* sp, const do
   return cudaGetLastError();
 }
 
+// (particle, gene) of every accepted pair, in the lists' order (grouped by gene)
+__global__ void accepted_pairs_kernel(const int64_t* aoff, const int64_t* idx, int64_t G, int64_t p_base, int32_t* sp,
+                                      int32_t* sg) {
+  const int64_t g = blockIdx.x;
+  if (g >= G) return;
+  for (int64_t i = aoff[g] + threadIdx.x; i < aoff[g + 1]; i += blockDim.x) {
+    sp[i] = (int32_t)(idx[i] - 1 - p_base);
+    sg[i] = (int32_t)g;
+  }
+}
+
+cudaError_t launch_accepted_errors(const DistInputs& in, const int64_t* aoff, const int64_t* idx, int64_t G,
+                                   int64_t p_base, int64_t n, int32_t* sp, int32_t* sg, double* err, cudaStream_t s) {
+  if (G <= 0 || n <= 0) return cudaSuccess;
+  accepted_pairs_kernel<<<(unsigned)G, 256, 0, s>>>(aoff, idx, G, p_base, sp, sg);
+  recheck_grouped_kernel<<<grouped_blocks(n), kRecheckWarps * 32, 0, s>>>(in, sp, sg, n, err);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_scan(const int64_t* cnt, int64_t G, int64_t* off, cudaStream_t s) {
   scan_kernel<<<1, 1024, 0, s>>>(cnt, G, off);
   return cudaGetLastError();

@@ -147,6 +147,11 @@ cudaError_t launch_dist_accept_len(const int64_t* goff, const double* se64, int6
 cudaError_t launch_dist_compact(const int64_t* goff, const int32_t* sp, const double* se64, const int64_t* aoff,
                                 int64_t G, int64_t p_base, int64_t* idx, double* err, cudaStream_t s);
 cudaError_t launch_scan(const int64_t* cnt, int64_t G, int64_t* off, cudaStream_t s);
+// FP64 errors, in the reference's operation order, of accepted pairs given as
+// per-gene lists (offsets aoff, 1-based indices idx - p_base); needs in.den,
+// in.rden.  sp, sg: n scratch entries each.
+cudaError_t launch_accepted_errors(const DistInputs& in, const int64_t* aoff, const int64_t* idx, int64_t G,
+                                   int64_t p_base, int64_t n, int32_t* sp, int32_t* sg, double* err, cudaStream_t s);
 // full FP64 error matrix [P][G]
 cudaError_t launch_dist_full(const DistInputs& in, double* err, cudaStream_t s);
 

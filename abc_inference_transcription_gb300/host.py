@@ -229,6 +229,7 @@ class Context:
         return self._fetch(G, tot.value, errors)
 
     def _fetch(self, G: int, total: int, errors: bool = True):
+        self._last_total = total
         self._sel_G = G
         off = np.zeros(G + 1, np.int64)
         idx = np.empty(max(total, 1), np.int64)
@@ -265,6 +266,15 @@ class Context:
                                                       C.c_void_p(d_stats), n, mode, float(eps_or_q), ptr(t),
                                                       C.byref(tot)))
         return self._fetch(G, tot.value, errors)
+
+    def accept_errors(self) -> np.ndarray:
+        """FP64 errors of the last selection's accepted pairs (computed for them
+        alone when the selection returned indices only)."""
+        total = int(getattr(self, "_last_total", 0))
+        out = np.zeros(total)
+        if total:
+            self._check(self.lib.abc_accept_errors(self.h, ptr(out)))
+        return out
 
     def select_profile(self) -> tuple[float, int]:
         """(candidate-pass kernel ms, passes) of the last selection (needs profile(True))."""
@@ -430,6 +440,18 @@ def merge_accept_lists(parts, mode: int, eps_or_q: float, n_particles: int):
         offs.append(offs[-1] + order.shape[0])
     return (np.asarray(offs, np.int64), np.concatenate(idx_out) if idx_out else np.zeros(0, np.int64),
             np.concatenate(err_out) if err_out else np.zeros(0))
+
+
+def shard_select(ctx: Context, data: np.ndarray, se: np.ndarray, d_stats: int, n_shard: int, start: int, mode: int,
+                 eps_or_q: float, n_particles: int, families=None):
+    """One shard's part of a sharded acceptance: the fast indices-only
+    selection over the shard's particles (statistics in device memory), its
+    accepted lists (top-q with the global k), the FP64 errors of those pairs
+    only, and global 1-based indices -- an entry of merge_accept_lists' parts."""
+    q = local_select_q(eps_or_q, n_particles, n_shard) if mode == 1 else eps_or_q
+    off, idx, _ = ctx.select_device(data, se, d_stats, n_shard, mode, q, families=families, errors=False)
+    err = ctx.accept_errors()
+    return off, idx + start, err
 
 
 def local_select_q(q: float, n_particles: int, n_shard: int) -> float:

@@ -249,6 +249,14 @@ int abc_errors_select_device(abc_ctx* ctx, const double* data, const double* se,
  * abc_accept_fetch then requires err = NULL.  The reference's acceptance
  * writes indices only (scripts/accepted_particles.jl:21-29). */
 int abc_set_select_errors(abc_ctx* ctx, int keep_errors);
+/* FP64 errors (compute_errors.jl:30-43, 62-64, the reference's operation
+ * order) of the last selection's accepted pairs, in the order of
+ * abc_accept_fetch's indices; for selections made with
+ * abc_set_select_errors(ctx, 0), computed now for the accepted pairs only --
+ * e.g. a particle shard's local top-k, which a host merge of several shards'
+ * lists needs.  The statistics of the selection must still be in place (a
+ * d_stats pointer given to abc_errors_select_device). */
+int abc_accept_errors(abc_ctx* ctx, double* err);
 /* gene_offsets: G+1 entries; particle_idx: 1-based, n_accepted_total entries;
  * err: FP64 errors of the accepted pairs (may be NULL; must be NULL after a
  * selection with abc_set_select_errors(ctx, 0)). */
