@@ -19,7 +19,7 @@ def H(built):
     return host
 
 
-@pytest.mark.parametrize("mode,eps_or_q", [(1, 0.01), (1, 0.003), (0, 0.2)])
+@pytest.mark.parametrize("mode,eps_or_q", [(1, 0.01), (1, 0.003), (0, 4.8)])  # 4.8: accepted_particles.jl:10
 def test_sharded_selection_merges_to_single_run(H, mode, eps_or_q):
     import torch
     z = np.load(f"{GOLDEN}/summary_stats.npz")

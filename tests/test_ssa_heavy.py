@@ -131,6 +131,17 @@ def family_deviation(mean: np.ndarray, ode: np.ndarray) -> dict:
     return out
 
 
+def family_z(z: np.ndarray) -> dict:
+    """Largest |z| (replicate mean vs moment ODE, in Monte Carlo standard errors) per statistic family."""
+    names = ["pulse_mean", "pulse_ff", "chase_mean", "chase_ff", "ratio", "mean_corr", "corr_mean"]
+    sizes = [5, 5, 5, 5, 11, 11, 11]
+    out, k = {}, 0
+    for nm, n in zip(names, sizes):
+        out[nm] = float(np.nanmax(np.abs(z[k:k + n])))
+        k += n
+    return out
+
+
 FP32_THETAS = [
     (1, [0.5, 1.0, 20.0, 0.1, 0.7]),                          # scripts/model_realisation.jl:294-315
     (3, [0.1, 0.1, 30.0, 0.1, 0.1, 1.0, 15.0, 0.1, 0.7]),
@@ -183,7 +194,7 @@ def test_ssa_fp32_statistics_within_3_mc_se(Ctx, orc, model, rates):
               "max_abs_z_statistics": float(np.nanmax(np.abs(z_stat))),
               "max_abs_z_group_moments": float(np.max(np.abs(z_mom))),
               "frac_abs_z_above_3": float((np.abs(z) > 3).mean()), "comparisons": int(z.shape[0]),
-              "rel_dev_by_family": family_deviation(mean, ode)}
+              "rel_dev_by_family": family_deviation(mean, ode), "max_abs_z_by_family": family_z(z_stat)}
     if os.environ.get("ABC_REPORT_DIR"):
         with open(os.path.join(os.environ["ABC_REPORT_DIR"], f"fp32_stats_{model}_{int(rates[2])}_{rates[-2]:g}.json"), "w") as f:
             json.dump(report, f)
