@@ -310,6 +310,274 @@ __global__ void __launch_bounds__(kThreads, 1)
 }
 
 // ---------------------------------------------------------------------------
+// One-term candidate pass with the gene operand resident in shared memory.
+//
+// A 128 x 256 tile of the streaming kernel above loads 80 KB of particle rows
+// and 160 KB of gene rows (depth 160) through L2 for about 1.4 us of one-term
+// MMAs, which makes L2-to-SM bandwidth the limit.  Here each CTA keeps the
+// gene rows of one 256-gene tile (n_chunks x 32 KB) in shared memory for all
+// of its particle tiles and streams only the particle rows through a ring of
+// 16 KB stages.  Work: nN gene tiles x cpt = max(1, grid / nN) particle-tile
+// sequences (m = j, j + cpt, ...), handed to the CTAs round-robin; the CTAs
+// that hold different gene tiles walk the same particle sequence in the same
+// order, so each particle tile comes from DRAM about once and from L2 after
+// that.  Roles, barriers, bounded waits and the epilogue are those of
+// dist_tc_kernel; two more barriers (bfull, bempty) order the gene-row loads
+// of successive assignments against the MMAs that read them.
+// ---------------------------------------------------------------------------
+constexpr int kResMaxStages = 4;
+constexpr uint32_t kResSmemMax = 227u * 1024u;  // dynamic shared memory of one CTA
+
+__host__ __device__ constexpr uint32_t res_smem(int n_chunks, int stages) {
+  return 1024u + (uint32_t)n_chunks * kBBytes + (uint32_t)stages * kABytes + 256u + 2u * BN * 4u;
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    dist_tc_res_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs a,
+                       int S) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = smem_raw + ((1024u - (su32(smem_raw) & 1023u)) & 1023u);
+  const int NC = a.n_chunks;
+  uint8_t* ring = smem + (uint32_t)NC * kBBytes;
+  uint64_t* full = (uint64_t*)(ring + (uint32_t)S * kABytes);
+  uint64_t* empty = full + kResMaxStages;
+  uint64_t* tfull = empty + kResMaxStages;
+  uint64_t* tempty = tfull + 2;
+  uint64_t* bfull = tempty + 2;
+  uint64_t* bempty = bfull + 1;
+  uint64_t* drain = bempty + 1;
+  uint32_t* tslot = (uint32_t*)(drain + 1);
+  uint32_t* s_count = tslot + 1;
+  uint32_t* s_abort = tslot + 2;
+  float* Ys = (float*)((uint8_t*)full + 256);
+  float* Cs = Ys + BN;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < S; ++st) {
+      mbar_init(&full[st], 1);
+      mbar_init(&empty[st], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], kEpiThreads);
+    }
+    mbar_init(bfull, 1);
+    mbar_init(bempty, 1);
+    mbar_init(drain, 1);
+    *s_count = 0;
+    *s_abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tslot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = *tslot;
+  const uint32_t b_base = su32(smem), ring_base = su32(ring);
+  const int cpt = max(1, (int)gridDim.x / a.nN);
+  const int n_assign = a.nN * cpt;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---------------- TMA producer: gene rows once per assignment, particle rows per tile
+      int stage = 0;
+      uint32_t phase = 0, issued = 0, issued_par = 0;
+      bool ok = true;
+      uint32_t b_issued = 0;  // gene-row loads issued (one per assignment)
+      for (int as = blockIdx.x; as < n_assign && ok; as += gridDim.x) {
+        const int n = as % a.nN, j = as / a.nN;
+        if (b_issued > 0 && !mbar_wait(bempty, (b_issued - 1) & 1u)) {  // the previous gene rows are no longer read
+          atomicOr(a.err, kErrProducer);
+          break;
+        }
+        mbar_expect_tx(bfull, (uint32_t)NC * kBBytes);
+        for (int c = 0; c < NC; ++c) tma_load(b_base + (uint32_t)c * kBBytes, &tmB, bfull, c * BK, n * BN);
+        ++b_issued;
+        for (int m = j; m < a.nM && ok; m += cpt) {
+          for (int c = 0; c < NC; ++c) {
+            if (!mbar_wait(&empty[stage], phase ^ 1)) {
+              atomicOr(a.err, kErrProducer);
+              ok = false;
+              break;
+            }
+            mbar_expect_tx(&full[stage], kABytes);
+            tma_load(ring_base + (uint32_t)stage * kABytes, &tmA, &full[stage], c * BK, m * BM);
+            issued |= 1u << stage;
+            issued_par = (issued_par & ~(1u << stage)) | (phase << stage);
+            if (++stage == S) {
+              stage = 0;
+              phase ^= 1;
+            }
+          }
+        }
+      }
+      // loads still in flight land before the CTA leaves
+      for (int st = 0; st < S; ++st)
+        if ((issued >> st) & 1u)
+          if (!mbar_wait(&full[st], (issued_par >> st) & 1u)) atomicOr(a.err, kErrDrain);
+      if (b_issued > 0 && !mbar_wait(bfull, (b_issued - 1) & 1u)) atomicOr(a.err, kErrDrain);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---------------- MMA issuer
+      int stage = 0;
+      uint32_t phase = 0;
+      int acc = 0;
+      uint32_t acc_phase = 0;
+      bool ok = true;
+      uint32_t k_as = 0;
+      for (int as = blockIdx.x; as < n_assign && ok; as += gridDim.x, ++k_as) {
+        const int j = as / a.nN;
+        if (!mbar_wait(bfull, k_as & 1u)) {
+          atomicOr(a.err, kErrMma);
+          break;
+        }
+        for (int m = j; m < a.nM && ok; m += cpt) {
+          if (!mbar_wait(&tempty[acc], acc_phase ^ 1)) {
+            atomicOr(a.err, kErrMma);
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t d_tmem = tbase + (uint32_t)(acc * BN);
+          for (int c = 0; c < NC; ++c) {
+            if (!mbar_wait(&full[stage], phase)) {
+              atomicOr(a.err, kErrMma);
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint64_t a0 = sw128_desc(ring_base + (uint32_t)stage * kABytes);
+            const uint64_t b0 = sw128_desc(b_base + (uint32_t)c * kBBytes);
+#pragma unroll
+            for (int kk = 0; kk < BK / 8; ++kk) {
+              const uint64_t adv = (uint64_t)(kk * 32) >> 4;  // 8 TF32 = 32 bytes along K
+              mma_tf32(d_tmem, a0 + adv, b0 + adv, (c | kk) != 0);
+            }
+            mma_commit(&empty[stage]);
+            if (++stage == S) {
+              stage = 0;
+              phase ^= 1;
+            }
+          }
+          if (!ok) break;
+          mma_commit(&tfull[acc]);
+          if (++acc == 2) {
+            acc = 0;
+            acc_phase ^= 1;
+          }
+        }
+        mma_commit(bempty);  // the gene rows may be replaced once these MMAs are done
+      }
+      mma_commit(drain);
+      if (!mbar_wait(drain, 0)) atomicOr(a.err, kErrDrain);
+    }
+  } else {
+    // ---------------- epilogue (as in dist_tc_kernel)
+    const int et = threadIdx.x - 64;
+    const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
+    const float invK = 1.0f / (float)a.K;
+    int acc = 0;
+    uint32_t acc_phase = 0;
+    bool stop = false;
+    for (int as = blockIdx.x; as < n_assign && !stop; as += gridDim.x) {
+      const int n = as % a.nN, j = as / a.nN;
+      for (int m = j; m < a.nM; m += cpt) {
+        epi_bar();  // readers of the previous tile's Y / c are done
+        for (int jj = et; jj < BN; jj += kEpiThreads) {
+          const int64_t g = (int64_t)n * BN + jj;
+          Ys[jj] = g < a.G ? a.Y[g] : -INFINITY;
+          Cs[jj] = g < a.G ? a.cg[g] : 0.0f;
+        }
+        const bool got = mbar_wait(&tfull[acc], acc_phase);
+        if (!got) atomicOr(s_abort, 1u);
+        epi_bar();
+        if (*(volatile uint32_t*)s_abort) {
+          atomicOr(a.err, kErrEpilogue);
+          stop = true;
+          break;
+        }
+        tc_fence_after();
+        const int64_t row = (int64_t)m * BM + q * 32 + lane;
+        const bool valid = row < a.P;
+        const uint32_t lane_addr = tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN);
+#pragma unroll 1
+        for (int c4 = 0; c4 < BN / 64; ++c4) {
+          const int cc = half * (BN / 64) + c4;
+          __syncwarp();
+          uint32_t v[32];
+          tmem_ld32(lane_addr + (uint32_t)(cc * 32), v);
+          const float4* Y4 = reinterpret_cast<const float4*>(Ys + cc * 32);
+          float dm[8];
+#pragma unroll
+          for (int j4 = 0; j4 < 8; ++j4) {
+            const float4 y = Y4[j4];
+            dm[j4] = fminf(fminf(__uint_as_float(v[4 * j4 + 0]) - y.x, __uint_as_float(v[4 * j4 + 1]) - y.y),
+                           fminf(__uint_as_float(v[4 * j4 + 2]) - y.z, __uint_as_float(v[4 * j4 + 3]) - y.w));
+          }
+          const float dmin = fminf(fminf(fminf(dm[0], dm[1]), fminf(dm[2], dm[3])),
+                                   fminf(fminf(dm[4], dm[5]), fminf(dm[6], dm[7])));
+          const bool has = valid && dmin <= 0.0f;
+          if (__ballot_sync(0xffffffffu, has) == 0u) continue;
+          uint32_t msk = 0;
+          if (has) {
+#pragma unroll
+            for (int jb = 0; jb < 32; ++jb) msk |= (uint32_t)(__uint_as_float(v[jb]) <= Ys[cc * 32 + jb]) << jb;
+          }
+          const uint32_t cnt = __popc(msk);
+          uint32_t incl = cnt;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+          }
+          uint32_t base = 0;
+          if (lane == 31) base = atomicAdd(s_count, incl);
+          base = __shfl_sync(0xffffffffu, base, 31);
+          if (msk) {
+            float vv[32];
+#pragma unroll
+            for (int jb = 0; jb < 32; ++jb) vv[jb] = __uint_as_float(v[jb]);
+            uint32_t pos = base + incl - cnt;
+            while (msk) {
+              const int jb = __ffs(msk) - 1;
+              msk &= msk - 1;
+              if ((int64_t)pos < a.seg_cap) {
+                const int64_t slot = (int64_t)blockIdx.x * a.seg_cap + pos;
+                Cand cd;
+                cd.p = (int32_t)row;
+                cd.g = (int32_t)((int64_t)n * BN + cc * 32 + jb);
+                a.cand[slot] = cd;
+                a.cand_e[slot] = fminf((vv[jb] + Cs[cc * 32 + jb]) * invK, 10.0f);
+              }
+              ++pos;
+            }
+          }
+        }
+        tc_fence_before();
+        mbar_arrive(&tempty[acc]);
+        if (++acc == 2) {
+          acc = 0;
+          acc_phase ^= 1;
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(kTmemCols));
+  if (threadIdx.x == 0) a.seg_count[blockIdx.x] = *s_count;
+}
+
+// ---------------------------------------------------------------------------
 // operand preparation
 // ---------------------------------------------------------------------------
 
@@ -578,9 +846,30 @@ int tc_grid(int64_t P, int64_t G, int sms) {
   return (int)(tiles < sms ? tiles : sms);
 }
 
+static cudaError_t launch_res(const float* A, const float* B, const TcArgs& args, int grid, int stages,
+                              cudaStream_t s) {
+  const uint32_t smem = res_smem(args.n_chunks, stages);
+  static std::atomic<uint64_t> attr{0};
+  // the largest configuration sets the limit once per device; smaller ones fit under it
+  cudaError_t e = set_smem_once(attr, dist_tc_res_kernel, (int)kResSmemMax);
+  if (e != cudaSuccess) return e;
+  CUtensorMap ma, mb;
+  if (!make_map(&ma, A, args.P, args.KA, BM) || !make_map(&mb, B, args.G, args.KA, BN)) return cudaErrorInvalidValue;
+  dist_tc_res_kernel<<<grid, kThreads, smem, s>>>(ma, mb, args, stages);
+  return cudaGetLastError();
+}
+
+int tc_res_stages(int n_chunks) {
+  for (int st = kResMaxStages; st >= 2; --st)
+    if (res_smem(n_chunks, st) <= kResSmemMax) return st;
+  return 0;
+}
+
 cudaError_t launch_dist_tc(int nh, const float* A, const float* B, const TcArgs& args, int grid, cudaStream_t s) {
   if (args.P <= 0 || args.G <= 0) return cudaSuccess;
-  return nh == 2 ? launch_nh<2>(A, B, args, grid, s) : launch_nh<1>(A, B, args, grid, s);
+  if (nh == 2) return launch_nh<2>(A, B, args, grid, s);
+  const int stages = tc_res_stages(args.n_chunks);
+  return stages ? launch_res(A, B, args, grid, stages, s) : launch_nh<1>(A, B, args, grid, s);
 }
 
 cudaError_t launch_tc_gather(const Cand* seg, const float* seg_e, const unsigned* count, int n_seg, int64_t seg_cap,
