@@ -938,7 +938,7 @@ static int candidate_pass_simt(abc_ctx* c, const DistInputs& in, int64_t* n) {
 // segments are concatenated into d_cand / d_cande.
 static int candidate_pass_tc(abc_ctx* c, const DistInputs& in, int nh, int64_t* n) {
   const int grid = tc_grid(in.P, in.G, c->sms);
-  const int KA = tc_ka(in.K);
+  const int KA = tc_ka(in.K, nh);
   CK(launch_tc_y(c->d_X.p, c->d_cg64.p, in.G, in.K, c->d_Y.p, c->stream));
   CK(c->d_segcount.ensure((size_t)grid));
   CK(c->d_tcerr.ensure(1));
@@ -953,11 +953,10 @@ static int candidate_pass_tc(abc_ctx* c, const DistInputs& in, int nh, int64_t* 
     a.G = in.G;
     a.K = in.K;
     a.KA = KA;
-    a.n_chunks = KA / 32;
+    a.n_chunks = KA / (nh == 3 ? 64 : 32);  // one 128-byte row per chunk
     a.nM = (int)((in.P + 127) / 128);
     a.nN = (int)((in.G + 255) / 256);
     a.Y = c->d_Y.p;
-    a.cg = c->d_cg32.p;
     a.cand = c->d_seg.p;
     a.cand_e = c->d_seg_e.p;
     a.seg_cap = c->seg_cap;
@@ -986,8 +985,8 @@ static int candidate_pass_tc(abc_ctx* c, const DistInputs& in, int nh, int64_t* 
     if (mx <= c->seg_cap) {
       CK(c->d_cand.ensure((size_t)std::max<int64_t>(total, 1)));
       CK(c->d_cande.ensure((size_t)std::max<int64_t>(total, 1)));
-      CK(launch_tc_gather(c->d_seg.p, c->d_seg_e.p, c->d_segcount.p, grid, c->seg_cap, c->d_cand.p, c->d_cande.p,
-                          c->stream));
+      CK(launch_tc_gather(c->d_seg.p, c->d_seg_e.p, c->d_segcount.p, grid, c->seg_cap, c->d_cg32.p, in.K, c->d_cand.p,
+                          c->d_cande.p, c->stream));
       *n = total;
       return ABC_OK;
     }
@@ -1008,9 +1007,11 @@ static int prepare_candidate_pass(abc_ctx* c, const DistInputs& in, int* dmode_o
   int dmode = c->dist_mode;
   float b1 = 0.0f;
   if (dmode) {
-    const int KA = tc_ka(K);
-    CK(c->d_tcA.ensure((size_t)P * dmode * KA));
-    CK(c->d_tcB.ensure((size_t)G * dmode * KA));
+    const int KA = tc_ka(K, dmode);
+    // FP32-sized words per row: hi (and lo) TF32 halves, or hi + lo BF16 halves in KA words
+    const size_t words = dmode == 3 ? (size_t)KA : (size_t)dmode * KA;
+    CK(c->d_tcA.ensure((size_t)P * words));
+    CK(c->d_tcB.ensure((size_t)G * words));
     CK(c->d_cg64.ensure((size_t)G));
     CK(c->d_cg32.ensure((size_t)G));
     CK(c->d_Y.ensure((size_t)G));
@@ -1531,7 +1532,7 @@ int abc_posterior_summary(abc_ctx* c, const double* theta, int64_t ld, int npar,
 
 int abc_set_distance_mode(abc_ctx* c, int mode) {
   if (!c) return ABC_ERR_INVALID;
-  if (mode < 0 || mode > 2) return fail(c, ABC_ERR_INVALID, "distance mode must be 0, 1 or 2");
+  if (mode < 0 || mode > 3) return fail(c, ABC_ERR_INVALID, "distance mode must be 0, 1, 2 or 3");
   c->dist_mode = mode;
   return ABC_OK;
 }

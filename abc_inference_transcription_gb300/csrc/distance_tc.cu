@@ -1,6 +1,6 @@
-// distance_tc.cu — the particle x gene candidate pass as a TF32 tensor-core
-// GEMM (tcgen05 MMA, accumulators in tensor memory, operands staged by TMA)
-// with a fused candidate epilogue.
+// distance_tc.cu — the particle x gene candidate pass as a tensor-core GEMM
+// (tcgen05 MMA with TF32 or BF16 operands, accumulators in tensor memory,
+// operands staged by TMA) with a fused candidate epilogue.
 //
 // The reference error (scripts/compute_errors.jl:30-43) of particle p for gene g
 // is (1/K) sum_k w_gk (d_gk - s_pk)^2, w_gk = 1/((se_gk^2 + 0.01 d_gk^2) + eps_gk).
@@ -8,24 +8,27 @@
 //   K err_pg = c_g + sum_k [ (-2 w_gk d_gk) s_pk + w_gk s_pk^2 ],   c_g = sum_k w_gk d_gk^2,
 // i.e. one GEMM of A = [s | s^2] (particles, K-major rows) against
 // B = [-2 w d | w] (genes, K-major rows) of depth 2K, FP32 accumulation.
-// Three-term mode splits each operand into TF32 hi + lo parts and accumulates
-// hi*hi + hi*lo + lo*hi, so every product is exact to ~2^-21.
+// Three-term modes split each operand into hi + lo parts and accumulate
+// hi*hi + hi*lo + lo*hi: TF32 parts leave every product exact to ~2^-21,
+// BF16 parts (MMAs at twice the TF32 rate, half the operand bytes) to ~2^-17.
 //
-// CTA: 10 warps, one persistent CTA per SM.  Warp 0 issues TMA loads of
-// 128 x 32 (A) and 256 x 32 (B) FP32 boxes with the 128-byte swizzle into a
-// ring of shared-memory stages; warp 1 owns 512 tensor-memory columns (two
-// 128 x 256 FP32 accumulators) and issues the MMAs; warps 2-9 read the
-// finished accumulator (two warps per TMEM lane quarter, half of the columns
-// each), compare acc <= Y_g
-// (Y_g = K X_g - c_g rounded up) and append candidates, with their FP32
-// error clipped at 10 like the reference's, to this CTA's own output segment
-// through a shared-memory counter.  The epilogue of one tile
+// CTA: 18 warps, one persistent CTA per SM.  Warp 0 issues TMA loads of
+// 128 x 128-byte (A) and 256 x 128-byte (B) boxes with the 128-byte swizzle
+// into a ring of shared-memory stages; warp 1 owns 512 tensor-memory columns
+// (two 128 x 256 FP32 accumulators) and issues the MMAs; warps 2-17 read the
+// finished accumulator (four warps per TMEM lane quarter, a quarter of the
+// columns each), compare acc <= Y_g (Y_g = K X_g - c_g rounded up) and append
+// candidates with their raw accumulator to this CTA's own output segment
+// through a shared-memory counter; the gather that concatenates the segments
+// turns the accumulator into the FP32 error, clipped at 10 like the
+// reference's.  The epilogue of one tile
 // overlaps the MMAs of the next.  Every wait on an mbarrier is bounded by a
 // clock limit; a wait that runs out sets an error bit, the CTA stops issuing
 // work, waits (bounded) for its copies and MMAs in flight, frees its tensor
 // memory and returns.
 #include <cuda.h>
 #include <cudaTypedefs.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -45,8 +48,9 @@ using namespace tc;
 constexpr int BM = 128;          // particles per tile = TMEM lanes
 constexpr int BN = 256;          // genes per tile = TMEM columns per accumulator
 constexpr int BK = 32;           // FP32 values per 128-byte swizzled row (one TMA box width)
-constexpr int kEpiWarps = 8;                 // two per TMEM lane quarter, each half of the columns
+constexpr int kEpiWarps = 16;                // four per TMEM lane quarter, each a quarter of the columns
 constexpr int kEpiThreads = 32 * kEpiWarps;
+constexpr int kEpiGroups = BN / 32 / (kEpiWarps / 4);  // 32-column groups per epilogue warp
 constexpr int kThreads = 64 + kEpiThreads;
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kABytes = BM * BK * 4;    // 16 KB
@@ -57,8 +61,8 @@ struct Cfg {
   static constexpr int kStages = NH == 1 ? 4 : 2;
   static constexpr uint32_t kStageBytes = NH * (kABytes + kBBytes);
   static constexpr uint32_t kTileBytes = kStages * kStageBytes;
-  // tiles + barriers (2 S + 5) + tmem slot + counters + per-gene Y and c of a tile
-  static constexpr uint32_t kSmem = 1024 + kTileBytes + 256 + 2 * BN * 4;
+  // tiles + barriers (2 S + 5) + tmem slot + counters + per-gene Y of a tile
+  static constexpr uint32_t kSmem = 1024 + kTileBytes + 256 + BN * 4;
 };
 
 // Instruction descriptor: D = F32, A = B = TF32, both K-major, M = 128, N = 256.
@@ -73,13 +77,116 @@ __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b
       "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
       : "memory");
 }
+
+// The same tile shape with BF16 operands (D = F32, A = B = BF16, K-major, K = 16 per MMA).
+constexpr uint32_t kIdescBf16 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                                ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(kIdescBf16), "r"(accumulate)
+      : "memory");
+}
+
+// one K-step (32 bytes of a 128-byte swizzled row: 8 TF32 or 16 BF16 values)
+template <bool BF>
+__device__ __forceinline__ void mma_step(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+  if (BF)
+    mma_bf16(d_tmem, a, b, accumulate);
+  else
+    mma_tf32(d_tmem, a, b, accumulate);
+}
 __device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory"); }
+
+// v[j] for a lane-dependent j, by a 5-level select tree on the bits of j
+// (a dynamically indexed register array would go to local memory).
+__device__ __forceinline__ float pick32(const uint32_t (&v)[32], uint32_t j) {
+  uint32_t a16[16], a8[8], a4[4], a2[2];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) a16[i] = (j & 1u) ? v[2 * i + 1] : v[2 * i];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) a8[i] = (j & 2u) ? a16[2 * i + 1] : a16[2 * i];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) a4[i] = (j & 4u) ? a8[2 * i + 1] : a8[2 * i];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) a2[i] = (j & 8u) ? a4[2 * i + 1] : a4[2 * i];
+  return __uint_as_float((j & 16u) ? a2[1] : a2[0]);
+}
+
+// Epilogue of one warp: its 32 accumulator rows (one TMEM lane quarter, lane =
+// particle row) x NG groups of 32 columns starting at TMEM address taddr.
+// Bit j of a lane's mask is acc <= Y_j (false for NaN).  A warp with any
+// candidate takes its positions in the CTA segment with one shared-memory
+// atomic plus the lanes' exclusive prefix (a ballot when no lane holds more
+// than one candidate, the common case); each candidate stores (p, g) and the
+// raw accumulator, which tc_gather_kernel turns into the clipped FP32 error.
+template <int NG>
+__device__ __forceinline__ void epi_warp(uint32_t taddr, const float* Ycol, int64_t row, bool valid, int64_t g0,
+                                         uint32_t* s_count, const TcArgs& a, int lane) {
+#pragma unroll 1
+  for (int gi = 0; gi < NG; ++gi) {
+    __syncwarp();
+    uint32_t v[32];
+    tmem_ld32(taddr + (uint32_t)(gi * 32), v);
+    const float4* Y4 = reinterpret_cast<const float4*>(Ycol + gi * 32);
+    uint32_t msk = 0;
+#pragma unroll
+    for (int j4 = 0; j4 < 8; ++j4) {
+      const float4 y = Y4[j4];
+      msk |= (uint32_t)(__uint_as_float(v[4 * j4 + 0]) <= y.x) << (4 * j4 + 0);
+      msk |= (uint32_t)(__uint_as_float(v[4 * j4 + 1]) <= y.y) << (4 * j4 + 1);
+      msk |= (uint32_t)(__uint_as_float(v[4 * j4 + 2]) <= y.z) << (4 * j4 + 2);
+      msk |= (uint32_t)(__uint_as_float(v[4 * j4 + 3]) <= y.w) << (4 * j4 + 3);
+    }
+    if (!valid) msk = 0;
+    const uint32_t has = __ballot_sync(0xffffffffu, msk != 0u);
+    if (has == 0u) continue;
+    const uint32_t cnt = __popc(msk);
+    uint32_t excl, total;
+    if (__all_sync(0xffffffffu, cnt <= 1u)) {
+      excl = __popc(has & ((1u << lane) - 1u));
+      total = __popc(has);
+    } else {
+      uint32_t incl = cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      excl = incl - cnt;
+      total = __shfl_sync(0xffffffffu, incl, 31);
+    }
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(s_count, total);
+    uint32_t pos = __shfl_sync(0xffffffffu, base, 0) + excl;
+    while (msk) {
+      const uint32_t j = (uint32_t)__ffs(msk) - 1u;
+      msk &= msk - 1u;
+      if ((int64_t)pos < a.seg_cap) {
+        const int64_t slot = (int64_t)blockIdx.x * a.seg_cap + pos;
+        Cand cd;
+        cd.p = (int32_t)row;
+        cd.g = (int32_t)(g0 + gi * 32 + (int)j);
+        a.cand[slot] = cd;
+        a.cand_e[slot] = pick32(v, j);
+      }
+      ++pos;
+    }
+  }
+}
 
 enum : int { kErrProducer = 1, kErrMma = 2, kErrEpilogue = 4, kErrDrain = 8 };
 
-template <int NH>
+// BF: BF16 operands (64 values per 128-byte row) instead of TF32 (32 values).
+// K-steps that lie wholly in the zero padding beyond the 2K real columns are skipped.
+template <int NH, bool BF>
 __global__ void __launch_bounds__(kThreads, 1)
     dist_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs a) {
+  constexpr int kEl = BF ? 64 : 32;  // values per chunk (one swizzled row)
+  const int twoK = 2 * a.K;
   using C = Cfg<NH>;
   constexpr int S = C::kStages;
   extern __shared__ uint8_t smem_raw[];
@@ -94,7 +201,6 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint32_t* s_count = tslot + 1;
   uint32_t* s_abort = tslot + 2;
   float* Ys = (float*)(smem + C::kTileBytes + 256);
-  float* Cs = Ys + BN;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -144,10 +250,10 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint32_t st = smem_base + stage * C::kStageBytes;
 #pragma unroll
           for (int h = 0; h < NH; ++h)
-            tma_load(st + h * kABytes, &tmA, &full[stage], h * a.KA + c * BK, m * BM);
+            tma_load(st + h * kABytes, &tmA, &full[stage], h * a.KA + c * kEl, m * BM);
 #pragma unroll
           for (int h = 0; h < NH; ++h)
-            tma_load(st + NH * kABytes + h * kBBytes, &tmB, &full[stage], h * a.KA + c * BK, n * BN);
+            tma_load(st + NH * kABytes + h * kBBytes, &tmB, &full[stage], h * a.KA + c * kEl, n * BN);
           issued |= 1u << stage;
           issued_par = (issued_par & ~(1u << stage)) | (phase << stage);
           if (++stage == S) {
@@ -186,13 +292,14 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint32_t st = smem_base + stage * C::kStageBytes;
           const uint64_t a0 = sw128_desc(st), b0 = sw128_desc(st + NH * kABytes);
 #pragma unroll
-          for (int kk = 0; kk < BK / 8; ++kk) {
-            const uint64_t adv = (uint64_t)(kk * 32) >> 4;  // 8 TF32 = 32 bytes along K
-            mma_tf32(d_tmem, a0 + adv, b0 + adv, (c | kk) != 0);
+          for (int kk = 0; kk < 4; ++kk) {
+            if (c * kEl + kk * (kEl / 4) >= twoK) break;  // zero padding: nothing to add
+            const uint64_t adv = (uint64_t)(kk * 32) >> 4;  // 32 bytes along K
+            mma_step<BF>(d_tmem, a0 + adv, b0 + adv, (c | kk) != 0);
             if (NH == 2) {
               const uint64_t a1 = sw128_desc(st + kABytes), b1 = sw128_desc(st + NH * kABytes + kBBytes);
-              mma_tf32(d_tmem, a0 + adv, b1 + adv, 1u);  // hi x lo
-              mma_tf32(d_tmem, a1 + adv, b0 + adv, 1u);  // lo x hi
+              mma_step<BF>(d_tmem, a0 + adv, b1 + adv, 1u);  // hi x lo
+              mma_step<BF>(d_tmem, a1 + adv, b0 + adv, 1u);  // lo x hi
             }
           }
           mma_commit(&empty[stage]);  // stage reusable once these MMAs have read it
@@ -212,21 +319,19 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (!mbar_wait(drain, 0)) atomicOr(a.err, kErrDrain);
     }
   } else {
-    // ---------------- epilogue: warps 2..9; TMEM lane quarter = warp % 4,
-    // columns [128 h, 128 h + 128) with h = (warp - 2) / 4
+    // ---------------- epilogue: warps 2.. ; TMEM lane quarter = warp % 4,
+    // kEpiGroups 32-column groups from column 32 kEpiGroups part
     const int et = threadIdx.x - 64;
     const int q = warp & 3;
-    const int half = (warp - 2) >> 2;
-    const float invK = 1.0f / (float)a.K;
+    const int part = (warp - 2) >> 2;
     int acc = 0;
     uint32_t acc_phase = 0;
     for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
       const int m = t / a.nN, n = t - (t / a.nN) * a.nN;
-      epi_bar();  // readers of the previous tile's Y / c are done
+      epi_bar();  // readers of the previous tile's Y are done
       for (int j = et; j < BN; j += kEpiThreads) {
         const int64_t g = (int64_t)n * BN + j;
         Ys[j] = g < a.G ? a.Y[g] : -INFINITY;
-        Cs[j] = g < a.G ? a.cg[g] : 0.0f;
       }
       const bool got = mbar_wait(&tfull[acc], acc_phase);
       if (!got) atomicOr(s_abort, 1u);
@@ -237,63 +342,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       tc_fence_after();
       const int64_t row = (int64_t)m * BM + q * 32 + lane;
-      const bool valid = row < a.P;
-      const uint32_t lane_addr = tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN);
-#pragma unroll 1
-      for (int c4 = 0; c4 < BN / 64; ++c4) {
-        const int cc = half * (BN / 64) + c4;
-        __syncwarp();
-        uint32_t v[32];
-        tmem_ld32(lane_addr + (uint32_t)(cc * 32), v);
-        // fast test: min_j (v_j - Y_j) <= 0 iff some v_j <= Y_j (NaN terms drop out)
-        const float4* Y4 = reinterpret_cast<const float4*>(Ys + cc * 32);
-        float dm[8];
-#pragma unroll
-        for (int j4 = 0; j4 < 8; ++j4) {
-          const float4 y = Y4[j4];
-          dm[j4] = fminf(fminf(__uint_as_float(v[4 * j4 + 0]) - y.x, __uint_as_float(v[4 * j4 + 1]) - y.y),
-                         fminf(__uint_as_float(v[4 * j4 + 2]) - y.z, __uint_as_float(v[4 * j4 + 3]) - y.w));
-        }
-        const float dmin = fminf(fminf(fminf(dm[0], dm[1]), fminf(dm[2], dm[3])),
-                                 fminf(fminf(dm[4], dm[5]), fminf(dm[6], dm[7])));
-        const bool has = valid && dmin <= 0.0f;
-        if (__ballot_sync(0xffffffffu, has) == 0u) continue;
-        // exact test, one atomic per warp, then the candidates of this lane
-        uint32_t msk = 0;
-        if (has) {
-#pragma unroll
-          for (int j = 0; j < 32; ++j) msk |= (uint32_t)(__uint_as_float(v[j]) <= Ys[cc * 32 + j]) << j;
-        }
-        const uint32_t cnt = __popc(msk);
-        uint32_t incl = cnt;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-          if (lane >= o) incl += y;
-        }
-        uint32_t base = 0;
-        if (lane == 31) base = atomicAdd(s_count, incl);
-        base = __shfl_sync(0xffffffffu, base, 31);
-        if (msk) {
-          float vv[32];  // indexed by candidate column below
-#pragma unroll
-          for (int j = 0; j < 32; ++j) vv[j] = __uint_as_float(v[j]);
-          uint32_t pos = base + incl - cnt;
-          while (msk) {
-            const int j = __ffs(msk) - 1;
-            msk &= msk - 1;
-            if ((int64_t)pos < a.seg_cap) {
-              const int64_t slot = (int64_t)blockIdx.x * a.seg_cap + pos;
-              Cand cd;
-              cd.p = (int32_t)row;
-              cd.g = (int32_t)((int64_t)n * BN + cc * 32 + j);
-              a.cand[slot] = cd;
-              a.cand_e[slot] = fminf((vv[j] + Cs[cc * 32 + j]) * invK, 10.0f);
-            }
-            ++pos;
-          }
-        }
-      }
+      const int col0 = part * kEpiGroups * 32;
+      epi_warp<kEpiGroups>(tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + col0), Ys + col0, row,
+                           row < a.P, (int64_t)n * BN + col0, s_count, a, lane);
       tc_fence_before();
       mbar_arrive(&tempty[acc]);
       if (++acc == 2) {
@@ -329,7 +380,7 @@ constexpr int kResMaxStages = 4;
 constexpr uint32_t kResSmemMax = 227u * 1024u;  // dynamic shared memory of one CTA
 
 __host__ __device__ constexpr uint32_t res_smem(int n_chunks, int stages) {
-  return 1024u + (uint32_t)n_chunks * kBBytes + (uint32_t)stages * kABytes + 256u + 2u * BN * 4u;
+  return 1024u + (uint32_t)n_chunks * kBBytes + (uint32_t)stages * kABytes + 256u + BN * 4u;
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
@@ -350,7 +401,6 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint32_t* s_count = tslot + 1;
   uint32_t* s_abort = tslot + 2;
   float* Ys = (float*)((uint8_t*)full + 256);
-  float* Cs = Ys + BN;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -457,6 +507,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint64_t b0 = sw128_desc(b_base + (uint32_t)c * kBBytes);
 #pragma unroll
             for (int kk = 0; kk < BK / 8; ++kk) {
+              if (c * BK + kk * 8 >= 2 * a.K) break;  // zero padding: nothing to add
               const uint64_t adv = (uint64_t)(kk * 32) >> 4;  // 8 TF32 = 32 bytes along K
               mma_tf32(d_tmem, a0 + adv, b0 + adv, (c | kk) != 0);
             }
@@ -482,19 +533,17 @@ __global__ void __launch_bounds__(kThreads, 1)
     // ---------------- epilogue (as in dist_tc_kernel)
     const int et = threadIdx.x - 64;
     const int q = warp & 3;
-    const int half = (warp - 2) >> 2;
-    const float invK = 1.0f / (float)a.K;
+    const int part = (warp - 2) >> 2;
     int acc = 0;
     uint32_t acc_phase = 0;
     bool stop = false;
     for (int as = blockIdx.x; as < n_assign && !stop; as += gridDim.x) {
       const int n = as % a.nN, j = as / a.nN;
       for (int m = j; m < a.nM; m += cpt) {
-        epi_bar();  // readers of the previous tile's Y / c are done
+        epi_bar();  // readers of the previous tile's Y are done
         for (int jj = et; jj < BN; jj += kEpiThreads) {
           const int64_t g = (int64_t)n * BN + jj;
           Ys[jj] = g < a.G ? a.Y[g] : -INFINITY;
-          Cs[jj] = g < a.G ? a.cg[g] : 0.0f;
         }
         const bool got = mbar_wait(&tfull[acc], acc_phase);
         if (!got) atomicOr(s_abort, 1u);
@@ -506,61 +555,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         tc_fence_after();
         const int64_t row = (int64_t)m * BM + q * 32 + lane;
-        const bool valid = row < a.P;
-        const uint32_t lane_addr = tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN);
-#pragma unroll 1
-        for (int c4 = 0; c4 < BN / 64; ++c4) {
-          const int cc = half * (BN / 64) + c4;
-          __syncwarp();
-          uint32_t v[32];
-          tmem_ld32(lane_addr + (uint32_t)(cc * 32), v);
-          const float4* Y4 = reinterpret_cast<const float4*>(Ys + cc * 32);
-          float dm[8];
-#pragma unroll
-          for (int j4 = 0; j4 < 8; ++j4) {
-            const float4 y = Y4[j4];
-            dm[j4] = fminf(fminf(__uint_as_float(v[4 * j4 + 0]) - y.x, __uint_as_float(v[4 * j4 + 1]) - y.y),
-                           fminf(__uint_as_float(v[4 * j4 + 2]) - y.z, __uint_as_float(v[4 * j4 + 3]) - y.w));
-          }
-          const float dmin = fminf(fminf(fminf(dm[0], dm[1]), fminf(dm[2], dm[3])),
-                                   fminf(fminf(dm[4], dm[5]), fminf(dm[6], dm[7])));
-          const bool has = valid && dmin <= 0.0f;
-          if (__ballot_sync(0xffffffffu, has) == 0u) continue;
-          uint32_t msk = 0;
-          if (has) {
-#pragma unroll
-            for (int jb = 0; jb < 32; ++jb) msk |= (uint32_t)(__uint_as_float(v[jb]) <= Ys[cc * 32 + jb]) << jb;
-          }
-          const uint32_t cnt = __popc(msk);
-          uint32_t incl = cnt;
-#pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
-          }
-          uint32_t base = 0;
-          if (lane == 31) base = atomicAdd(s_count, incl);
-          base = __shfl_sync(0xffffffffu, base, 31);
-          if (msk) {
-            float vv[32];
-#pragma unroll
-            for (int jb = 0; jb < 32; ++jb) vv[jb] = __uint_as_float(v[jb]);
-            uint32_t pos = base + incl - cnt;
-            while (msk) {
-              const int jb = __ffs(msk) - 1;
-              msk &= msk - 1;
-              if ((int64_t)pos < a.seg_cap) {
-                const int64_t slot = (int64_t)blockIdx.x * a.seg_cap + pos;
-                Cand cd;
-                cd.p = (int32_t)row;
-                cd.g = (int32_t)((int64_t)n * BN + cc * 32 + jb);
-                a.cand[slot] = cd;
-                a.cand_e[slot] = fminf((vv[jb] + Cs[cc * 32 + jb]) * invK, 10.0f);
-              }
-              ++pos;
-            }
-          }
-        }
+        const int col0 = part * kEpiGroups * 32;
+        epi_warp<kEpiGroups>(tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + col0), Ys + col0, row,
+                             row < a.P, (int64_t)n * BN + col0, s_count, a, lane);
         tc_fence_before();
         mbar_arrive(&tempty[acc]);
         if (++acc == 2) {
@@ -597,6 +594,8 @@ __device__ __forceinline__ void split_tf32(double x, float& hi, float& lo) {
   lo = (hi == hi && fabs(hi) < INFINITY) ? tf32_rn((float)r) : 0.0f;
 }
 
+
+
 // flags[0]: bit 0 = an operand is infinite in FP32; flags[1] / flags[2] = the
 // largest w and the largest s^2 (FP32 bit patterns of non-negative values,
 // ordered like unsigned integers), so the host can check that no w s^2 product
@@ -611,6 +610,34 @@ __device__ __forceinline__ void split_tf32f(float x, float& hi, float& lo) {
   lo = fabsf(hi) < INFINITY ? tf32_rn(x - hi) : 0.0f;
 }
 
+// hi/lo BF16 parts (as the FP32 values they represent exactly)
+__device__ __forceinline__ float bf16_rn(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+__device__ __forceinline__ void split_bf16(double x, float& hi, float& lo) {
+  hi = bf16_rn((float)x);
+  const double r = x - (double)hi;
+  lo = (hi == hi && fabs(hi) < INFINITY) ? bf16_rn((float)r) : 0.0f;
+}
+__device__ __forceinline__ void split_bf16f(float x, float& hi, float& lo) {
+  hi = bf16_rn(x);
+  lo = (hi == hi && fabsf(hi) < INFINITY) ? bf16_rn(x - hi) : 0.0f;  // x - hi is exact in FP32
+}
+
+// operand element i of the pass's type: TF32 values as FP32, or BF16
+template <bool BF>
+__device__ __forceinline__ void put_op(void* base, int64_t i, float v) {
+  if (BF)
+    ((__nv_bfloat16*)base)[i] = __float2bfloat16_rn(v);  // v is a BF16 value: exact
+  else
+    ((float*)base)[i] = v;
+}
+template <bool BF>
+__device__ __forceinline__ void split_opf(float x, float& hi, float& lo) {
+  if (BF)
+    split_bf16f(x, hi, lo);
+  else
+    split_tf32f(x, hi, lo);
+}
+
 // A rows: [s (K) | s^2 (K) | 0 ...] per half, in FP32 (s rounded once from FP64,
 // s^2 = fl(s s): both within 2^-23 relative, inside the bound's rounding terms).
 // One warp per row, rows strided over the grid; the overflow monitors are
@@ -621,7 +648,8 @@ __device__ __forceinline__ void split_tf32f(float x, float& hi, float& lo) {
 // flight per SM to stream at full rate).
 constexpr int kPrepLoads = 16;
 
-__global__ void tc_prep_rows_kernel(const double* stats, int64_t P, int K, int KA, int NH, float* A,
+template <bool BF>
+__global__ void tc_prep_rows_kernel(const double* stats, int64_t P, int K, int KA, int NH, void* A,
                                     unsigned* flags) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -632,18 +660,18 @@ __global__ void tc_prep_rows_kernel(const double* stats, int64_t P, int K, int K
     const int rows = P - p0 < R ? (int)(P - p0) : R;
     if (K > 32 * kPrepLoads) {  // very wide rows: one row at a time
       const double* srow = stats + p0 * K;
-      float* arow = A + p0 * ld;
+      const int64_t arow = p0 * ld;
       for (int k = lane; k < K; k += 32) {
         const float sv = rn32_bits(srow[k]);
         const float s2 = sv * sv;
         float h1, l1, h2, l2;
-        split_tf32f(sv, h1, l1);
-        split_tf32f(s2, h2, l2);
-        arow[k] = h1;
-        arow[K + k] = h2;
+        split_opf<BF>(sv, h1, l1);
+        split_opf<BF>(s2, h2, l2);
+        put_op<BF>(A, arow + k, h1);
+        put_op<BF>(A, arow + K + k, h2);
         if (NH == 2) {
-          arow[KA + k] = l1;
-          arow[KA + K + k] = l2;
+          put_op<BF>(A, arow + KA + k, l1);
+          put_op<BF>(A, arow + KA + K + k, l2);
         }
         if (fabsf(sv) == INFINITY || fabsf(s2) == INFINITY) inf = 1u;
         if (s2 == s2) mx = max(mx, __float_as_uint(s2));
@@ -667,14 +695,14 @@ __global__ void tc_prep_rows_kernel(const double* stats, int64_t P, int K, int K
           const float sv = rn32_bits(v[t]);
           const float s2 = sv * sv;
           float h1, l1, h2, l2;
-          split_tf32f(sv, h1, l1);
-          split_tf32f(s2, h2, l2);
-          float* arow = A + (p0 + r) * ld;
-          arow[k] = h1;
-          arow[K + k] = h2;
+          split_opf<BF>(sv, h1, l1);
+          split_opf<BF>(s2, h2, l2);
+          const int64_t arow = (p0 + r) * ld;
+          put_op<BF>(A, arow + k, h1);
+          put_op<BF>(A, arow + K + k, h2);
           if (NH == 2) {
-            arow[KA + k] = l1;
-            arow[KA + K + k] = l2;
+            put_op<BF>(A, arow + KA + k, l1);
+            put_op<BF>(A, arow + KA + K + k, l2);
           }
           if (fabsf(sv) == INFINITY || fabsf(s2) == INFINITY) inf = 1u;
           if (s2 == s2) mx = max(mx, __float_as_uint(s2));
@@ -687,10 +715,10 @@ __global__ void tc_prep_rows_kernel(const double* stats, int64_t P, int K, int K
       }
     }
     for (int rr = 0; rr < rows; ++rr) {
-      float* arow = A + (p0 + rr) * ld;
+      const int64_t arow = (p0 + rr) * ld;
       for (int k = 2 * K + lane; k < KA; k += 32) {
-        arow[k] = 0.0f;
-        if (NH == 2) arow[KA + k] = 0.0f;
+        put_op<BF>(A, arow + k, 0.0f);
+        if (NH == 2) put_op<BF>(A, arow + KA + k, 0.0f);
       }
     }
   }
@@ -704,8 +732,9 @@ __global__ void tc_prep_rows_kernel(const double* stats, int64_t P, int K, int K
 
 // B rows: [-2 w d (K) | w (K) | 0 ...] per half; c_g = sum_k w d^2 in FP64; the
 // per-gene term of the error bound b0_g = 5 beta c_g / K.
+template <bool BF>
 __global__ void tc_prep_genes_kernel(const double* data, const double* se, int64_t G, int K, int KA, int NH,
-                                     double beta, float* B, double* cg64, float* cg32, float* b0, unsigned* flags) {
+                                     double beta, void* B, double* cg64, float* cg32, float* b0, unsigned* flags) {
   const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= G) return;
   const int64_t ld = (int64_t)NH * KA;
@@ -725,9 +754,12 @@ __global__ void tc_prep_genes_kernel(const double* data, const double* se, int64
       else c += w * d * d;
     }
     float hi, lo;
-    split_tf32(v, hi, lo);
-    B[g * ld + k] = hi;
-    if (NH == 2) B[g * ld + KA + k] = lo;
+    if (BF)
+      split_bf16(v, hi, lo);
+    else
+      split_tf32(v, hi, lo);
+    put_op<BF>(B, g * ld + k, hi);
+    if (NH == 2) put_op<BF>(B, g * ld + KA + k, lo);
   }
   if (bad) atomicOr(&flags[0], 1u);
   cg64[g] = c;
@@ -752,7 +784,7 @@ __global__ void tc_y_kernel(const float* X, const double* cg64, int64_t G, int K
 
 // Concatenate the per-CTA segments: out[off_b + i] = seg_b[i].
 __global__ void tc_gather_kernel(const Cand* seg, const float* seg_e, const unsigned* count, int n_seg,
-                                 int64_t seg_cap, Cand* out, float* out_e) {
+                                 int64_t seg_cap, const float* cg, float invK, Cand* out, float* out_e) {
   __shared__ int64_t off;
   const int b = blockIdx.x;
   if (threadIdx.x == 0) {
@@ -763,12 +795,15 @@ __global__ void tc_gather_kernel(const Cand* seg, const float* seg_e, const unsi
   __syncthreads();
   const int64_t n = count[b];
   for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
-    out[off + i] = seg[(int64_t)b * seg_cap + i];
-    out_e[off + i] = seg_e[(int64_t)b * seg_cap + i];
+    const Cand cd = seg[(int64_t)b * seg_cap + i];
+    out[off + i] = cd;
+    out_e[off + i] = fminf((seg_e[(int64_t)b * seg_cap + i] + cg[cd.g]) * invK, 10.0f);
   }
 }
 
-bool make_map(CUtensorMap* map, const float* base, int64_t rows, int64_t cols, int box_rows) {
+// rows x cols row-major operand, 128-byte swizzled boxes of box_rows x (one
+// 128-byte row: 32 FP32 / TF32 values, or 64 BF16 values when bf16)
+bool make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t cols, int box_rows, bool bf16 = false) {
   static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
   if (!encode) {
     void* fn = nullptr;
@@ -781,29 +816,34 @@ bool make_map(CUtensorMap* map, const float* base, int64_t rows, int64_t cols, i
   }
   memset(map, 0, sizeof(*map));
   cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)cols * 4};
-  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  const int es = bf16 ? 2 : 4;
+  cuuint64_t strides[1] = {(cuuint64_t)cols * es};
+  cuuint32_t box[2] = {(cuuint32_t)(128 / es), (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
-  return encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, estr,
+  return encode(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base,
+                dims, strides, box, estr,
                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <int NH>
-cudaError_t launch_nh(const float* A, const float* B, const TcArgs& args, int grid, cudaStream_t s) {
+template <int NH, bool BF>
+cudaError_t launch_nh(const void* A, const void* B, const TcArgs& args, int grid, cudaStream_t s) {
   static std::atomic<uint64_t> attr{0};  // devices where the limit is set, shared by all contexts
-  cudaError_t e = set_smem_once(attr, dist_tc_kernel<NH>, (int)Cfg<NH>::kSmem);
+  cudaError_t e = set_smem_once(attr, dist_tc_kernel<NH, BF>, (int)Cfg<NH>::kSmem);
   if (e != cudaSuccess) return e;
   CUtensorMap ma, mb;
   const int64_t ld = (int64_t)NH * args.KA;
-  if (!make_map(&ma, A, args.P, ld, BM) || !make_map(&mb, B, args.G, ld, BN)) return cudaErrorInvalidValue;
-  dist_tc_kernel<NH><<<grid, kThreads, Cfg<NH>::kSmem, s>>>(ma, mb, args);
+  if (!make_map(&ma, A, args.P, ld, BM, BF) || !make_map(&mb, B, args.G, ld, BN, BF)) return cudaErrorInvalidValue;
+  dist_tc_kernel<NH, BF><<<grid, kThreads, Cfg<NH>::kSmem, s>>>(ma, mb, args);
   return cudaGetLastError();
 }
 
 }  // namespace
 
-int tc_ka(int K) { return ((2 * K + BK - 1) / BK) * BK; }
+int tc_ka(int K, int mode) {
+  const int el = mode == 3 ? 64 : BK;  // values per 128-byte row
+  return ((2 * K + el - 1) / el) * el;
+}
 
 double tc_beta(int K, int nh) {
   // |K e32 - K e| <= beta * sum_k |term_k| with sum_k |term_k| <= 5 c_g + 4 K e:
@@ -813,25 +853,42 @@ double tc_beta(int K, int nh) {
   //   three terms: representation error of hi + lo <= 2^-21 per operand, the
   //     dropped lo*lo <= 2^-22, 6K accumulations.
   // Plus the final FP32 rounding of Y / e, with a 10 % safety factor.
+  //   BF16 three terms (nh = 3): hi = RN_bf16(x), lo = RN_bf16(x - hi) leave
+  //     |x - hi - lo| <= 2^-9 |x - hi| <= 2^-18 |x|, plus <= 2^-22 from the
+  //     FP64 -> FP32 steps, per operand; the dropped lo*lo <= 2^-18; BF16 x BF16
+  //     products are exact in FP32; 6K accumulations.
   const double u23 = 1.1920928955078125e-07;
   double b;
   if (nh == 1)
     b = (std::pow(1.0 + 4.8828125e-04 + 5.960464477539063e-08, 2) - 1.0) + (2.0 * K + 4) * u23;
+  else if (nh == 3)
+    b = 2.0 * (3.814697265625e-06 + 2.384185791015625e-07) + 3.814697265625e-06 + (6.0 * K + 4) * u23;
   else
     b = 2.0 * 4.76837158203125e-07 + 2.384185791015625e-07 + (6.0 * K + 4) * u23;
   return 1.1 * b;
 }
 
-cudaError_t launch_tc_prep(const DistInputs& in, int nh, double beta, float* A, float* B, double* cg64, float* cg32,
+cudaError_t launch_tc_prep(const DistInputs& in, int mode, double beta, void* A, void* B, double* cg64, float* cg32,
                            float* b0, unsigned* flags, cudaStream_t s) {
-  const int KA = tc_ka(in.K);
+  const int KA = tc_ka(in.K, mode);
+  const int NH = mode == 1 ? 1 : 2;
+  const bool bf = mode == 3;
   if (in.P > 0) {
     const int64_t blocks = (in.P + 31) / 32 < 8192 ? (in.P + 31) / 32 : 8192;
-    tc_prep_rows_kernel<<<(unsigned)blocks, 256, 0, s>>>(in.stats, in.P, in.K, KA, nh, A, flags);
+    if (bf)
+      tc_prep_rows_kernel<true><<<(unsigned)blocks, 256, 0, s>>>(in.stats, in.P, in.K, KA, NH, A, flags);
+    else
+      tc_prep_rows_kernel<false><<<(unsigned)blocks, 256, 0, s>>>(in.stats, in.P, in.K, KA, NH, A, flags);
   }
-  if (in.G > 0)
-    tc_prep_genes_kernel<<<(unsigned)((in.G + 127) / 128), 128, 0, s>>>(in.data, in.se, in.G, in.K, KA, nh, beta,
-                                                                        B, cg64, cg32, b0, flags);
+  if (in.G > 0) {
+    const unsigned gb = (unsigned)((in.G + 127) / 128);
+    if (bf)
+      tc_prep_genes_kernel<true><<<gb, 128, 0, s>>>(in.data, in.se, in.G, in.K, KA, NH, beta, B, cg64, cg32, b0,
+                                                    flags);
+    else
+      tc_prep_genes_kernel<false><<<gb, 128, 0, s>>>(in.data, in.se, in.G, in.K, KA, NH, beta, B, cg64, cg32, b0,
+                                                     flags);
+  }
   return cudaGetLastError();
 }
 
@@ -846,7 +903,7 @@ int tc_grid(int64_t P, int64_t G, int sms) {
   return (int)(tiles < sms ? tiles : sms);
 }
 
-static cudaError_t launch_res(const float* A, const float* B, const TcArgs& args, int grid, int stages,
+static cudaError_t launch_res(const void* A, const void* B, const TcArgs& args, int grid, int stages,
                               cudaStream_t s) {
   const uint32_t smem = res_smem(args.n_chunks, stages);
   static std::atomic<uint64_t> attr{0};
@@ -865,17 +922,18 @@ int tc_res_stages(int n_chunks) {
   return 0;
 }
 
-cudaError_t launch_dist_tc(int nh, const float* A, const float* B, const TcArgs& args, int grid, cudaStream_t s) {
+cudaError_t launch_dist_tc(int nh, const void* A, const void* B, const TcArgs& args, int grid, cudaStream_t s) {
   if (args.P <= 0 || args.G <= 0) return cudaSuccess;
-  if (nh == 2) return launch_nh<2>(A, B, args, grid, s);
+  if (nh == 3) return launch_nh<2, true>(A, B, args, grid, s);
+  if (nh == 2) return launch_nh<2, false>(A, B, args, grid, s);
   const int stages = tc_res_stages(args.n_chunks);
-  return stages ? launch_res(A, B, args, grid, stages, s) : launch_nh<1>(A, B, args, grid, s);
+  return stages ? launch_res(A, B, args, grid, stages, s) : launch_nh<1, false>(A, B, args, grid, s);
 }
 
 cudaError_t launch_tc_gather(const Cand* seg, const float* seg_e, const unsigned* count, int n_seg, int64_t seg_cap,
-                             Cand* out, float* out_e, cudaStream_t s) {
+                             const float* cg, int K, Cand* out, float* out_e, cudaStream_t s) {
   if (n_seg <= 0) return cudaSuccess;
-  tc_gather_kernel<<<n_seg, 256, 0, s>>>(seg, seg_e, count, n_seg, seg_cap, out, out_e);
+  tc_gather_kernel<<<n_seg, 256, 0, s>>>(seg, seg_e, count, n_seg, seg_cap, cg, 1.0f / (float)K, out, out_e);
   return cudaGetLastError();
 }
 

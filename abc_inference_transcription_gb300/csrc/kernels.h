@@ -73,24 +73,27 @@ struct TcArgs {
   int64_t P, G;
   int K, KA, n_chunks, nM, nN;
   const float* Y;       // per gene: K X_g - c_g rounded up (candidate iff acc <= Y_g)
-  const float* cg;      // per gene c_g in FP32 (for the reported FP32 error)
   Cand* cand;           // per-CTA segments of seg_cap entries
-  float* cand_e;        // FP32 error of each candidate
+  float* cand_e;        // raw accumulator of each candidate (K err - c_g)
   int64_t seg_cap;
   unsigned* seg_count;  // per CTA: candidates found (may exceed seg_cap)
   int* err;             // nonzero: a bounded wait ran out
 };
-int tc_ka(int K);
+// operand row length (values per half) of candidate-pass mode 1, 2 (TF32) or 3 (BF16)
+int tc_ka(int K, int mode = 2);
 // relative error factor beta: |e32 - e| <= beta (5 c_g / K + 4 e)
 double tc_beta(int K, int nh);
 int tc_grid(int64_t P, int64_t G, int sms);
 // flags[0] bit 0: an operand is infinite in FP32; flags[1], flags[2]: max w, max s^2 (FP32 bits)
-cudaError_t launch_tc_prep(const DistInputs& in, int nh, double beta, float* A, float* B, double* cg64, float* cg32,
+cudaError_t launch_tc_prep(const DistInputs& in, int mode, double beta, void* A, void* B, double* cg64, float* cg32,
                            float* b0, unsigned* flags, cudaStream_t s);
 cudaError_t launch_tc_y(const float* X, const double* cg64, int64_t G, int K, float* Y, cudaStream_t s);
-cudaError_t launch_dist_tc(int nh, const float* A, const float* B, const TcArgs& args, int grid, cudaStream_t s);
+// mode 1: TF32 one term, 2: TF32 hi/lo three terms, 3: BF16 hi/lo three terms
+cudaError_t launch_dist_tc(int mode, const void* A, const void* B, const TcArgs& args, int grid, cudaStream_t s);
+// concatenates the per-CTA segments; seg_e holds raw accumulators, out_e the
+// clipped FP32 errors min((acc + c_g) / K, 10)
 cudaError_t launch_tc_gather(const Cand* seg, const float* seg_e, const unsigned* count, int n_seg, int64_t seg_cap,
-                             Cand* out, float* out_e, cudaStream_t s);
+                             const float* cg, int K, Cand* out, float* out_e, cudaStream_t s);
 
 // per (g,k): sw = sqrt(w), dw = sqrt(w) d in FP32, w = 1/((se^2 + 0.01 d^2) + eps)
 // and s32[r][k] = stats[r stride][k] in FP32 for r < s32_rows (s32 may be null)

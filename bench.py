@@ -223,11 +223,12 @@ def distance_bench(P: int, G: int, K: int, q: float, seed: int, cpu_seconds: flo
     ctx = Context(make_config("hour"), None)
     try:
         ctx.profile(True)
-        # both tensor-core candidate passes on the same selection (indices only):
-        # one term (TF32 hi, gene rows resident in shared memory) and three terms (hi/lo splits)
+        # the tensor-core candidate passes on the same selection (indices only):
+        # one term (TF32 hi, gene rows resident in shared memory), three terms
+        # with TF32 hi/lo splits, three terms with BF16 hi/lo splits
         per_mode = {}
         default_mode = ctx.distance_mode()[0]
-        for dm_try in (1, 2):
+        for dm_try in (1, 2, 3):
             ctx.set_distance_mode(dm_try)
             ctx.select_device(data, se, stats.data_ptr(), min(P, 200000), 1, q)  # warm-up
             torch.cuda.synchronize()
@@ -241,8 +242,8 @@ def distance_bench(P: int, G: int, K: int, q: float, seed: int, cpu_seconds: flo
                                 "candidate_passes": f_pass, "candidates": c_m, "fp64_rechecked": r_m,
                                 "algorithmic_tflops": 2.0 * P * G * 2 * K / (f_ms / max(f_pass, 1) / 1e3) / 1e12,
                                 "_lists": (o_m, i_m)}
-        same_lists = bool(np.array_equal(per_mode[1]["_lists"][0], per_mode[2]["_lists"][0]) and
-                          np.array_equal(per_mode[1]["_lists"][1], per_mode[2]["_lists"][1]))
+        same_lists = all(np.array_equal(per_mode[1]["_lists"][0], per_mode[m]["_lists"][0]) and
+                         np.array_equal(per_mode[1]["_lists"][1], per_mode[m]["_lists"][1]) for m in (2, 3))
         for v in per_mode.values():
             del v["_lists"]
         ctx.set_distance_mode(default_mode)
@@ -343,23 +344,27 @@ def distance_bench(P: int, G: int, K: int, q: float, seed: int, cpu_seconds: flo
            "distance_mode": mode_used, "downstream": down,
            "fp64_error_path": {"seconds": dt_e, "pairs_per_s": P * G / dt_e, "accepted": int(off_e[-1])},
            "candidate_pass_modes": {"one_term_tf32_resident_genes": per_mode[1], "three_term_tf32": per_mode[2],
+                                    "three_term_bf16": per_mode[3],
                                     "identical_accepted_lists": same_lists},
            "oracle_check": oracle_chk}
     kernel_ms = fast_ms / max(passes, 1)
     pk, src = load_peaks()
     algo = 2.0 * P * G * (2 * K)  # one multiply-add per (particle, gene, operand column) of [s | s^2]
-    if mode_used in (1, 2):
-        # tcgen05 TF32 MMAs issued per pass: 128 x 256 tiles, depth KA per term, 1 or 3 terms
-        ka = -(-2 * K // 32) * 32
+    if mode_used in (1, 2, 3):
+        # tcgen05 MMAs issued per pass: 128 x 256 tiles, depth KA per term, 1 or 3 terms
+        # (TF32 for modes 1-2, KA a multiple of 32; BF16 for mode 3, KA a multiple of 64)
+        el = 64 if mode_used == 3 else 32
+        ka = -(-2 * K // el) * el
         tiles = -(-P // 128) * -(-G // 256)
-        terms = 3 if mode_used == 2 else 1
+        terms = 1 if mode_used == 1 else 3
         issued = 2.0 * 128 * 256 * ka * terms * tiles
+        mma_kind, rate = ("BF16", "which run at") if mode_used == 3 else ("TF32", "which run at half")
         peak = float(pk.get("bf16_tflops", 1900.0)) * 1e12
         out["roofline"] = {"bound": "tensor", "achieved": algo / (kernel_ms / 1e3) / 1e12, "peak": peak / 1e12,
                            "unit": "TFLOP/s", "frac": algo / (kernel_ms / 1e3) / peak, "traffic": None,
                            "basis": f"algorithmic flops 2 P G (2K) per candidate pass over its kernel time, against "
-                                    f"the {src} dense BF16 GEMM rate; the pass issues TF32 MMAs ({terms} term(s), "
-                                    f"128 x 256 tiles, depth {ka}), which run at half that rate",
+                                    f"the {src} dense BF16 GEMM rate; the pass issues {mma_kind} MMAs ({terms} term(s), "
+                                    f"128 x 256 tiles, depth {ka}), {rate} that rate",
                            "kernel_ms_per_pass": kernel_ms,
                            "issued_mma_tflops": issued / (kernel_ms / 1e3) / 1e12}
     else:

@@ -17,7 +17,7 @@ from abc_inference_transcription_gb300.config import REF_FAMILIES, make_config
 pytestmark = pytest.mark.gpu
 
 GOLDEN = __file__.rsplit("/", 1)[0] + "/golden"
-MODES = (0, 1, 2)
+MODES = (0, 1, 2, 3)
 
 
 @pytest.fixture(scope="module")
@@ -111,7 +111,7 @@ def test_infinite_statistic_falls_back_to_fp32_pass(Ctx, orc):
     assert np.array_equal(off, roff) and np.array_equal(idx, ridx)
 
 
-@pytest.mark.parametrize("mode", (1, 2))
+@pytest.mark.parametrize("mode", (1, 2, 3))
 def test_many_tiles_topq_and_segment_growth(Ctx, orc, mode):
     """391 particle tiles x 3 gene tiles: persistent CTAs loop over several
     tiles (both tensor-memory accumulators wrap), and the dense candidate

@@ -10,7 +10,7 @@ from abc_inference_transcription_gb300.config import (beta_moments, make_config,
                                                       synthetic_cells)
 
 pytestmark = pytest.mark.gpu
-MODES = (0, 1, 2)
+MODES = (0, 1, 2, 3)
 
 
 @pytest.fixture(scope="module")
@@ -119,7 +119,7 @@ def test_data_stats_silent_and_minimal_cells(Ctx, orc):
 
 
 @pytest.mark.parametrize("errors", (True, False))
-@pytest.mark.parametrize("mode", (0, 2))
+@pytest.mark.parametrize("mode", (0, 2, 3))
 def test_selection_sort_paths_and_ties(Ctx, orc, mode, errors):
     """Per-gene lists of every sort size class (one entry per thread up to
     1,024 entries, 2, 4 and 8 per thread, and the global-memory network above
