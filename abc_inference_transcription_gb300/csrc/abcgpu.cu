@@ -94,9 +94,10 @@ struct abc_ctx {
   DBuf<Cand> d_cand;
   DBuf<float> d_cande;  // FP32 error of each candidate
   // tensor-core candidate pass: operands, per-gene terms, per-CTA output segments
-  int dist_mode = 2;       // 0 FP32 CUDA cores, 1 TF32 one-term, 2 TF32 three-term
+  int dist_mode = 3;       // 0 FP32 CUDA cores, 1 TF32 one-term, 2 TF32 three-term, 3 BF16 three-term
   int dist_mode_used = -1;
   DBuf<float> d_tcA, d_tcB, d_cg32, d_b0, d_Y, d_Xt, d_seg_e;
+  DBuf<uint8_t> d_rowbad;  // per particle of the candidate pass: a statistic is NaN
   DBuf<double> d_cg64;
   DBuf<unsigned> d_tcflags, d_segcount, d_hist;
   DBuf<int> d_tcerr;
@@ -239,7 +240,7 @@ int abc_destroy(abc_ctx* c) {
   c->d_dirty.release();
   c->d_out_err.release(); c->d_sw.release(); c->d_dw.release(); c->d_s32.release(); c->d_X.release();
   c->d_esub.release(); c->d_cand.release(); c->d_sp.release(); c->d_gcount.release(); c->d_goff.release();
-  c->d_cande.release(); c->d_den.release(); c->d_rden.release(); c->d_tcA.release(); c->d_tcB.release(); c->d_cg32.release(); c->d_b0.release();
+  c->d_cande.release(); c->d_den.release(); c->d_rden.release(); c->d_tcA.release(); c->d_tcB.release(); c->d_rowbad.release(); c->d_cg32.release(); c->d_b0.release();
   c->d_Y.release(); c->d_Xt.release(); c->d_seg_e.release(); c->d_cg64.release(); c->d_tcflags.release();
   c->d_segcount.release(); c->d_hist.release(); c->d_tcerr.release(); c->d_seg.release(); c->d_cand2.release();
   c->d_alen.release(); c->d_aoff.release(); c->d_out_idx.release(); c->d_gcursor.release();
@@ -938,7 +939,7 @@ static int candidate_pass_simt(abc_ctx* c, const DistInputs& in, int64_t* n) {
 // segments are concatenated into d_cand / d_cande.
 static int candidate_pass_tc(abc_ctx* c, const DistInputs& in, int nh, int64_t* n) {
   const int grid = tc_grid(in.P, in.G, c->sms);
-  const int KA = tc_ka(in.K, nh);
+  const TcLayout L = tc_layout(in.K, nh);
   CK(launch_tc_y(c->d_X.p, c->d_cg64.p, in.G, in.K, c->d_Y.p, c->stream));
   CK(c->d_segcount.ensure((size_t)grid));
   CK(c->d_tcerr.ensure(1));
@@ -952,8 +953,10 @@ static int candidate_pass_tc(abc_ctx* c, const DistInputs& in, int nh, int64_t* 
     a.P = in.P;
     a.G = in.G;
     a.K = in.K;
-    a.KA = KA;
-    a.n_chunks = KA / (nh == 3 ? 64 : 32);  // one 128-byte row per chunk
+    a.KA = L.H;
+    a.n_chunks = L.n_chunks;
+    a.cg = c->d_cg32.p;
+    a.rowbad = c->d_rowbad.p;
     a.nM = (int)((in.P + 127) / 128);
     a.nN = (int)((in.G + 255) / 256);
     a.Y = c->d_Y.p;
@@ -1006,19 +1009,19 @@ static int prepare_candidate_pass(abc_ctx* c, const DistInputs& in, int* dmode_o
   CK(c->d_b0.ensure((size_t)G));
   int dmode = c->dist_mode;
   float b1 = 0.0f;
+  if (dmode == 3 && !tc_mode3_fits(K)) dmode = 2;  // gene rows too long to stay in shared memory
   if (dmode) {
-    const int KA = tc_ka(K, dmode);
-    // FP32-sized words per row: hi (and lo) TF32 halves, or hi + lo BF16 halves in KA words
-    const size_t words = dmode == 3 ? (size_t)KA : (size_t)dmode * KA;
+    const size_t words = tc_layout(K, dmode).words();
     CK(c->d_tcA.ensure((size_t)P * words));
     CK(c->d_tcB.ensure((size_t)G * words));
+    CK(c->d_rowbad.ensure((size_t)std::max<int64_t>(P, 1)));
     CK(c->d_cg64.ensure((size_t)G));
     CK(c->d_cg32.ensure((size_t)G));
     CK(c->d_Y.ensure((size_t)G));
     CK(c->d_tcflags.ensure(3));
     CK(cudaMemsetAsync(c->d_tcflags.p, 0, sizeof(unsigned) * 3, c->stream));
     const double beta = tc_beta(K, dmode);
-    CK(launch_tc_prep(in, dmode, beta, c->d_tcA.p, c->d_tcB.p, c->d_cg64.p, c->d_cg32.p, c->d_b0.p,
+    CK(launch_tc_prep(in, dmode, beta, c->d_tcA.p, c->d_tcB.p, c->d_rowbad.p, c->d_cg64.p, c->d_cg32.p, c->d_b0.p,
                       c->d_tcflags.p, c->stream));
     unsigned fl[3];
     CK(cudaMemcpyAsync(fl, c->d_tcflags.p, sizeof(fl), cudaMemcpyDeviceToHost, c->stream));

@@ -55,14 +55,15 @@ constexpr int kThreads = 64 + kEpiThreads;
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kABytes = BM * BK * 4;    // 16 KB
 constexpr uint32_t kBBytes = BN * BK * 4;    // 32 KB
+static_assert(kABytes >> 4 == 1024 && kBBytes >> 4 == 2048, "descriptor offsets in 16-byte units");
 
 template <int NH>
 struct Cfg {
   static constexpr int kStages = NH == 1 ? 4 : 2;
   static constexpr uint32_t kStageBytes = NH * (kABytes + kBBytes);
   static constexpr uint32_t kTileBytes = kStages * kStageBytes;
-  // tiles + barriers (2 S + 5) + tmem slot + counters + per-gene Y of a tile
-  static constexpr uint32_t kSmem = 1024 + kTileBytes + 256 + BN * 4;
+  // tiles + barriers (2 S + 5) + tmem slot + counters + per-gene Y and column masks of a tile
+  static constexpr uint32_t kSmem = 1024 + kTileBytes + 256 + BN * 4 + BN / 8;
 };
 
 // Instruction descriptor: D = F32, A = B = TF32, both K-major, M = 128, N = 256.
@@ -91,14 +92,6 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b
       : "memory");
 }
 
-// one K-step (32 bytes of a 128-byte swizzled row: 8 TF32 or 16 BF16 values)
-template <bool BF>
-__device__ __forceinline__ void mma_step(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
-  if (BF)
-    mma_bf16(d_tmem, a, b, accumulate);
-  else
-    mma_tf32(d_tmem, a, b, accumulate);
-}
 __device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory"); }
 
 // v[j] for a lane-dependent j, by a 5-level select tree on the bits of j
@@ -116,32 +109,68 @@ __device__ __forceinline__ float pick32(const uint32_t (&v)[32], uint32_t j) {
   return __uint_as_float((j & 16u) ? a2[1] : a2[0]);
 }
 
+// Smallest float above y (y itself for +inf and NaN).
+__device__ __forceinline__ float next_up(float y) {
+  if (y != y || y == INFINITY) return y;
+  if (y == 0.0f) return __uint_as_float(1u);
+  const uint32_t u = __float_as_uint(y);
+  return __uint_as_float(y > 0.0f ? u + 1u : u - 1u);
+}
+
+// Per-tile inputs of the epilogue, written by epilogue threads et < BN:
+// Yn[j] = next_up(Y_g) and bit j of CM[w] set when column 32 w + j is a gene
+// g < G with Y_g and c_g not NaN (its accumulators are finite in every row
+// without a NaN statistic).
+__device__ __forceinline__ void epi_fill(int et, int64_t g0, const TcArgs& a, float* Yn, uint32_t* CM) {
+  static_assert(kEpiThreads >= BN && BN % 32 == 0, "one epilogue thread per column, whole warps");
+  if (et < BN) {
+    const int64_t g = g0 + et;
+    bool ok = false;
+    float y = -INFINITY;
+    if (g < a.G) {
+      y = a.Y[g];
+      const float c = a.cg[g];
+      ok = y == y && c == c;
+    }
+    Yn[et] = ok ? next_up(y) : -INFINITY;
+    const uint32_t b = __ballot_sync(0xffffffffu, ok);
+    if ((et & 31) == 0) CM[et >> 5] = b;
+  }
+}
+
 // Epilogue of one warp: its 32 accumulator rows (one TMEM lane quarter, lane =
 // particle row) x NG groups of 32 columns starting at TMEM address taddr.
-// Bit j of a lane's mask is acc <= Y_j (false for NaN).  A warp with any
-// candidate takes its positions in the CTA segment with one shared-memory
-// atomic plus the lanes' exclusive prefix (a ballot when no lane holds more
-// than one candidate, the common case); each candidate stores (p, g) and the
-// raw accumulator, which tc_gather_kernel turns into the clipped FP32 error.
+// For finite acc and Y, acc <= Y iff acc < next_up(Y) iff the sign bit of
+// the rounded difference acc - next_up(Y) is set (a nonzero difference keeps
+// its sign under rounding; acc == next_up(Y) gives +0): one subtraction (FMA
+// pipe) and one funnel shift per element build the lane's candidate mask,
+// which the column mask CM (genes with finite accumulators) and the row mask
+// rm (0 for a particle with a NaN statistic or beyond P) then restrict.  A
+// warp with any candidate takes its positions in the CTA segment with one
+// shared-memory atomic plus the lanes' exclusive prefix (a ballot when no lane
+// holds more than one candidate, the common case); each candidate stores
+// (p, g) and the raw accumulator, which tc_gather_kernel turns into the
+// clipped FP32 error.
 template <int NG>
-__device__ __forceinline__ void epi_warp(uint32_t taddr, const float* Ycol, int64_t row, bool valid, int64_t g0,
-                                         uint32_t* s_count, const TcArgs& a, int lane) {
+__device__ __forceinline__ void epi_warp(uint32_t taddr, const float* Yn, const uint32_t* CM, int64_t row,
+                                         uint32_t rm, int64_t g0, uint32_t* s_count, const TcArgs& a, int lane) {
 #pragma unroll 1
   for (int gi = 0; gi < NG; ++gi) {
     __syncwarp();
     uint32_t v[32];
     tmem_ld32(taddr + (uint32_t)(gi * 32), v);
-    const float4* Y4 = reinterpret_cast<const float4*>(Ycol + gi * 32);
-    uint32_t msk = 0;
+    const float4* Y4 = reinterpret_cast<const float4*>(Yn + gi * 32);
+    uint32_t m[4] = {0u, 0u, 0u, 0u};  // four independent chains, columns 8c .. 8c + 7
 #pragma unroll
-    for (int j4 = 0; j4 < 8; ++j4) {
+    for (int j4 = 7; j4 >= 0; --j4) {
       const float4 y = Y4[j4];
-      msk |= (uint32_t)(__uint_as_float(v[4 * j4 + 0]) <= y.x) << (4 * j4 + 0);
-      msk |= (uint32_t)(__uint_as_float(v[4 * j4 + 1]) <= y.y) << (4 * j4 + 1);
-      msk |= (uint32_t)(__uint_as_float(v[4 * j4 + 2]) <= y.z) << (4 * j4 + 2);
-      msk |= (uint32_t)(__uint_as_float(v[4 * j4 + 3]) <= y.w) << (4 * j4 + 3);
+      uint32_t& mc = m[j4 >> 1];
+      mc = __funnelshift_l(__float_as_uint(__fsub_rn(__uint_as_float(v[4 * j4 + 3]), y.w)), mc, 1);
+      mc = __funnelshift_l(__float_as_uint(__fsub_rn(__uint_as_float(v[4 * j4 + 2]), y.z)), mc, 1);
+      mc = __funnelshift_l(__float_as_uint(__fsub_rn(__uint_as_float(v[4 * j4 + 1]), y.y)), mc, 1);
+      mc = __funnelshift_l(__float_as_uint(__fsub_rn(__uint_as_float(v[4 * j4 + 0]), y.x)), mc, 1);
     }
-    if (!valid) msk = 0;
+    uint32_t msk = (m[0] | (m[1] << 8) | (m[2] << 16) | (m[3] << 24)) & CM[gi] & rm;
     const uint32_t has = __ballot_sync(0xffffffffu, msk != 0u);
     if (has == 0u) continue;
     const uint32_t cnt = __popc(msk);
@@ -180,12 +209,11 @@ __device__ __forceinline__ void epi_warp(uint32_t taddr, const float* Ycol, int6
 
 enum : int { kErrProducer = 1, kErrMma = 2, kErrEpilogue = 4, kErrDrain = 8 };
 
-// BF: BF16 operands (64 values per 128-byte row) instead of TF32 (32 values).
-// K-steps that lie wholly in the zero padding beyond the 2K real columns are skipped.
-template <int NH, bool BF>
+// TF32 operands streamed for both A and B (modes 1 and 2).  K-steps that lie
+// wholly in the zero padding beyond the 2K real columns are skipped.
+template <int NH>
 __global__ void __launch_bounds__(kThreads, 1)
     dist_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs a) {
-  constexpr int kEl = BF ? 64 : 32;  // values per chunk (one swizzled row)
   const int twoK = 2 * a.K;
   using C = Cfg<NH>;
   constexpr int S = C::kStages;
@@ -201,6 +229,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint32_t* s_count = tslot + 1;
   uint32_t* s_abort = tslot + 2;
   float* Ys = (float*)(smem + C::kTileBytes + 256);
+  uint32_t* CM = (uint32_t*)(Ys + BN);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -250,10 +279,10 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint32_t st = smem_base + stage * C::kStageBytes;
 #pragma unroll
           for (int h = 0; h < NH; ++h)
-            tma_load(st + h * kABytes, &tmA, &full[stage], h * a.KA + c * kEl, m * BM);
+            tma_load(st + h * kABytes, &tmA, &full[stage], h * a.KA + c * BK, m * BM);
 #pragma unroll
           for (int h = 0; h < NH; ++h)
-            tma_load(st + NH * kABytes + h * kBBytes, &tmB, &full[stage], h * a.KA + c * kEl, n * BN);
+            tma_load(st + NH * kABytes + h * kBBytes, &tmB, &full[stage], h * a.KA + c * BK, n * BN);
           issued |= 1u << stage;
           issued_par = (issued_par & ~(1u << stage)) | (phase << stage);
           if (++stage == S) {
@@ -292,14 +321,14 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint32_t st = smem_base + stage * C::kStageBytes;
           const uint64_t a0 = sw128_desc(st), b0 = sw128_desc(st + NH * kABytes);
 #pragma unroll
-          for (int kk = 0; kk < 4; ++kk) {
-            if (c * kEl + kk * (kEl / 4) >= twoK) break;  // zero padding: nothing to add
-            const uint64_t adv = (uint64_t)(kk * 32) >> 4;  // 32 bytes along K
-            mma_step<BF>(d_tmem, a0 + adv, b0 + adv, (c | kk) != 0);
+          for (int kk = 0; kk < BK / 8; ++kk) {
+            if (c * BK + kk * 8 >= twoK) break;  // zero padding: nothing to add
+            const uint64_t adv = (uint64_t)(kk * 32) >> 4;  // 8 TF32 = 32 bytes along K
+            mma_tf32(d_tmem, a0 + adv, b0 + adv, (c | kk) != 0);
             if (NH == 2) {
               const uint64_t a1 = sw128_desc(st + kABytes), b1 = sw128_desc(st + NH * kABytes + kBBytes);
-              mma_step<BF>(d_tmem, a0 + adv, b1 + adv, 1u);  // hi x lo
-              mma_step<BF>(d_tmem, a1 + adv, b0 + adv, 1u);  // lo x hi
+              mma_tf32(d_tmem, a0 + adv, b1 + adv, 1u);  // hi x lo
+              mma_tf32(d_tmem, a1 + adv, b0 + adv, 1u);  // lo x hi
             }
           }
           mma_commit(&empty[stage]);  // stage reusable once these MMAs have read it
@@ -328,11 +357,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     uint32_t acc_phase = 0;
     for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
       const int m = t / a.nN, n = t - (t / a.nN) * a.nN;
+      const int64_t row = (int64_t)m * BM + q * 32 + lane;
+      const uint32_t rm = (row < a.P && !a.rowbad[row]) ? 0xffffffffu : 0u;
       epi_bar();  // readers of the previous tile's Y are done
-      for (int j = et; j < BN; j += kEpiThreads) {
-        const int64_t g = (int64_t)n * BN + j;
-        Ys[j] = g < a.G ? a.Y[g] : -INFINITY;
-      }
+      epi_fill(et, (int64_t)n * BN, a, Ys, CM);
       const bool got = mbar_wait(&tfull[acc], acc_phase);
       if (!got) atomicOr(s_abort, 1u);
       epi_bar();
@@ -341,10 +369,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         break;
       }
       tc_fence_after();
-      const int64_t row = (int64_t)m * BM + q * 32 + lane;
       const int col0 = part * kEpiGroups * 32;
-      epi_warp<kEpiGroups>(tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + col0), Ys + col0, row,
-                           row < a.P, (int64_t)n * BN + col0, s_count, a, lane);
+      epi_warp<kEpiGroups>(tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + col0), Ys + col0,
+                           CM + col0 / 32, row, rm, (int64_t)n * BN + col0, s_count, a, lane);
       tc_fence_before();
       mbar_arrive(&tempty[acc]);
       if (++acc == 2) {
@@ -361,31 +388,42 @@ __global__ void __launch_bounds__(kThreads, 1)
 }
 
 // ---------------------------------------------------------------------------
-// One-term candidate pass with the gene operand resident in shared memory.
+// Candidate pass with the gene operand resident in shared memory: TF32 one
+// term (mode 1) or BF16 hi/lo three terms (mode 3, BF3).
 //
-// A 128 x 256 tile of the streaming kernel above loads 80 KB of particle rows
-// and 160 KB of gene rows (depth 160) through L2 for about 1.4 us of one-term
-// MMAs, which makes L2-to-SM bandwidth the limit.  Here each CTA keeps the
-// gene rows of one 256-gene tile (n_chunks x 32 KB) in shared memory for all
-// of its particle tiles and streams only the particle rows through a ring of
-// 16 KB stages.  Work: nN gene tiles x cpt = max(1, grid / nN) particle-tile
-// sequences (m = j, j + cpt, ...), handed to the CTAs round-robin; the CTAs
-// that hold different gene tiles walk the same particle sequence in the same
-// order, so each particle tile comes from DRAM about once and from L2 after
-// that.  Roles, barriers, bounded waits and the epilogue are those of
-// dist_tc_kernel; two more barriers (bfull, bempty) order the gene-row loads
-// of successive assignments against the MMAs that read them.
+// A 128 x 256 tile of the streaming kernel above loads particle and gene rows
+// for every tile (240 KB at depth 160 in one-term mode, 480 KB in three-term
+// mode) through L2, which makes L2-to-SM bandwidth the limit.  Here each CTA
+// keeps the gene rows of one 256-gene tile (n_chunks x 32 KB) in shared memory
+// for all of its particle tiles and streams only the particle rows through a
+// ring of 16 KB stages.  Work: nN gene tiles x cpt = max(1, grid / nN)
+// particle-tile sequences (m = j, j + cpt, ...), handed to the CTAs
+// round-robin; the CTAs that hold different gene tiles walk the same particle
+// sequence in the same order, so each particle tile comes from DRAM about once
+// and from L2 after that.  Roles, barriers, bounded waits and the epilogue are
+// those of dist_tc_kernel; two more barriers (bfull, bempty) order the
+// gene-row loads of successive assignments against the MMAs that read them.
+//
+// BF3 rows hold hi at [0, 2K) and lo at [H, H + 2K) with H a multiple of 16
+// (one BF16 K-step), so K-step s < H/16 of a particle row is a hi step, paired
+// with gene K-steps s (hi x hi) and s + H/16 (hi x lo), and K-step
+// H/16 <= s < 2H/16 a lo step, paired with gene K-step s - H/16 (lo x hi):
+// the whole gene row is resident, so any gene K-step is at hand.
 // ---------------------------------------------------------------------------
 constexpr int kResMaxStages = 4;
+constexpr int kResPrefetch = 2;  // particle tiles ahead whose rows are prefetched into L2
 constexpr uint32_t kResSmemMax = 227u * 1024u;  // dynamic shared memory of one CTA
 
 __host__ __device__ constexpr uint32_t res_smem(int n_chunks, int stages) {
-  return 1024u + (uint32_t)n_chunks * kBBytes + (uint32_t)stages * kABytes + 256u + BN * 4u;
+  return 1024u + (uint32_t)n_chunks * kBBytes + (uint32_t)stages * kABytes + 256u + BN * 4u + BN / 8u;
 }
 
+template <bool BF3>
 __global__ void __launch_bounds__(kThreads, 1)
     dist_tc_res_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs a,
                        int S) {
+  constexpr int kEl = BF3 ? 64 : 32;  // values per 128-byte chunk
+  constexpr int kStepEl = kEl / 4;    // values per K-step (32 bytes)
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = smem_raw + ((1024u - (su32(smem_raw) & 1023u)) & 1023u);
   const int NC = a.n_chunks;
@@ -401,6 +439,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint32_t* s_count = tslot + 1;
   uint32_t* s_abort = tslot + 2;
   float* Ys = (float*)((uint8_t*)full + 256);
+  uint32_t* CM = (uint32_t*)(Ys + BN);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -447,9 +486,14 @@ __global__ void __launch_bounds__(kThreads, 1)
           break;
         }
         mbar_expect_tx(bfull, (uint32_t)NC * kBBytes);
-        for (int c = 0; c < NC; ++c) tma_load(b_base + (uint32_t)c * kBBytes, &tmB, bfull, c * BK, n * BN);
+        for (int c = 0; c < NC; ++c) tma_load(b_base + (uint32_t)c * kBBytes, &tmB, bfull, c * kEl, n * BN);
         ++b_issued;
         for (int m = j; m < a.nM && ok; m += cpt) {
+          // the particle rows of the tile kResPrefetch steps ahead start their way from DRAM into L2
+          // now, so that the ring's loads (at most S chunks ahead of the MMAs) find them there
+          const int mp = m + kResPrefetch * cpt;
+          if (mp < a.nM)
+            for (int c = 0; c < NC; ++c) tma_prefetch_l2(&tmA, c * kEl, mp * BM);
           for (int c = 0; c < NC; ++c) {
             if (!mbar_wait(&empty[stage], phase ^ 1)) {
               atomicOr(a.err, kErrProducer);
@@ -457,7 +501,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               break;
             }
             mbar_expect_tx(&full[stage], kABytes);
-            tma_load(ring_base + (uint32_t)stage * kABytes, &tmA, &full[stage], c * BK, m * BM);
+            tma_load(ring_base + (uint32_t)stage * kABytes, &tmA, &full[stage], c * kEl, m * BM);
             issued |= 1u << stage;
             issued_par = (issued_par & ~(1u << stage)) | (phase << stage);
             if (++stage == S) {
@@ -482,6 +526,11 @@ __global__ void __launch_bounds__(kThreads, 1)
       uint32_t acc_phase = 0;
       bool ok = true;
       uint32_t k_as = 0;
+      const int hs = a.KA / kStepEl;                    // K-steps per half (BF3)
+      const int n_steps = BF3 ? 2 * hs : (2 * a.K + kStepEl - 1) / kStepEl;  // K-steps holding real values
+      // descriptors by offset: chunk c of the gene rows and stage s of the ring are kBBytes / kABytes
+      // apart, K-step kk of a chunk 32 bytes in (the start-address field counts 16-byte units)
+      const uint64_t bd0 = sw128_desc(b_base), ad0 = sw128_desc(ring_base);
       for (int as = blockIdx.x; as < n_assign && ok; as += gridDim.x, ++k_as) {
         const int j = as / a.nN;
         if (!mbar_wait(bfull, k_as & 1u)) {
@@ -503,13 +552,24 @@ __global__ void __launch_bounds__(kThreads, 1)
               break;
             }
             tc_fence_after();
-            const uint64_t a0 = sw128_desc(ring_base + (uint32_t)stage * kABytes);
-            const uint64_t b0 = sw128_desc(b_base + (uint32_t)c * kBBytes);
+            const uint64_t a0 = ad0 + (uint64_t)(stage * (int)(kABytes >> 4));
 #pragma unroll
-            for (int kk = 0; kk < BK / 8; ++kk) {
-              if (c * BK + kk * 8 >= 2 * a.K) break;  // zero padding: nothing to add
-              const uint64_t adv = (uint64_t)(kk * 32) >> 4;  // 8 TF32 = 32 bytes along K
-              mma_tf32(d_tmem, a0 + adv, b0 + adv, (c | kk) != 0);
+            for (int kk = 0; kk < 4; ++kk) {
+              const int st_a = c * 4 + kk;  // K-step of the particle row
+              if (st_a >= n_steps) break;   // zero padding: nothing to add
+              const uint64_t adv = (uint64_t)(kk * 2);  // 32 bytes along K
+              if (BF3) {
+                // gene K-step t: resident chunk t / 4, 32 (t % 4) bytes in
+                const int t0 = st_a < hs ? st_a : st_a - hs;
+                mma_bf16(d_tmem, a0 + adv, bd0 + (uint64_t)(((t0 >> 2) << 11) + ((t0 & 3) << 1)),
+                         st_a != 0);  // hi x hi, or lo x hi
+                if (st_a < hs) {
+                  const int t1 = st_a + hs;
+                  mma_bf16(d_tmem, a0 + adv, bd0 + (uint64_t)(((t1 >> 2) << 11) + ((t1 & 3) << 1)), 1u);  // hi x lo
+                }
+              } else {
+                mma_tf32(d_tmem, a0 + adv, bd0 + (uint64_t)((c << 11) + kk * 2), st_a != 0);
+              }
             }
             mma_commit(&empty[stage]);
             if (++stage == S) {
@@ -540,11 +600,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int as = blockIdx.x; as < n_assign && !stop; as += gridDim.x) {
       const int n = as % a.nN, j = as / a.nN;
       for (int m = j; m < a.nM; m += cpt) {
+        const int64_t row = (int64_t)m * BM + q * 32 + lane;
+        const uint32_t rm = (row < a.P && !a.rowbad[row]) ? 0xffffffffu : 0u;
         epi_bar();  // readers of the previous tile's Y are done
-        for (int jj = et; jj < BN; jj += kEpiThreads) {
-          const int64_t g = (int64_t)n * BN + jj;
-          Ys[jj] = g < a.G ? a.Y[g] : -INFINITY;
-        }
+        epi_fill(et, (int64_t)n * BN, a, Ys, CM);
         const bool got = mbar_wait(&tfull[acc], acc_phase);
         if (!got) atomicOr(s_abort, 1u);
         epi_bar();
@@ -554,10 +613,9 @@ __global__ void __launch_bounds__(kThreads, 1)
           break;
         }
         tc_fence_after();
-        const int64_t row = (int64_t)m * BM + q * 32 + lane;
         const int col0 = part * kEpiGroups * 32;
-        epi_warp<kEpiGroups>(tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + col0), Ys + col0, row,
-                             row < a.P, (int64_t)n * BN + col0, s_count, a, lane);
+        epi_warp<kEpiGroups>(tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + col0), Ys + col0,
+                             CM + col0 / 32, row, rm, (int64_t)n * BN + col0, s_count, a, lane);
         tc_fence_before();
         mbar_arrive(&tempty[acc]);
         if (++acc == 2) {
@@ -649,15 +707,16 @@ __device__ __forceinline__ void split_opf(float x, float& hi, float& lo) {
 constexpr int kPrepLoads = 16;
 
 template <bool BF>
-__global__ void tc_prep_rows_kernel(const double* stats, int64_t P, int K, int KA, int NH, void* A,
-                                    unsigned* flags) {
+__global__ void tc_prep_rows_kernel(const double* stats, int64_t P, int K, int H, int ld_, int NH, void* A,
+                                    uint8_t* rowbad, unsigned* flags) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  const int64_t ld = (int64_t)NH * KA;
+  const int64_t ld = ld_;
   const int R = K <= 32 * kPrepLoads ? (32 * kPrepLoads) / K < 4 ? (32 * kPrepLoads) / K : 4 : 1;
   unsigned inf = 0, mx = 0;
   for (int64_t p0 = ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * R; p0 < P; p0 += warps * R) {
     const int rows = P - p0 < R ? (int)(P - p0) : R;
+    uint32_t nanr = 0;  // bit r: row p0 + r holds a NaN statistic
     if (K > 32 * kPrepLoads) {  // very wide rows: one row at a time
       const double* srow = stats + p0 * K;
       const int64_t arow = p0 * ld;
@@ -670,11 +729,12 @@ __global__ void tc_prep_rows_kernel(const double* stats, int64_t P, int K, int K
         put_op<BF>(A, arow + k, h1);
         put_op<BF>(A, arow + K + k, h2);
         if (NH == 2) {
-          put_op<BF>(A, arow + KA + k, l1);
-          put_op<BF>(A, arow + KA + K + k, l2);
+          put_op<BF>(A, arow + H + k, l1);
+          put_op<BF>(A, arow + H + K + k, l2);
         }
         if (fabsf(sv) == INFINITY || fabsf(s2) == INFINITY) inf = 1u;
         if (s2 == s2) mx = max(mx, __float_as_uint(s2));
+        if (sv != sv) nanr = 1u;
       }
     } else {
       // flat index f = lane + 32 t over rows x K, (r, k) = divmod(f, K)
@@ -701,11 +761,12 @@ __global__ void tc_prep_rows_kernel(const double* stats, int64_t P, int K, int K
           put_op<BF>(A, arow + k, h1);
           put_op<BF>(A, arow + K + k, h2);
           if (NH == 2) {
-            put_op<BF>(A, arow + KA + k, l1);
-            put_op<BF>(A, arow + KA + K + k, l2);
+            put_op<BF>(A, arow + H + k, l1);
+            put_op<BF>(A, arow + H + K + k, l2);
           }
           if (fabsf(sv) == INFINITY || fabsf(s2) == INFINITY) inf = 1u;
           if (s2 == s2) mx = max(mx, __float_as_uint(s2));
+          if (sv != sv) nanr |= 1u << r;
         }
         k += 32;
         while (k >= K) {
@@ -714,12 +775,15 @@ __global__ void tc_prep_rows_kernel(const double* stats, int64_t P, int K, int K
         }
       }
     }
+    nanr = __reduce_or_sync(0xffffffffu, nanr);
+    if (lane < rows) rowbad[p0 + lane] = (uint8_t)((nanr >> lane) & 1u);
     for (int rr = 0; rr < rows; ++rr) {
       const int64_t arow = (p0 + rr) * ld;
-      for (int k = 2 * K + lane; k < KA; k += 32) {
+      for (int k = 2 * K + lane; k < H; k += 32) {
         put_op<BF>(A, arow + k, 0.0f);
-        if (NH == 2) put_op<BF>(A, arow + KA + k, 0.0f);
+        if (NH == 2) put_op<BF>(A, arow + H + k, 0.0f);
       }
+      for (int k = NH * H + lane; k < ld_; k += 32) put_op<BF>(A, arow + k, 0.0f);
     }
   }
   inf = __reduce_or_sync(0xffffffffu, inf);
@@ -733,15 +797,16 @@ __global__ void tc_prep_rows_kernel(const double* stats, int64_t P, int K, int K
 // B rows: [-2 w d (K) | w (K) | 0 ...] per half; c_g = sum_k w d^2 in FP64; the
 // per-gene term of the error bound b0_g = 5 beta c_g / K.
 template <bool BF>
-__global__ void tc_prep_genes_kernel(const double* data, const double* se, int64_t G, int K, int KA, int NH,
+__global__ void tc_prep_genes_kernel(const double* data, const double* se, int64_t G, int K, int H, int ld_, int NH,
                                      double beta, void* B, double* cg64, float* cg32, float* b0, unsigned* flags) {
   const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= G) return;
-  const int64_t ld = (int64_t)NH * KA;
+  const int64_t ld = ld_;
   const double sig2 = 0.1 * 0.1;
   double c = 0.0;
   bool bad = false;
-  for (int k = 0; k < KA; ++k) {
+  for (int k = NH * H; k < ld_; ++k) put_op<BF>(B, g * ld + k, 0.0f);
+  for (int k = 0; k < H; ++k) {
     double v = 0.0;
     if (k < 2 * K) {
       const int kk = k < K ? k : k - K;
@@ -759,7 +824,7 @@ __global__ void tc_prep_genes_kernel(const double* data, const double* se, int64
     else
       split_tf32(v, hi, lo);
     put_op<BF>(B, g * ld + k, hi);
-    if (NH == 2) put_op<BF>(B, g * ld + KA + k, lo);
+    if (NH == 2) put_op<BF>(B, g * ld + H + k, lo);
   }
   if (bad) atomicOr(&flags[0], 1u);
   cg64[g] = c;
@@ -826,23 +891,36 @@ bool make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t cols, in
                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <int NH, bool BF>
+template <int NH>
 cudaError_t launch_nh(const void* A, const void* B, const TcArgs& args, int grid, cudaStream_t s) {
   static std::atomic<uint64_t> attr{0};  // devices where the limit is set, shared by all contexts
-  cudaError_t e = set_smem_once(attr, dist_tc_kernel<NH, BF>, (int)Cfg<NH>::kSmem);
+  cudaError_t e = set_smem_once(attr, dist_tc_kernel<NH>, (int)Cfg<NH>::kSmem);
   if (e != cudaSuccess) return e;
   CUtensorMap ma, mb;
   const int64_t ld = (int64_t)NH * args.KA;
-  if (!make_map(&ma, A, args.P, ld, BM, BF) || !make_map(&mb, B, args.G, ld, BN, BF)) return cudaErrorInvalidValue;
-  dist_tc_kernel<NH, BF><<<grid, kThreads, Cfg<NH>::kSmem, s>>>(ma, mb, args);
+  if (!make_map(&ma, A, args.P, ld, BM) || !make_map(&mb, B, args.G, ld, BN)) return cudaErrorInvalidValue;
+  dist_tc_kernel<NH><<<grid, kThreads, Cfg<NH>::kSmem, s>>>(ma, mb, args);
   return cudaGetLastError();
 }
 
+constexpr int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
 }  // namespace
 
-int tc_ka(int K, int mode) {
-  const int el = mode == 3 ? 64 : BK;  // values per 128-byte row
-  return ((2 * K + el - 1) / el) * el;
+TcLayout tc_layout(int K, int mode) {
+  TcLayout L;
+  if (mode == 3) {
+    L.H = round_up(2 * K, 16);
+    L.ld = round_up(2 * L.H, 64);
+    L.n_chunks = L.ld / 64;
+    L.es = 2;
+  } else {
+    L.H = round_up(2 * K, BK);
+    L.ld = mode == 1 ? L.H : 2 * L.H;
+    L.n_chunks = L.H / BK;
+    L.es = 4;
+  }
+  return L;
 }
 
 double tc_beta(int K, int nh) {
@@ -868,26 +946,28 @@ double tc_beta(int K, int nh) {
   return 1.1 * b;
 }
 
-cudaError_t launch_tc_prep(const DistInputs& in, int mode, double beta, void* A, void* B, double* cg64, float* cg32,
-                           float* b0, unsigned* flags, cudaStream_t s) {
-  const int KA = tc_ka(in.K, mode);
+cudaError_t launch_tc_prep(const DistInputs& in, int mode, double beta, void* A, void* B, uint8_t* rowbad,
+                           double* cg64, float* cg32, float* b0, unsigned* flags, cudaStream_t s) {
+  const TcLayout L = tc_layout(in.K, mode);
   const int NH = mode == 1 ? 1 : 2;
   const bool bf = mode == 3;
   if (in.P > 0) {
     const int64_t blocks = (in.P + 31) / 32 < 8192 ? (in.P + 31) / 32 : 8192;
     if (bf)
-      tc_prep_rows_kernel<true><<<(unsigned)blocks, 256, 0, s>>>(in.stats, in.P, in.K, KA, NH, A, flags);
+      tc_prep_rows_kernel<true><<<(unsigned)blocks, 256, 0, s>>>(in.stats, in.P, in.K, L.H, L.ld, NH, A, rowbad,
+                                                                 flags);
     else
-      tc_prep_rows_kernel<false><<<(unsigned)blocks, 256, 0, s>>>(in.stats, in.P, in.K, KA, NH, A, flags);
+      tc_prep_rows_kernel<false><<<(unsigned)blocks, 256, 0, s>>>(in.stats, in.P, in.K, L.H, L.ld, NH, A, rowbad,
+                                                                  flags);
   }
   if (in.G > 0) {
     const unsigned gb = (unsigned)((in.G + 127) / 128);
     if (bf)
-      tc_prep_genes_kernel<true><<<gb, 128, 0, s>>>(in.data, in.se, in.G, in.K, KA, NH, beta, B, cg64, cg32, b0,
-                                                    flags);
+      tc_prep_genes_kernel<true><<<gb, 128, 0, s>>>(in.data, in.se, in.G, in.K, L.H, L.ld, NH, beta, B, cg64, cg32,
+                                                    b0, flags);
     else
-      tc_prep_genes_kernel<false><<<gb, 128, 0, s>>>(in.data, in.se, in.G, in.K, KA, NH, beta, B, cg64, cg32, b0,
-                                                     flags);
+      tc_prep_genes_kernel<false><<<gb, 128, 0, s>>>(in.data, in.se, in.G, in.K, L.H, L.ld, NH, beta, B, cg64, cg32,
+                                                     b0, flags);
   }
   return cudaGetLastError();
 }
@@ -903,16 +983,18 @@ int tc_grid(int64_t P, int64_t G, int sms) {
   return (int)(tiles < sms ? tiles : sms);
 }
 
+template <bool BF3>
 static cudaError_t launch_res(const void* A, const void* B, const TcArgs& args, int grid, int stages,
                               cudaStream_t s) {
   const uint32_t smem = res_smem(args.n_chunks, stages);
   static std::atomic<uint64_t> attr{0};
   // the largest configuration sets the limit once per device; smaller ones fit under it
-  cudaError_t e = set_smem_once(attr, dist_tc_res_kernel, (int)kResSmemMax);
+  cudaError_t e = set_smem_once(attr, dist_tc_res_kernel<BF3>, (int)kResSmemMax);
   if (e != cudaSuccess) return e;
   CUtensorMap ma, mb;
-  if (!make_map(&ma, A, args.P, args.KA, BM) || !make_map(&mb, B, args.G, args.KA, BN)) return cudaErrorInvalidValue;
-  dist_tc_res_kernel<<<grid, kThreads, smem, s>>>(ma, mb, args, stages);
+  const int64_t ld = (int64_t)args.n_chunks * (BF3 ? 64 : 32);  // row length in values
+  if (!make_map(&ma, A, args.P, ld, BM, BF3) || !make_map(&mb, B, args.G, ld, BN, BF3)) return cudaErrorInvalidValue;
+  dist_tc_res_kernel<BF3><<<grid, kThreads, smem, s>>>(ma, mb, args, stages);
   return cudaGetLastError();
 }
 
@@ -922,12 +1004,14 @@ int tc_res_stages(int n_chunks) {
   return 0;
 }
 
-cudaError_t launch_dist_tc(int nh, const void* A, const void* B, const TcArgs& args, int grid, cudaStream_t s) {
+bool tc_mode3_fits(int K) { return tc_res_stages(tc_layout(K, 3).n_chunks) != 0; }
+
+cudaError_t launch_dist_tc(int mode, const void* A, const void* B, const TcArgs& args, int grid, cudaStream_t s) {
   if (args.P <= 0 || args.G <= 0) return cudaSuccess;
-  if (nh == 3) return launch_nh<2, true>(A, B, args, grid, s);
-  if (nh == 2) return launch_nh<2, false>(A, B, args, grid, s);
-  const int stages = tc_res_stages(args.n_chunks);
-  return stages ? launch_res(A, B, args, grid, stages, s) : launch_nh<1, false>(A, B, args, grid, s);
+  const int stages = mode == 2 ? 0 : tc_res_stages(args.n_chunks);
+  if (mode == 3) return stages ? launch_res<true>(A, B, args, grid, stages, s) : cudaErrorInvalidValue;
+  if (mode == 2) return launch_nh<2>(A, B, args, grid, s);
+  return stages ? launch_res<false>(A, B, args, grid, stages, s) : launch_nh<1>(A, B, args, grid, s);
 }
 
 cudaError_t launch_tc_gather(const Cand* seg, const float* seg_e, const unsigned* count, int n_seg, int64_t seg_cap,

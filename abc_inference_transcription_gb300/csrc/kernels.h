@@ -67,26 +67,40 @@ struct Cand {
 };
 
 // Tensor-core candidate pass (distance_tc.cu).  A = [s | s^2] per particle and
-// B = [-2 w d | w] per gene, TF32, rows of tc_ka(K) values per half (hi, and lo
-// in three-term mode); K err = c_g + A.B accumulated in FP32.
+// B = [-2 w d | w] per gene; K err = c_g + A.B accumulated in FP32.  Operand
+// rows hold the hi part at [0, 2K) and, in the three-term modes, the lo part at
+// [H, H + 2K), zero elsewhere up to the row length ld:
+//   mode 1  TF32 hi only,   H = 2K rounded up to 32, ld = H;
+//   mode 2  TF32 hi and lo, H = 2K rounded up to 32, ld = 2H;
+//   mode 3  BF16 hi and lo, H = 2K rounded up to 16, ld = 2H rounded up to 64.
+struct TcLayout {
+  int H;         // offset of the lo part (values)
+  int ld;        // row length (values)
+  int n_chunks;  // 128-byte chunks the MMA loop walks: per half (mode 2) or per row (modes 1, 3)
+  int es;        // bytes per value (4 TF32, 2 BF16)
+  size_t words() const { return (size_t)ld * es / 4; }  // row length in 4-byte words
+};
+TcLayout tc_layout(int K, int mode);
 struct TcArgs {
   int64_t P, G;
-  int K, KA, n_chunks, nM, nN;
+  int K, KA, n_chunks, nM, nN;  // KA = TcLayout::H
   const float* Y;       // per gene: K X_g - c_g rounded up (candidate iff acc <= Y_g)
+  const float* cg;      // per gene c_g in FP32 (NaN: the gene's operand row holds a NaN)
+  const uint8_t* rowbad;  // per particle: 1 if a statistic is NaN (its accumulators are NaN)
   Cand* cand;           // per-CTA segments of seg_cap entries
   float* cand_e;        // raw accumulator of each candidate (K err - c_g)
   int64_t seg_cap;
   unsigned* seg_count;  // per CTA: candidates found (may exceed seg_cap)
   int* err;             // nonzero: a bounded wait ran out
 };
-// operand row length (values per half) of candidate-pass mode 1, 2 (TF32) or 3 (BF16)
-int tc_ka(int K, int mode = 2);
+// mode 3 needs the gene tile resident in shared memory; false: K too large, use mode 2
+bool tc_mode3_fits(int K);
 // relative error factor beta: |e32 - e| <= beta (5 c_g / K + 4 e)
 double tc_beta(int K, int nh);
 int tc_grid(int64_t P, int64_t G, int sms);
 // flags[0] bit 0: an operand is infinite in FP32; flags[1], flags[2]: max w, max s^2 (FP32 bits)
-cudaError_t launch_tc_prep(const DistInputs& in, int mode, double beta, void* A, void* B, double* cg64, float* cg32,
-                           float* b0, unsigned* flags, cudaStream_t s);
+cudaError_t launch_tc_prep(const DistInputs& in, int mode, double beta, void* A, void* B, uint8_t* rowbad,
+                           double* cg64, float* cg32, float* b0, unsigned* flags, cudaStream_t s);
 cudaError_t launch_tc_y(const float* X, const double* cg64, int64_t G, int K, float* Y, cudaStream_t s);
 // mode 1: TF32 one term, 2: TF32 hi/lo three terms, 3: BF16 hi/lo three terms
 cudaError_t launch_dist_tc(int mode, const void* A, const void* B, const TcArgs& args, int grid, cudaStream_t s);

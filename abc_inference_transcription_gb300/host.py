@@ -359,8 +359,8 @@ class Context:
 
     def set_distance_mode(self, mode: int) -> None:
         """Candidate pass: 0 FP32 CUDA cores, 1 TF32 tensor cores (one term),
-        2 TF32 tensor cores with hi/lo splits (default), 3 BF16 tensor cores
-        with hi/lo splits (three terms)."""
+        2 TF32 tensor cores with hi/lo splits, 3 BF16 tensor cores with hi/lo
+        splits (three terms; default; K > 96 runs mode 2)."""
         self._check(self.lib.abc_set_distance_mode(self.h, int(mode)))
 
     def distance_mode(self) -> tuple[int, int]:

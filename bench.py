@@ -344,17 +344,17 @@ def distance_bench(P: int, G: int, K: int, q: float, seed: int, cpu_seconds: flo
            "distance_mode": mode_used, "downstream": down,
            "fp64_error_path": {"seconds": dt_e, "pairs_per_s": P * G / dt_e, "accepted": int(off_e[-1])},
            "candidate_pass_modes": {"one_term_tf32_resident_genes": per_mode[1], "three_term_tf32": per_mode[2],
-                                    "three_term_bf16": per_mode[3],
+                                    "three_term_bf16_resident_genes": per_mode[3],
                                     "identical_accepted_lists": same_lists},
            "oracle_check": oracle_chk}
     kernel_ms = fast_ms / max(passes, 1)
     pk, src = load_peaks()
     algo = 2.0 * P * G * (2 * K)  # one multiply-add per (particle, gene, operand column) of [s | s^2]
     if mode_used in (1, 2, 3):
-        # tcgen05 MMAs issued per pass: 128 x 256 tiles, depth KA per term, 1 or 3 terms
-        # (TF32 for modes 1-2, KA a multiple of 32; BF16 for mode 3, KA a multiple of 64)
-        el = 64 if mode_used == 3 else 32
-        ka = -(-2 * K // el) * el
+        # tcgen05 MMAs issued per pass: 128 x 256 tiles, 1 or 3 terms, each of depth 2K rounded up to
+        # the K-step (8 TF32 values for modes 1-2, 16 BF16 values for mode 3; steps of zero padding are skipped)
+        step = 16 if mode_used == 3 else 8
+        ka = -(-2 * K // step) * step
         tiles = -(-P // 128) * -(-G // 256)
         terms = 1 if mode_used == 1 else 3
         issued = 2.0 * 128 * 256 * ka * terms * tiles

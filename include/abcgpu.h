@@ -281,9 +281,10 @@ int abc_select_profile_read(const abc_ctx* ctx, double* fast_ms, int* fast_passe
  * reference evaluates every pair in FP64):
  *   0  FP32 on the CUDA cores, 2 FMA per (particle, gene, statistic);
  *   1  TF32 tensor cores, K err = c_g + [s | s^2] . [-2 w d | w], one term;
- *   2  as 1 with hi/lo TF32 splits (three terms, ~FP32 products; default);
- *   3  as 2 with hi/lo BF16 splits (three BF16 MMAs at twice the TF32 rate,
- *      half the operand bytes; products to ~2^-16 relative).
+ *   2  as 1 with hi/lo TF32 splits (three terms, ~FP32 products);
+ *   3  as 2 with hi/lo BF16 splits (products to ~2^-17 relative; BF16 MMAs
+ *      with the gene rows resident in shared memory; default).  Rows longer
+ *      than 4K = 384 values (K > 96) do not fit; such a selection runs mode 2.
  * Modes 1-3 fall back to 0 for a selection whose inputs hold an infinite
  * value or could overflow FP32 in w s^2.  Accepted sets do not depend on the
  * mode: every mode is followed by the same FP64 recheck. */

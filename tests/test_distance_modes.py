@@ -1,6 +1,6 @@
 """Candidate passes of the distance step: FP32 on the CUDA cores (mode 0) and
-the TF32 tensor-core GEMM expansion (modes 1 and 2, scripts/compute_errors.jl:30-43
-expanded as K err = c_g + [s | s^2] . [-2 w d | w]).
+the tensor-core GEMM expansion (TF32 modes 1 and 2, BF16 hi/lo mode 3;
+scripts/compute_errors.jl:30-43 expanded as K err = c_g + [s | s^2] . [-2 w d | w]).
 
 Every candidate error lies within the stated bound of the exact FP64 error,
 and the accepted sets after the FP64 recheck are identical to the oracle's in
@@ -109,6 +109,22 @@ def test_infinite_statistic_falls_back_to_fp32_pass(Ctx, orc):
         assert ctx.distance_mode() == (2, 0)
     roff, ridx = orc.accept(orc.errors(data, se, stats, None), 1, 0.01)
     assert np.array_equal(off, roff) and np.array_equal(idx, ridx)
+
+
+def test_mode3_falls_back_to_mode2_for_long_rows(Ctx, orc):
+    """Mode 3 keeps a 256-gene tile of BF16 rows (4K values, rounded up) in
+    shared memory; beyond K = 96 it does not fit and the pass runs in mode 2."""
+    data, se, stats = _synthetic(3000, 40, 120, 8)
+    with Ctx(make_config("hour"), None) as ctx:
+        ctx.set_distance_mode(3)
+        off, idx, _ = ctx.select(data, se, stats, 1, 0.01, None)
+        assert ctx.distance_mode() == (3, 2)
+        e32, b0, b1, used = ctx.errors_candidate(data, se, stats)
+        assert used == 2
+    roff, ridx = orc.accept(orc.errors(data, se, stats, None), 1, 0.01)
+    assert np.array_equal(off, roff) and np.array_equal(idx, ridx)
+    E = np.minimum(_exact_unclipped(data, se, stats), 10.0)
+    assert (np.abs(e32 - E) <= b0[None, :] + b1 * E).all()
 
 
 @pytest.mark.parametrize("mode", (1, 2, 3))

@@ -52,7 +52,10 @@ def test_selection_shapes(Ctx, orc, mode, P, G, K, errors):
 def test_selection_nan_and_no_candidates(Ctx, orc, mode, errors):
     data, se, stats = _problem(400, 40, 24, 3)
     stats[::3] = np.nan                     # a third of the particles all-NaN
+    stats[1, 7] = np.nan                    # a particle with one NaN statistic
     data[5] = np.nan                        # a gene with NaN data
+    data[9, 2] = np.nan                     # a gene with one NaN statistic
+    se[12, 4] = np.nan                      # a gene with one NaN standard error
     with Ctx(make_config("hour"), None) as ctx:
         ctx.set_distance_mode(mode)
         off = _check(ctx, orc, data, se, stats, 0, 1e-12, errors)   # almost nothing accepted
