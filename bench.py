@@ -51,9 +51,12 @@ LANES_PER_SM = 128
 SMS = 152
 PER_MODEL_DEFAULT = 200_000  # 10^6 particles over the five models
 # DRAM bytes per (particle, cell) trajectory of the production SSA kernel,
-# measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum) on a
-# 10^4-particle x 2,000-cell launch whose count buffer exceeds L2; None until measured
-SSA_DRAM_BYTES_PER_TRAJECTORY = None
+# measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum, one pass) on
+# the 5 x 4,000-particle x 2,000-cell launch, whose 320 MB count buffer exceeds
+# L2: 326.0 MB read + 269.4 MB write over 4 x 10^7 trajectories (the initial
+# (u, G) pair in, the final counts out: 16 B algorithmic, part of the writes
+# still in L2 when the kernel ends)
+SSA_DRAM_BYTES_PER_TRAJECTORY = (326002688 + 269423104) / 4.0e7
 
 
 def parse():
