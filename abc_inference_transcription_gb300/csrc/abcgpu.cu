@@ -493,6 +493,7 @@ static int enqueue_simulate(abc_ctx* c, int model, const int32_t* d_models, cons
     st.seed = seed;
     st.stats = d_stats + p0 * K;
     st.captured = want_cells ? c->d_captured.p : nullptr;
+    st.fp32 = fp64 ? 0 : 1;
     CK(launch_stats(st, c->stream));
     CK(prof_mark(c));
   }

@@ -20,6 +20,7 @@ struct StatsArgs {
   uint64_t seed;
   double* stats;             // [P][K]
   int2* captured;            // optional [P][C]
+  int fp32 = 0;              // production mode: FP32 binomial capture (a different realisation)
 };
 
 struct SetupArgs {

@@ -244,6 +244,7 @@ extern "C" int abc_simulate_noalloc(const abc_config* cfg, int model, int64_t n_
   sta.seed = seed;
   sta.stats = d_stats;
   sta.captured = nullptr;
+  sta.fp32 = fp64 ? 0 : 1;
   NA_CK(launch_stats(sta, stream));
 
   int hs = 0;

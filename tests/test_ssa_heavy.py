@@ -11,7 +11,7 @@ BTRD at n p ~ 10^5).  Counts, captured counts, event counts, event-sequence
 hashes and the 53 statistics must be identical.
 
 FP32 production mode against the reference's own model, the moment ODE
-(scripts/model.jl:67-239): R replicate particles of one theta (distinct
+(scripts/model.jl:67-239) started at its periodic solution: R replicate particles of one theta (distinct
 random streams) on a table with N cells in every (condition, age) group and
 one capture efficiency.  Per statistic of scripts/abc_simulation.jl:23-46,
 the replicate mean must lie within 3 Monte Carlo standard errors of the
@@ -142,6 +142,20 @@ def family_z(z: np.ndarray) -> dict:
     return out
 
 
+def periodic_iv(orc, cfg, model: int, th: np.ndarray) -> np.ndarray:
+    """Start of the moment ODE at its periodic solution, in the order of
+    model.jl:74-86 (E G, E u, E l, Var G, Cov(G,u), Cov(G,l), Var u, Cov(u,l),
+    Var l), from the fixed point the SSA also starts from.  The reference's
+    transient_phase (model.jl:114-142) approaches the same point but stops at
+    a 1 % change per cycle, which for slow decay (gamma = 10^-2 / h) leaves its
+    means 3-5 x 10^-4 below it: about one Monte Carlo standard error at 1,024
+    replicates, a bias of the stopping rule, not of the simulation."""
+    S = cfg.n_steps
+    rec = orc.setup(cfg, model, th)
+    g0, u0, _, c0, v0 = rec[4 * S + 4:4 * S + 9]
+    return np.array([g0, u0, 0.0, g0 * (1.0 - g0), c0, 0.0, v0, 0.0, 0.0])
+
+
 FP32_THETAS = [
     (1, [0.5, 1.0, 20.0, 0.1, 0.7]),                          # scripts/model_realisation.jl:294-315
     (3, [0.1, 0.1, 30.0, 0.1, 0.1, 1.0, 15.0, 0.1, 0.7]),
@@ -164,7 +178,7 @@ def test_ssa_fp32_statistics_within_3_mc_se(Ctx, orc, model, rates):
         out = ctx.simulate_cells(model, np.repeat(th[None, :], R, axis=0), seed=41)
     st = out["stats"]
     cap = out["captured"].astype(np.float64)  # R x C x 2
-    raw = orc.moment_model(make_config("hour"), model, th, np.array([0, 0.5, 0, 0, 0, 0, 0, 0, 0.0]))["moments"]
+    raw = orc.moment_model(make_config("hour"), model, th, periodic_iv(orc, make_config("hour"), model, th))["moments"]
     mom = captured_moments(raw, b)
     ode = orc.stats_from_moments(make_config("hour"), mom, cells.age_dist)
     # statistics: replicate means vs the moment ODE
@@ -200,3 +214,43 @@ def test_ssa_fp32_statistics_within_3_mc_se(Ctx, orc, model, rates):
             json.dump(report, f)
     assert np.isfinite(z_stat).sum() >= 50, report
     assert (np.abs(z) > 3).mean() <= 0.01 and np.abs(z).max() <= 4.5, report
+
+
+@pytest.mark.parametrize("precision", [abi.FP32, abi.FP64])
+def test_capture_unbiased_given_counts(Ctx, precision):
+    """The binomial capture alone (model.jl:221-239, realised per cell), given
+    the simulated counts n and one capture efficiency b per cell: per (condition,
+    age) group and species, the sum of c - b n against its binomial standard
+    error, and the sum of (c - b n)^2 - b (1 - b) n against the standard error
+    of that sum (Var (X - np)^2 = npq + (2 n^2 - 6 n) p^2 q^2).  Counts from 0
+    to several 10^4 exercise both samplers (inversion below n b = 10, BTRD
+    above, in FP32 arithmetic in the production mode)."""
+    cfg = make_config("hour", precision=precision)
+    zs = []
+    for model, rates, b in ((1, [0.5, 1.0, 20.0, 0.1, 0.7], 0.3), (1, [0.05, 0.02, 300.0, 0.01, 0.5], 0.15),
+                            (4, [0.5, 0.5, 400.0, 630.0, 320.0, 800.0, 500.0, 1.0, 0.6], 0.7)):
+        cells = group_cells(200, b)
+        th = np.repeat(np.log10(np.array(rates))[None, :], 64, axis=0)
+        with Ctx(cfg, cells) as ctx:
+            out = ctx.simulate_cells(model, th, seed=77)
+        n = out["counts"].astype(np.float64)
+        c = out["captured"].astype(np.float64)
+        q = 1.0 - b
+        for j in range(11):
+            for a in range(5):
+                sel = (cells.cond == j) & (cells.age == a)
+                for sp in (0, 1):
+                    nn, cc = n[:, sel, sp].ravel(), c[:, sel, sp].ravel()
+                    var1 = (b * q * nn).sum()
+                    if var1 <= 0:
+                        assert (cc == 0).all()
+                        continue
+                    d = cc - b * nn
+                    zs.append(d.sum() / np.sqrt(var1))
+                    var2 = (nn * b * q + (2 * nn * nn - 6 * nn) * (b * q) ** 2).sum()
+                    zs.append(((d * d) - b * q * nn).sum() / np.sqrt(var2))
+    zs = np.array(zs)
+    assert zs.shape[0] > 400
+    # about 600 comparisons: by chance a couple beyond 3, none beyond 4.5
+    assert (np.abs(zs) > 3).mean() <= 0.01 and np.abs(zs).max() <= 4.5, (np.abs(zs).max(), (np.abs(zs) > 3).sum())
+    assert abs(zs.mean()) < 4.0 / np.sqrt(zs.shape[0]), zs.mean()
