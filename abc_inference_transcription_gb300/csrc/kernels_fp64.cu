@@ -2,6 +2,7 @@
 // fused capture + statistics kernel.  Built with -fmad=false: every FP64
 // result here is bit-identical to the FP64 CPU oracle.
 #include "kernels.h"
+#include "sampler32.cuh"
 
 namespace abc {
 
@@ -190,40 +191,41 @@ cudaError_t launch_ssa_fp64(const SsaArgs& a, int grid, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-// One thread per trajectory: the gene state from the first word of the
-// trajectory's main stream and the moment-matched first mRNA count
-// (initial_count, auxiliary stream), the draws traj_init makes.  Runs on
-// the FP64 pipe at full occupancy instead of inside the production kernel's
-// divergent refill path.
+// One thread per trajectory of the production mode: the gene state from the
+// first word of the trajectory's main stream and the moment-matched first
+// mRNA count (auxiliary stream), drawn from the distribution traj_init uses
+// in the FP64 mode with FP32 samplers.  Runs at full occupancy instead of
+// inside the production kernel's divergent refill path.
 __global__ void __launch_bounds__(256) init_state_kernel(SsaArgs A) {
-  const int64_t n = A.n_items;
-  for (int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; item < n;
-       item += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t pl = item / A.n_cells;
-    const int64_t ci = item - pl * A.n_cells;
+  const int64_t P = A.n_items / A.n_cells;
+  const int C = (int)A.n_cells;
+  for (int64_t pl = blockIdx.x; pl < P; pl += gridDim.x) {  // a block per particle, a thread per cell
     const PRec& R = A.rec[pl];
-    const uint32_t cell = A.cell_id[ci], particle = (uint32_t)(A.p_offset + pl);
-    Rng r;
-    rng_init(r, A.seed, ST_SSA, cell, particle);
-    uint32_t w0, w1;
-    rng_pair(r, w0, w1);
-    const int G = ((double)w0 * ABC_TWO_M32 < R.g0) ? 1 : 0;
-    int64_t u;
-    if (A.cfg.splicing) {
-      u = (int64_t)floor(R.u0 + 0.5);
-    } else {
-      Rng aux;
-      rng_init(aux, A.seed, ST_AUX, cell, particle);
-      u = initial_count(R, G, w1, aux);
+    const uint32_t particle = (uint32_t)(A.p_offset + pl);
+    for (int ci = threadIdx.x; ci < C; ci += blockDim.x) {
+      const uint32_t cell = A.cell_id[ci];
+      Rng r;
+      rng_init(r, A.seed, ST_SSA, cell, particle);
+      uint32_t w0, w1;
+      rng_pair(r, w0, w1);
+      const int G = ((double)w0 * ABC_TWO_M32 < R.g0) ? 1 : 0;
+      int u;
+      if (A.cfg.splicing) {
+        u = (int)fmin(floor(R.u0 + 0.5), 2147483647.0);
+      } else {
+        Rng aux;
+        rng_init(aux, A.seed, ST_AUX, cell, particle);
+        u = initial_count32(R, G, w1, aux);
+      }
+      A.counts[pl * A.n_cells + ci] = make_int2(u, G);
     }
-    A.counts[item] = make_int2((int)(u < 2147483647 ? u : 2147483647), G);
   }
 }
 
 cudaError_t launch_init_states(const SsaArgs& a, int sms, cudaStream_t s) {
-  if (a.n_items <= 0) return cudaSuccess;
-  const int64_t want = (a.n_items + 255) / 256, cap = (int64_t)sms * 16;
-  init_state_kernel<<<(unsigned)(want < cap ? want : cap), 256, 0, s>>>(a);
+  if (a.n_items <= 0 || a.n_cells <= 0) return cudaSuccess;
+  const int64_t P = a.n_items / a.n_cells, cap = (int64_t)sms * 16;
+  init_state_kernel<<<(unsigned)(P < cap ? P : cap), 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -244,113 +246,6 @@ __device__ __forceinline__ __int128 shfl_xor_i128(__int128 v, int o) {
   lo = __shfl_xor_sync(0xffffffffu, lo, o);
   hi = __shfl_xor_sync(0xffffffffu, hi, o);
   return (__int128)(((unsigned __int128)(unsigned long long)hi << 64) | (unsigned __int128)lo);
-}
-
-// ---------------------------------------------------------------------------
-// Binomial capture for the FP32 production mode: the same two methods as the
-// FP64 samplers above (inversion below n p = 10, Kachitvichyanukul &
-// Schmeiser 1988; BTRD above, Hormann 1993) with the per-draw arithmetic in
-// FP32, which runs at the full rate where the FP64 samplers are bound by
-// GB300's narrow FP64 pipe.  Only BTRD's final exact test (the log-density
-// comparison between its two squeezes, a small fraction of the draws) stays
-// in FP64, where (n + 1) log(...) needs the precision.  Counts are below 2^23
-// in this mode.  A different realisation than the FP64 mode's, drawn from the
-// same distribution.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ float u24open(uint32_t w) { return ((float)(w >> 8) + 0.5f) * 5.9604644775390625e-8f; }
-__device__ __forceinline__ float u24(uint32_t w) { return (float)(w >> 8) * 5.9604644775390625e-8f; }
-
-__device__ int binv32(Rng& rr, int n, float p) {
-  const float q = 1.0f - p;
-  const float s = p / q;
-  const float a = (float)(n + 1) * s;
-  const float r0 = expf((float)n * log1pf(-p));
-  uint32_t w[2] = {0u, 0u};
-  for (int it = 0; it < 64; ++it) {
-    if ((it & 1) == 0) rng_pair(rr, w[0], w[1]);
-    float u = u24(w[it & 1]);
-    float f = r0;
-    int x = 0;
-    for (;;) {
-      if (u < f) return x;
-      if (x >= n || x >= 110) break;
-      u = u - f;
-      x = x + 1;
-      f = f * (a / (float)x - s);
-    }
-  }
-  return (int)floorf((float)n * p + 0.5f);
-}
-
-__device__ int btrd32(Rng& rr, int n, float p) {
-  const float nd = (float)n;
-  const float q = 1.0f - p;
-  const float m = floorf((nd + 1.0f) * p);
-  const float r = p / q;
-  const float nr = (nd + 1.0f) * r;
-  const float npq = (nd * p) * q;
-  const float sq = sqrtf(npq);
-  const float b = 1.15f + 2.53f * sq;
-  const float a = (-0.0873f + 0.0248f * b) + 0.01f * p;
-  const float c = nd * p + 0.5f;
-  const float alpha = (2.83f + 5.1f / b) * sq;
-  const float vr = 0.92f - 4.2f / b;
-  const float urvr = 0.86f * vr;
-  for (int it = 0; it < 1000; ++it) {
-    uint32_t w0, w1;
-    rng_pair(rr, w0, w1);
-    float v = u24open(w0);
-    float u;
-    if (v <= urvr) {
-      u = v / vr - 0.43f;
-      return (int)floorf(((2.0f * a) / (0.5f - fabsf(u)) + b) * u + c);
-    }
-    if (v >= vr) {
-      u = u24open(w1) - 0.5f;
-    } else {
-      u = v / vr - 0.93f;
-      u = (u < 0.0f ? -0.5f : 0.5f) - u;
-      v = u24open(w1) * vr;
-    }
-    const float us = 0.5f - fabsf(u);
-    const float kd = floorf(((2.0f * a) / us + b) * u + c);
-    if (kd < 0.0f || kd > nd) continue;
-    v = (v * alpha) / (a / (us * us) + b);
-    const float km = fabsf(kd - m);
-    if (km <= 15.0f) {
-      float f = 1.0f;
-      if (m < kd) {
-        for (float i = m + 1.0f; i <= kd; i += 1.0f) f = f * (nr / i - r);
-      } else if (m > kd) {
-        for (float i = kd + 1.0f; i <= m; i += 1.0f) v = v * (nr / i - r);
-      }
-      if (v <= f) return (int)kd;
-      continue;
-    }
-    const float lv = logf(v);
-    const float rho = (km / npq) * (((km / 3.0f + 0.625f) * km + 0.16666667f) / npq + 0.5f);
-    const float t = (-km * km) / (2.0f * npq);
-    if (lv < t - rho) return (int)kd;
-    if (lv > t + rho) continue;
-    // exact test in FP64 (log f(k) - log f(m) against log v)
-    const double ndd = (double)n, pdd = (double)p, rd = pdd / (1.0 - pdd), md = (double)m, kdd = (double)kd;
-    const double nm = (ndd - md) + 1.0, nk = (ndd - kdd) + 1.0;
-    const double h = ((md + 0.5) * xlog((md + 1.0) / (rd * nm)) + stirling_fc(md)) + stirling_fc(ndd - md);
-    const double bound = (((h + (ndd + 1.0) * xlog(nm / nk)) + (kdd + 0.5) * xlog((nk * rd) / (kdd + 1.0))) -
-                          stirling_fc(kdd)) - stirling_fc(ndd - kdd);
-    if ((double)lv <= bound) return (int)kd;
-  }
-  return (int)floorf(nd * p + 0.5f);
-}
-
-__device__ __forceinline__ int64_t binomial32(Rng& r, int64_t n, double p) {
-  if (n <= 0 || !(p > 0.0)) return 0;
-  if (p >= 1.0) return n;
-  const bool flip = p > 0.5;
-  const float pp = (float)(flip ? 1.0 - p : p);
-  const int ni = (int)n;
-  const int k = ((float)ni * pp < 10.0f) ? binv32(r, ni, pp) : btrd32(r, ni, pp);
-  return flip ? n - k : k;
 }
 
 template <bool CAP32>

@@ -18,8 +18,9 @@ the replicate mean must lie within 3 Monte Carlo standard errors of the
 moment-ODE statistic, and per group the pooled mean, variance and covariance
 of the captured counts within 3 standard errors of their exact values.  With
 several hundred comparisons per theta a few |z| > 3 are expected by chance
-(0.27 % each), so the test allows 1 % of them beyond 3 and none beyond 4.5;
-the seeds are fixed, so the outcome is reproducible.
+(0.27 % each): the test allows the count that independent comparisons exceed
+with probability 10^-3 (5 of 328) and none beyond 4.5; the seeds are fixed,
+so the outcome is reproducible.
 """
 import json
 import math
@@ -142,6 +143,17 @@ def family_z(z: np.ndarray) -> dict:
     return out
 
 
+def allowed_beyond_3(n: int, alpha: float = 1e-3) -> int:
+    """Smallest k with P(X > k) < alpha for X ~ Bin(n, 0.0027), the number of
+    |z| > 3 among n independent standard normal z under exact agreement."""
+    p, k, cdf = 0.0026997960632601866, 0, 0.0
+    while True:
+        cdf += math.comb(n, k) * p ** k * (1.0 - p) ** (n - k)
+        if 1.0 - cdf < alpha:
+            return k
+        k += 1
+
+
 def periodic_iv(orc, cfg, model: int, th: np.ndarray) -> np.ndarray:
     """Start of the moment ODE at its periodic solution, in the order of
     model.jl:74-86 (E G, E u, E l, Var G, Cov(G,u), Cov(G,l), Var u, Cov(u,l),
@@ -213,7 +225,7 @@ def test_ssa_fp32_statistics_within_3_mc_se(Ctx, orc, model, rates):
         with open(os.path.join(os.environ["ABC_REPORT_DIR"], f"fp32_stats_{model}_{int(rates[2])}_{rates[-2]:g}.json"), "w") as f:
             json.dump(report, f)
     assert np.isfinite(z_stat).sum() >= 50, report
-    assert (np.abs(z) > 3).mean() <= 0.01 and np.abs(z).max() <= 4.5, report
+    assert (np.abs(z) > 3).sum() <= allowed_beyond_3(z.shape[0]) and np.abs(z).max() <= 4.5, report
 
 
 @pytest.mark.parametrize("precision", [abi.FP32, abi.FP64])
