@@ -252,25 +252,47 @@ __global__ void __launch_bounds__(256) refine_kernel(const unsigned int* hist, i
   }
 }
 
-// Keep candidates with e <= Xt[g] (warp-aggregated append).
-__global__ void cand_filter_kernel(const Cand* cand, const float* e, int64_t n, const float* Xt, Cand* out,
-                                   unsigned long long* count) {
-  const int lane = threadIdx.x & 31;
-  for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x; i0 < n; i0 += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = i0 + threadIdx.x;
-    bool keep = false;
-    Cand cd;
-    if (i < n) {
-      cd = cand[i];
-      keep = e[i] <= Xt[cd.g];
+// Keep candidates with e <= Xt[g].  A block takes 4 x 256 candidates per
+// iteration and appends its kept ones with one global atomic (positions from
+// the warps' ballots), so the shared output counter sees one atomic per 1,024
+// candidates instead of one per warp.
+constexpr int kFilterItems = 4;
+__global__ void __launch_bounds__(256) cand_filter_kernel(const Cand* cand, const float* e, int64_t n, const float* Xt,
+                                                          Cand* out, unsigned long long* count) {
+  __shared__ unsigned int wc[kFilterItems * 8];
+  __shared__ unsigned long long base;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t per = (int64_t)kFilterItems * blockDim.x;
+  for (int64_t i0 = (int64_t)blockIdx.x * per; i0 < n; i0 += (int64_t)gridDim.x * per) {
+    bool keep[kFilterItems];
+    Cand cd[kFilterItems];
+    unsigned m[kFilterItems];
+#pragma unroll
+    for (int j = 0; j < kFilterItems; ++j) {
+      const int64_t i = i0 + (int64_t)j * blockDim.x + threadIdx.x;
+      keep[j] = false;
+      if (i < n) {
+        cd[j] = cand[i];
+        keep[j] = e[i] <= Xt[cd[j].g];
+      }
+      m[j] = __ballot_sync(0xffffffffu, keep[j]);
+      if (lane == 0) wc[j * 8 + warp] = __popc(m[j]);
     }
-    const unsigned m = __ballot_sync(0xffffffffu, keep);
-    if (m) {
-      unsigned long long base = 0;
-      if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(m));
-      base = __shfl_sync(0xffffffffu, base, 0);
-      if (keep) out[base + __popc(m & ((1u << lane) - 1u))] = cd;
+    __syncthreads();
+    if (threadIdx.x == 0) {  // exclusive scan of the 32 warp counts, one reservation
+      unsigned int run = 0;
+      for (int q = 0; q < kFilterItems * 8; ++q) {
+        const unsigned int v = wc[q];
+        wc[q] = run;
+        run += v;
+      }
+      base = run ? atomicAdd(count, (unsigned long long)run) : 0ull;
     }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kFilterItems; ++j)
+      if (keep[j]) out[base + wc[j * 8 + warp] + __popc(m[j] & ((1u << lane) - 1u))] = cd[j];
+    __syncthreads();  // wc and base are rewritten by the next iteration
   }
 }
 

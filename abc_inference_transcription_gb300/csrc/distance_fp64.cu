@@ -435,6 +435,47 @@ __global__ void gene_count_kernel(const Cand* cand, int64_t n, int64_t* gcount) 
     atomicAdd((unsigned long long*)&gcount[cand[i].g], 1ull);
 }
 
+// The same count with a per-block histogram in shared memory (G counters):
+// one global atomic per (block, gene) instead of one per candidate, which
+// all land on a few thousand addresses.
+__global__ void __launch_bounds__(256) gene_count_smem_kernel(const Cand* cand, int64_t n, int G, int64_t chunk,
+                                                              int64_t* gcount) {
+  extern __shared__ unsigned int h[];
+  for (int g = threadIdx.x; g < G; g += blockDim.x) h[g] = 0u;
+  __syncthreads();
+  const int64_t b0 = (int64_t)blockIdx.x * chunk, b1 = b0 + chunk < n ? b0 + chunk : n;
+  for (int64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) atomicAdd(&h[cand[i].g], 1u);
+  __syncthreads();
+  for (int g = threadIdx.x; g < G; g += blockDim.x)
+    if (h[g]) atomicAdd((unsigned long long*)&gcount[g], (unsigned long long)h[g]);
+}
+
+// Scatter of a contiguous chunk per block: local counts per gene, one global
+// reservation per (block, gene), then positions from shared-memory atomics.
+__global__ void __launch_bounds__(256) scatter_smem_kernel(const Cand* cand, int64_t n, int G, int64_t chunk,
+                                                           const int64_t* goff, unsigned long long* cursor,
+                                                           int32_t* sp, int32_t* sg) {
+  extern __shared__ unsigned long long sb[];  // G reserved bases, then G local counters
+  unsigned int* cnt = reinterpret_cast<unsigned int*>(sb + G);
+  for (int g = threadIdx.x; g < G; g += blockDim.x) cnt[g] = 0u;
+  __syncthreads();
+  const int64_t b0 = (int64_t)blockIdx.x * chunk, b1 = b0 + chunk < n ? b0 + chunk : n;
+  for (int64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) atomicAdd(&cnt[cand[i].g], 1u);
+  __syncthreads();
+  for (int g = threadIdx.x; g < G; g += blockDim.x) {
+    const unsigned int c = cnt[g];
+    sb[g] = c ? (unsigned long long)goff[g] + atomicAdd(&cursor[g], (unsigned long long)c) : 0ull;
+    cnt[g] = 0u;
+  }
+  __syncthreads();
+  for (int64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
+    const Cand c = cand[i];
+    const unsigned long long pos = sb[c.g] + atomicAdd(&cnt[c.g], 1u);
+    sp[pos] = c.p;
+    sg[pos] = c.g;
+  }
+}
+
 __global__ void __launch_bounds__(1024) scan_kernel(const int64_t* cnt, int64_t G, int64_t* off) {
   __shared__ int64_t part[1024];
   const int64_t per = (G + 1023) / 1024;
@@ -571,14 +612,27 @@ cudaError_t launch_dist_group(const Cand* cand, int64_t n, int64_t G, int64_t* g
   if (err) return err;
   err = cudaMemsetAsync(gcursor, 0, sizeof(unsigned long long) * (size_t)G, s);
   if (err) return err;
+  // shared-memory versions while G counters (and G reservations) fit in 48 KB
+  const bool smem = G <= 4096;
+  const int64_t chunk = 16384;  // candidates per block: ~2 G global atomics per 16,384 candidates at most
+  const int64_t nb = (n + chunk - 1) / chunk;
   if (n > 0) {
-    int blocks = (int)((n + 255) / 256 < 65536 ? (n + 255) / 256 : 65536);
-    gene_count_kernel<<<blocks, 256, 0, s>>>(cand, n, gcount);
+    if (smem) {
+      gene_count_smem_kernel<<<(unsigned)nb, 256, sizeof(unsigned int) * (size_t)G, s>>>(cand, n, (int)G, chunk,
+                                                                                            gcount);
+    } else {
+      int blocks = (int)((n + 255) / 256 < 65536 ? (n + 255) / 256 : 65536);
+      gene_count_kernel<<<blocks, 256, 0, s>>>(cand, n, gcount);
+    }
   }
   scan_kernel<<<1, 1024, 0, s>>>(gcount, G, goff);
   if (n > 0) {
-    int blocks = (int)((n + 255) / 256 < 65536 ? (n + 255) / 256 : 65536);
-    scatter_kernel<<<blocks, 256, 0, s>>>(cand, n, goff, gcursor, sp, sg);
+    if (smem) {
+      scatter_smem_kernel<<<(unsigned)nb, 256, 12 * (size_t)G, s>>>(cand, n, (int)G, chunk, goff, gcursor, sp, sg);
+    } else {
+      int blocks = (int)((n + 255) / 256 < 65536 ? (n + 255) / 256 : 65536);
+      scatter_kernel<<<blocks, 256, 0, s>>>(cand, n, goff, gcursor, sp, sg);
+    }
   }
   return cudaGetLastError();
 }

@@ -847,19 +847,21 @@ __global__ void tc_y_kernel(const float* X, const double* cg64, int64_t G, int K
   Y[g] = y;
 }
 
-// Concatenate the per-CTA segments: out[off_b + i] = seg_b[i].
+// Concatenate the per-CTA segments: out[off_b + i] = seg_b[i], segment b in
+// blockIdx.y, its entries spread over the gridDim.x blocks of that row.
 __global__ void tc_gather_kernel(const Cand* seg, const float* seg_e, const unsigned* count, int n_seg,
                                  int64_t seg_cap, const float* cg, float invK, Cand* out, float* out_e) {
   __shared__ int64_t off;
-  const int b = blockIdx.x;
-  if (threadIdx.x == 0) {
-    int64_t o = 0;
-    for (int i = 0; i < b; ++i) o += count[i];
-    off = o;
+  const int b = blockIdx.y;
+  if (threadIdx.x < 32) {  // off_b = sum of the earlier segments' counts, one warp
+    unsigned long long o = 0;
+    for (int i = threadIdx.x; i < b; i += 32) o += count[i];
+    for (int d = 16; d > 0; d >>= 1) o += __shfl_xor_sync(0xffffffffu, o, d);
+    if (threadIdx.x == 0) off = (int64_t)o;
   }
   __syncthreads();
   const int64_t n = count[b];
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const Cand cd = seg[(int64_t)b * seg_cap + i];
     out[off + i] = cd;
     out_e[off + i] = fminf((seg_e[(int64_t)b * seg_cap + i] + cg[cd.g]) * invK, 10.0f);
@@ -1017,7 +1019,8 @@ cudaError_t launch_dist_tc(int mode, const void* A, const void* B, const TcArgs&
 cudaError_t launch_tc_gather(const Cand* seg, const float* seg_e, const unsigned* count, int n_seg, int64_t seg_cap,
                              const float* cg, int K, Cand* out, float* out_e, cudaStream_t s) {
   if (n_seg <= 0) return cudaSuccess;
-  tc_gather_kernel<<<n_seg, 256, 0, s>>>(seg, seg_e, count, n_seg, seg_cap, cg, 1.0f / (float)K, out, out_e);
+  tc_gather_kernel<<<dim3(32, (unsigned)n_seg), 256, 0, s>>>(seg, seg_e, count, n_seg, seg_cap, cg, 1.0f / (float)K,
+                                                              out, out_e);
   return cudaGetLastError();
 }
 
