@@ -14,9 +14,8 @@
 //
 // Host code must not use the array's name as a device address: it is only a
 // host-side stand-in.  The first call on each device (with that device
-// current) looks up the device address with cudaGetSymbolAddress; make that
-// first call before any stream capture.  The address is kept for the rest of
-// the process: calls after a cudaDeviceReset of that device are not supported
+// current) looks up the device address with cudaGetSymbolAddress.  The
+// address is kept for the rest of the process: calls after a cudaDeviceReset of that device are not supported
 // (the module, and with it the array, is reloaded at a new address).  All calls share the one array and
 // it keeps the last call's contents: the counter, event totals and status
 // word are cleared on every call, everything else is overwritten.  Calls that

@@ -161,9 +161,9 @@ int abc_simulate_batch_device(abc_ctx* ctx, const int32_t* d_models, const doubl
  * by every GPU that loads it until exit; particles x cells x 8 bytes plus
  * about 500 bytes per particle must fit, else ABC_ERR_INVALID (e.g. up to
  * ~4,000 particles with 2,000 cells).  The first call on a device looks up
- * the array's device address (cudaGetSymbolAddress) and should come before
- * any stream capture; the address is kept for the rest of the process, so
- * calls after a cudaDeviceReset of that device are not supported.  Calls
+ * the array's device address (cudaGetSymbolAddress); the address is kept for
+ * the rest of the process, so calls after a cudaDeviceReset of that device
+ * are not supported.  Calls
  * share the array: calls that overlap on the GPU race, so serialise them. */
 int abc_simulate_noalloc(const abc_config* cfg, int model, int64_t n_cells, const int32_t* cell_cond,
                          const int32_t* cell_age, const double* cell_beta, const double* age_dist,
