@@ -76,16 +76,19 @@ __global__ void setup_kernel(SetupArgs A) {
     R.cost = 1.0;
   }
   A.rec[p] = R;
+  // rates in log2 units (times log2 e), so the production kernel's waiting
+  // time is -log2(U) / a0 without a conversion per event
+  constexpr double kL2E = 1.4426950408889634;
   PRecF F;
   for (int k = 0; k < kMaxSteps; ++k) {
-    F.kon[k] = (float)R.kon[k];
-    F.alp[k] = (float)R.alp[k];
-    F.gam[k] = (float)R.gam[k];
-    F.amax[k] = (float)R.amax[k];
+    F.kon[k] = (float)(R.kon[k] * kL2E);
+    F.alp[k] = (float)(R.alp[k] * kL2E);
+    F.gam[k] = (float)(R.gam[k] * kL2E);
+    F.amax[k] = (float)(R.amax[k] * kL2E);
   }
-  F.koff = (float)R.koff;
+  F.koff = (float)(R.koff * kL2E);
   F.lam = (float)R.lam;
-  F.beta = (float)R.beta;
+  F.beta = (float)(R.beta * kL2E);
   F.scal = (float)R.scal;
   if (A.fp32) {
     // rates beyond the FP32 range would stall the production kernel's clock

@@ -72,7 +72,9 @@ struct PRec {
   double cost;        // expected fired events per trajectory (work estimate)
 };
 
-// FP32 copy of the rates for the production SSA.
+// FP32 copy of the rates for the production SSA, in log2 units: every rate
+// (kon, alp, gam, amax, koff, beta) times log2 e; lam (a probability) and
+// scal (an exponent) as they are.
 struct PRecF {
   float kon[kMaxSteps], alp[kMaxSteps], gam[kMaxSteps], amax[kMaxSteps];
   float koff, lam, beta, scal;

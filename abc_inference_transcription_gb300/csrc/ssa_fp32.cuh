@@ -207,17 +207,20 @@ __device__ __forceinline__ bool ev_step(LaneF<GRID>& s, float koff, float beta, 
     top = fmaf(s.gam, s.ls, c4);  // decay of labelled spliced
   }
   const float a0 = fmaf(G, s.amax, top);  // + transcription proposals (thinning bound) when on
-  // waiting time: U1 in (0, 1] from the low 23 bits of wt (mantissa fill)
+  // waiting time: U1 in (0, 1] from the low 23 bits of wt (mantissa fill);
+  // the rates are in log2 units, so -log2(U1) / a0 is the time
   const float U1 = 2.0f - __uint_as_float(0x3F800000u | (wt & 0x7FFFFFu));
-  const float tau = __fdividef(-__logf(U1), a0);  // a0 = 0 gives inf or NaN: a breakpoint
+  const float tau = __fdividef(-__log2f(U1), a0);  // a0 = 0 gives inf or NaN: a breakpoint
   const float y = tau - s.comp;
   const float tt = s.el + y;
-  // no branch: at a breakpoint (ok = 0) every update below is multiplied by
-  // zero or selected away, so the lane's state is unchanged
+  // no branch: at a breakpoint (ok = 0) every update of the counts, G and the
+  // counters below is multiplied by zero, so the lane's state is unchanged;
+  // the clock (el, comp) may advance past the interval, since the breakpoint
+  // that follows starts a new interval at el = comp = 0
   const bool ok = tt < len;
   const float okf = ok ? 1.0f : 0.0f;
-  s.comp = ok ? (tt - s.el) - y : s.comp;
-  s.el = ok ? tt : s.el;
+  s.comp = (tt - s.el) - y;
+  s.el = tt;
   s.evf += okf;
   // channel: 32-bit uniform times a0
   const float r = __uint2float_rn(wc) * (a0 * 2.3283064365386963e-10f);
