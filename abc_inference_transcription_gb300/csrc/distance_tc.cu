@@ -714,6 +714,9 @@ __global__ void tc_prep_rows_kernel(const double* stats, int64_t P, int K, int H
   const int64_t ld = ld_;
   const int R = K <= 32 * kPrepLoads ? (32 * kPrepLoads) / K < 4 ? (32 * kPrepLoads) / K : 4 : 1;
   unsigned inf = 0, mx = 0;
+  // pairs of statistics per lane: BF16, K even (rows and the lo / s^2 offsets
+  // stay 4-byte aligned in A), and 16-byte aligned statistics rows
+  const bool pairs = BF && (K & 1) == 0 && ((reinterpret_cast<uintptr_t>(stats) & 15) == 0);
   for (int64_t p0 = ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * R; p0 < P; p0 += warps * R) {
     const int rows = P - p0 < R ? (int)(P - p0) : R;
     uint32_t nanr = 0;  // bit r: row p0 + r holds a NaN statistic
@@ -735,6 +738,50 @@ __global__ void tc_prep_rows_kernel(const double* stats, int64_t P, int K, int H
         if (fabsf(sv) == INFINITY || fabsf(s2) == INFINITY) inf = 1u;
         if (s2 == s2) mx = max(mx, __float_as_uint(s2));
         if (sv != sv) nanr = 1u;
+      }
+    } else if (BF && pairs) {
+      // BF16 with K even and 16-byte aligned rows: a lane takes two adjacent
+      // statistics of one row (flat index f = 2 (lane + 32 t)) with one 16-byte
+      // load and stores each operand pair as one 4-byte bf16x2
+      const int n = rows * K;
+      double2 v[kPrepLoads / 2];
+      {
+        const double2* src = reinterpret_cast<const double2*>(stats + p0 * K);
+#pragma unroll
+        for (int t = 0; t < kPrepLoads / 2; ++t) {
+          const int f = 2 * (lane + 32 * t);
+          v[t] = f < n ? __ldg(src + (f >> 1)) : make_double2(0.0, 0.0);
+        }
+      }
+      int r = (2 * lane) / K, k = 2 * lane - ((2 * lane) / K) * K;
+#pragma unroll
+      for (int t = 0; t < kPrepLoads / 2; ++t) {
+        if (2 * (lane + 32 * t) < n) {
+          const float s0 = rn32_bits(v[t].x), s1 = rn32_bits(v[t].y);
+          const float q0 = s0 * s0, q1 = s1 * s1;
+          float h1a, l1a, h2a, l2a, h1b, l1b, h2b, l2b;
+          split_bf16f(s0, h1a, l1a);
+          split_bf16f(q0, h2a, l2a);
+          split_bf16f(s1, h1b, l1b);
+          split_bf16f(q1, h2b, l2b);
+          __nv_bfloat162* row = reinterpret_cast<__nv_bfloat162*>(reinterpret_cast<__nv_bfloat16*>(A) + (p0 + r) * ld);
+          row[k >> 1] = __floats2bfloat162_rn(h1a, h1b);  // the values are BF16: exact
+          row[(K + k) >> 1] = __floats2bfloat162_rn(h2a, h2b);
+          if (NH == 2) {
+            row[(H + k) >> 1] = __floats2bfloat162_rn(l1a, l1b);
+            row[(H + K + k) >> 1] = __floats2bfloat162_rn(l2a, l2b);
+          }
+          if (fabsf(s0) == INFINITY || fabsf(q0) == INFINITY || fabsf(s1) == INFINITY || fabsf(q1) == INFINITY)
+            inf = 1u;
+          if (q0 == q0) mx = max(mx, __float_as_uint(q0));
+          if (q1 == q1) mx = max(mx, __float_as_uint(q1));
+          if (s0 != s0 || s1 != s1) nanr |= 1u << r;
+        }
+        k += 64;
+        while (k >= K) {
+          k -= K;
+          ++r;
+        }
       }
     } else {
       // flat index f = lane + 32 t over rows x K, (r, k) = divmod(f, K)
