@@ -66,6 +66,7 @@ struct abc_ctx {
   DBuf<int32_t> d_cond, d_age, d_gstart;
   DBuf<uint32_t> d_id;
   DBuf<double> d_beta, d_age_dist;
+  DBuf<float> d_beta32;  // capture efficiencies in FP32 for the production mode's capture
   // simulation workspace
   DBuf<double> d_theta, d_stats;
   DBuf<int32_t> d_models;
@@ -232,7 +233,7 @@ int abc_destroy(abc_ctx* c) {
   cudaStreamSynchronize(c->stream);
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   c->d_cond.release(); c->d_age.release(); c->d_gstart.release(); c->d_id.release();
-  c->d_beta.release(); c->d_age_dist.release(); c->d_theta.release(); c->d_stats.release();
+  c->d_beta.release(); c->d_beta32.release(); c->d_age_dist.release(); c->d_theta.release(); c->d_stats.release();
   c->d_models.release(); c->d_order.release(); c->d_ohist.release(); c->d_rec.release(); c->d_recf.release(); c->d_counts.release(); c->d_captured.release();
   c->d_events.release(); c->d_hash.release(); c->d_misc.release(); c->d_status.release();
   c->d_data.release(); c->d_se.release(); c->d_sel_stats.release(); c->d_se64.release(); c->d_sg.release();
@@ -316,12 +317,15 @@ int abc_set_cells(abc_ctx* c, int64_t n_cells, const int32_t* cell_cond, const i
   CK(c->d_age.ensure(n_cells));
   CK(c->d_id.ensure(n_cells));
   CK(c->d_beta.ensure(n_cells));
+  CK(c->d_beta32.ensure(n_cells));
   CK(c->d_gstart.ensure(NG + 1));
   CK(c->d_age_dist.ensure(NG));
   CK(cudaMemcpy(c->d_cond.p, hc.data(), sizeof(int32_t) * n_cells, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(c->d_age.p, ha.data(), sizeof(int32_t) * n_cells, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(c->d_id.p, hid.data(), sizeof(uint32_t) * n_cells, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(c->d_beta.p, hb.data(), sizeof(double) * n_cells, cudaMemcpyHostToDevice));
+  std::vector<float> hb32(hb.begin(), hb.end());
+  CK(cudaMemcpy(c->d_beta32.p, hb32.data(), sizeof(float) * n_cells, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(c->d_gstart.p, gs.data(), sizeof(int32_t) * (NG + 1), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(c->d_age_dist.p, age_dist, sizeof(double) * NG, cudaMemcpyHostToDevice));
   c->perm = perm;
@@ -494,6 +498,7 @@ static int enqueue_simulate(abc_ctx* c, int model, const int32_t* d_models, cons
     st.stats = d_stats + p0 * K;
     st.captured = want_cells ? c->d_captured.p : nullptr;
     st.fp32 = fp64 ? 0 : 1;
+    st.beta32 = c->d_beta32.p;
     CK(launch_stats(st, c->stream));
     CK(prof_mark(c));
   }

@@ -21,6 +21,7 @@ struct StatsArgs {
   double* stats;             // [P][K]
   int2* captured;            // optional [P][C]
   int fp32 = 0;              // production mode: FP32 binomial capture (a different realisation)
+  const float* beta32 = nullptr;  // [C] the capture efficiencies in FP32 (production mode)
 };
 
 struct SetupArgs {

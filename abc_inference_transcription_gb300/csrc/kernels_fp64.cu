@@ -202,8 +202,18 @@ cudaError_t launch_ssa_fp64(const SsaArgs& a, int grid, cudaStream_t s) {
 __global__ void __launch_bounds__(256) init_state_kernel(SsaArgs A) {
   const int64_t P = A.n_items / A.n_cells;
   const int C = (int)A.n_cells;
+  __shared__ float mom[5];  // the particle's g0, u0, c0, v0 in FP32, and the rounded mean count
   for (int64_t pl = blockIdx.x; pl < P; pl += gridDim.x) {  // a block per particle, a thread per cell
-    const PRec& R = A.rec[pl];
+    if (threadIdx.x == 0) {  // the FP64 -> FP32 conversions once per particle, not per cell
+      const PRec& R = A.rec[pl];
+      mom[0] = (float)R.g0;
+      mom[1] = (float)R.u0;
+      mom[2] = (float)R.c0;
+      mom[3] = (float)R.v0;
+      mom[4] = (float)fmin(floor(R.u0 + 0.5), 1.0e9);  // far above the count limit (2^23), reported there
+    }
+    __syncthreads();
+    const float g0 = mom[0], u0 = mom[1], c0 = mom[2], v0 = mom[3], ur = mom[4];
     const uint32_t particle = (uint32_t)(A.p_offset + pl);
     for (int ci = threadIdx.x; ci < C; ci += blockDim.x) {
       const uint32_t cell = A.cell_id[ci];
@@ -211,17 +221,18 @@ __global__ void __launch_bounds__(256) init_state_kernel(SsaArgs A) {
       rng_init(r, A.seed, ST_SSA, cell, particle);
       uint32_t w0, w1;
       rng_pair(r, w0, w1);
-      const int G = ((double)w0 * ABC_TWO_M32 < R.g0) ? 1 : 0;
+      const int G = u24(w0) < g0 ? 1 : 0;
       int u;
       if (A.cfg.splicing) {
-        u = (int)fmin(floor(R.u0 + 0.5), 2147483647.0);
+        u = (int)ur;
       } else {
         Rng aux;
         rng_init(aux, A.seed, ST_AUX, cell, particle);
-        u = initial_count32(R, G, w1, aux);
+        u = initial_count32(g0, u0, c0, v0, G, w1, aux);
       }
       A.counts[pl * A.n_cells + ci] = make_int2(u, G);
     }
+    __syncthreads();  // mom is rewritten for the next particle
   }
 }
 
@@ -270,8 +281,15 @@ __global__ void __launch_bounds__(256) stats_kernel(StatsArgs A) {
         int2 c = cnt[i];
         Rng r;
         rng_init(r, A.seed, ST_CAPTURE, A.cell_id[i], pg);
-        long long cu = CAP32 ? binomial32(r, c.x, A.beta[i]) : binomial(r, c.x, A.beta[i]);
-        long long cl = CAP32 ? binomial32(r, c.y, A.beta[i]) : binomial(r, c.y, A.beta[i]);
+        long long cu, cl;
+        if (CAP32) {  // FP32 efficiencies: no FP64-pipe work per cell
+          const float b32 = A.beta32[i];
+          cu = binomial32(r, c.x, b32);
+          cl = binomial32(r, c.y, b32);
+        } else {
+          cu = binomial(r, c.x, A.beta[i]);
+          cl = binomial(r, c.y, A.beta[i]);
+        }
         if (A.captured) A.captured[p * A.n_cells + i] = make_int2((int)cu, (int)cl);
         su += cu;
         sl += cl;

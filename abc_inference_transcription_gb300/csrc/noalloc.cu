@@ -101,6 +101,7 @@ extern "C" int abc_simulate_noalloc(const abc_config* cfg, int model, int64_t n_
   const size_t o_age = off;    off = align256(off + sizeof(int32_t) * C);
   const size_t o_id = off;     off = align256(off + sizeof(uint32_t) * C);
   const size_t o_beta = off;   off = align256(off + sizeof(double) * C);
+  const size_t o_beta32 = off; off = align256(off + sizeof(float) * C);
   const size_t o_gs = off;     off = align256(off + sizeof(int32_t) * (NG + 1));
   const size_t o_w = off;      off = align256(off + sizeof(double) * NG);
   const size_t o_rec = off;    off = align256(off + sizeof(PRec) * (size_t)P);
@@ -147,6 +148,7 @@ extern "C" int abc_simulate_noalloc(const abc_config* cfg, int model, int64_t n_
   int32_t* d_age = (int32_t*)(S + o_age);
   uint32_t* d_id = (uint32_t*)(S + o_id);
   double* d_beta = (double*)(S + o_beta);
+  float* d_beta32 = (float*)(S + o_beta32);
   int32_t* d_gs = (int32_t*)(S + o_gs);
   double* d_w = (double*)(S + o_w);
   PRec* d_rec = (PRec*)(S + o_rec);
@@ -161,6 +163,8 @@ extern "C" int abc_simulate_noalloc(const abc_config* cfg, int model, int64_t n_
   NA_CK(cudaMemcpyAsync(d_age, ha.data(), sizeof(int32_t) * C, cudaMemcpyHostToDevice, stream));
   NA_CK(cudaMemcpyAsync(d_id, hid.data(), sizeof(uint32_t) * C, cudaMemcpyHostToDevice, stream));
   NA_CK(cudaMemcpyAsync(d_beta, hb.data(), sizeof(double) * C, cudaMemcpyHostToDevice, stream));
+  std::vector<float> hb32(hb.begin(), hb.end());
+  NA_CK(cudaMemcpyAsync(d_beta32, hb32.data(), sizeof(float) * C, cudaMemcpyHostToDevice, stream));
   NA_CK(cudaMemcpyAsync(d_gs, gs.data(), sizeof(int32_t) * (NG + 1), cudaMemcpyHostToDevice, stream));
   NA_CK(cudaMemcpyAsync(d_w, age_dist, sizeof(double) * NG, cudaMemcpyHostToDevice, stream));
   // what must start at zero: work counter, event totals, status word
@@ -244,6 +248,7 @@ extern "C" int abc_simulate_noalloc(const abc_config* cfg, int model, int64_t n_
   sta.stats = d_stats;
   sta.captured = nullptr;
   sta.fp32 = fp64 ? 0 : 1;
+  sta.beta32 = d_beta32;
   NA_CK(launch_stats(sta, stream));
 
   int hs = 0;

@@ -10,15 +10,39 @@
 
 namespace abc {
 
+// Stirling-series remainder log k! - [(k + 1/2) log(k + 1) - (k + 1) + log(2 pi)/2]
+// in FP32 (stirling_fc of common.cuh: the table below 10, the series above).
+__device__ __forceinline__ float stirling_fc32(float k) {
+  if (k < 10.0f) {
+    switch ((int)k) {
+      case 0: return 0.08106146679532726f;
+      case 1: return 0.0413406959554093f;
+      case 2: return 0.02767792568499834f;
+      case 3: return 0.020790672103765093f;
+      case 4: return 0.016644691189821193f;
+      case 5: return 0.013876128823070748f;
+      case 6: return 0.01189670994589177f;
+      case 7: return 0.010411265261972096f;
+      case 8: return 0.009255462182712733f;
+      default: return 0.00833056343336287f;
+    }
+  }
+  const float kp = k + 1.0f;
+  const float r2 = 1.0f / (kp * kp);
+  return (0.08333333333333333f - (0.002777777777777778f - 0.0007936507936507937f * r2) * r2) / kp;
+}
+
 // 24-bit uniforms in [0, 1) and (0, 1) for the FP32 samplers of the production mode
 __device__ __forceinline__ float u24open(uint32_t w) { return ((float)(w >> 8) + 0.5f) * 5.9604644775390625e-8f; }
 __device__ __forceinline__ float u24(uint32_t w) { return (float)(w >> 8) * 5.9604644775390625e-8f; }
 
 // Poisson(lam) for the production mode: the FP64 sampler's two methods
-// (inversion below lam = 10; Hormann's PTRS transformed rejection above) with
-// the per-draw arithmetic in FP32; PTRS's final log-density test, between its
-// squeezes, stays in FP64 (k log lam - lam - log k! cancels to a few units
-// from terms of order lam log lam).  Both loops are bounded.
+// (inversion below lam = 10; Hormann's PTRS transformed rejection above) in
+// FP32.  PTRS's final log-density test, k log lam - lam - log k!, cancels to a
+// few units from terms of order lam log lam; it is evaluated in the form
+// (d - k log1p(d / lam)) - log(k + 1)/2 - log(2 pi)/2 - fc(k), d = k + 1 - lam,
+// whose terms are of order d, so FP32 keeps it to ~1e-7 |d| (GB300 runs FP64
+// and its conversions at 1/64 of the FP32 rate).  Both loops are bounded.
 __device__ inline int poisson32(Rng& r, float lam) {
   if (!(lam > 0.0f)) return 0;
   if (lam > 1.0e9f) return 1000000000;  // far above the production mode's count limit (2^23), reported there
@@ -48,18 +72,18 @@ __device__ inline int poisson32(Rng& r, float lam) {
     const float kd = floorf((((2.0f * a) / us + b) * U + lam) + 0.43f);
     if (us >= 0.07f && V <= vr) return (int)kd;
     if (kd < 0.0f || (us < 0.013f && V > us)) continue;
-    const double ld = (double)lam, kk = (double)kd;
-    const double lhs = xlog(((double)V * (double)inv_alpha) / ((double)a / ((double)us * (double)us) + (double)b));
-    const double rhs = (kk * xlog(ld) - ld) - logfact(kk);
+    const float lhs = logf((V * inv_alpha) / (a / (us * us) + b));
+    const float d = (kd + 1.0f) - lam;
+    const float rhs = ((d - kd * log1pf(d / lam)) - 0.5f * logf(kd + 1.0f)) - 0.91893853320467274f - stirling_fc32(kd);
     if (lhs <= rhs) return (int)kd;
   }
   return (int)floorf(lam + 0.5f);
 }
 
 // initial_count (model.cuh) with FP32 arithmetic and the FP32 Poisson sampler:
-// the same moment-matched zero-inflated Poisson given G.
-__device__ inline int initial_count32(const PRec& R, int G, uint32_t wz, Rng& aux) {
-  const float g = (float)R.g0, m = (float)R.u0, c = (float)R.c0, v = (float)R.v0;
+// the same moment-matched zero-inflated Poisson given G, from the periodic
+// moments (g0, u0, c0, v0) in FP32.
+__device__ inline int initial_count32(float g, float m, float c, float v, int G, uint32_t wz, Rng& aux) {
   float mu = m, vr = v;
   if (g > 0.0f && g < 1.0f) {
     mu = G ? m + c / g : m - c / (1.0f - g);
@@ -79,13 +103,14 @@ __device__ inline int initial_count32(const PRec& R, int G, uint32_t wz, Rng& au
 // ---------------------------------------------------------------------------
 // Binomial capture for the FP32 production mode: the same two methods as the
 // FP64 samplers of common.cuh (inversion below n p = 10, Kachitvichyanukul &
-// Schmeiser 1988; BTRD above, Hormann 1993) with the per-draw arithmetic in
-// FP32, which runs at the full rate where the FP64 samplers are bound by
-// GB300's narrow FP64 pipe.  Only BTRD's final exact test (the log-density
-// comparison between its two squeezes, a small fraction of the draws) stays
-// in FP64, where (n + 1) log(...) needs the precision.  Counts are below 2^23
-// in this mode.  A different realisation than the FP64 mode's, drawn from the
-// same distribution.
+// Schmeiser 1988; BTRD above, Hormann 1993) in FP32, which runs at the full
+// rate where the FP64 samplers are bound by GB300's narrow FP64 pipe.  BTRD's
+// final exact test (the log-density comparison between its two squeezes)
+// has terms (n + 1) log(...) of order n; it is evaluated with log1p of the
+// ratios' distances from 1, (n + 2) p - (j + 1) formed by one FMA, so each
+// term is of order |k - m| and FP32 keeps the sum to ~1e-7 of that.  Counts
+// are below 2^23 in this mode.  A different realisation than the FP64 mode's,
+// drawn from the same distribution.
 // ---------------------------------------------------------------------------
 __device__ inline int binv32(Rng& rr, int n, float p) {
   const float q = 1.0f - p;
@@ -159,24 +184,27 @@ __device__ inline int btrd32(Rng& rr, int n, float p) {
     const float t = (-km * km) / (2.0f * npq);
     if (lv < t - rho) return (int)kd;
     if (lv > t + rho) continue;
-    // exact test in FP64 (log f(k) - log f(m) against log v)
-    const double ndd = (double)n, pdd = (double)p, rd = pdd / (1.0 - pdd), md = (double)m, kdd = (double)kd;
-    const double nm = (ndd - md) + 1.0, nk = (ndd - kdd) + 1.0;
-    const double h = ((md + 0.5) * xlog((md + 1.0) / (rd * nm)) + stirling_fc(md)) + stirling_fc(ndd - md);
-    const double bound = (((h + (ndd + 1.0) * xlog(nm / nk)) + (kdd + 0.5) * xlog((nk * rd) / (kdd + 1.0))) -
-                          stirling_fc(kdd)) - stirling_fc(ndd - kdd);
-    if ((double)lv <= bound) return (int)kd;
+    // exact test: log f(k) - log f(m) against log v, with
+    //   log((m + 1) / (r nm)) = -log1p(em),  em = ((n + 2) p - (m + 1)) / ((m + 1) q),
+    //   log(nm / nk) = log1p((k - m) / nk),  log(nk r / (k + 1)) = log1p(ek), likewise
+    const float nk = (nd - kd) + 1.0f;
+    const float em = fmaf(nd + 2.0f, p, -(m + 1.0f)) / ((m + 1.0f) * q);
+    const float ek = fmaf(nd + 2.0f, p, -(kd + 1.0f)) / ((kd + 1.0f) * q);
+    const float h = ((m + 0.5f) * -log1pf(em) + stirling_fc32(m)) + stirling_fc32(nd - m);
+    const float bound = (((h + (nd + 1.0f) * log1pf((kd - m) / nk)) + (kd + 0.5f) * log1pf(ek)) -
+                         stirling_fc32(kd)) - stirling_fc32(nd - kd);
+    if (lv <= bound) return (int)kd;
   }
   return (int)floorf(nd * p + 0.5f);
 }
 
-__device__ __forceinline__ int64_t binomial32(Rng& r, int64_t n, double p) {
-  if (n <= 0 || !(p > 0.0)) return 0;
-  if (p >= 1.0) return n;
-  const bool flip = p > 0.5;
-  const float pp = (float)(flip ? 1.0 - p : p);
-  const int ni = (int)n;
-  const int k = ((float)ni * pp < 10.0f) ? binv32(r, ni, pp) : btrd32(r, ni, pp);
+// Bin(n, p) for a capture efficiency p given in FP32 (1 - p is exact for p > 1/2)
+__device__ __forceinline__ int binomial32(Rng& r, int n, float p) {
+  if (n <= 0 || !(p > 0.0f)) return 0;
+  if (p >= 1.0f) return n;
+  const bool flip = p > 0.5f;
+  const float pp = flip ? 1.0f - p : p;
+  const int k = ((float)n * pp < 10.0f) ? binv32(r, n, pp) : btrd32(r, n, pp);
   return flip ? n - k : k;
 }
 

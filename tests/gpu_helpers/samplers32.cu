@@ -17,7 +17,7 @@ __global__ void draw_kernel(int kind, long long n, double p, float lam, long lon
     abc::Rng r;
     abc::rng_init(r, seed, 2u, (uint32_t)i, (uint32_t)(i >> 32));
     long long x = 0;
-    if (kind == 0) x = abc::binomial32(r, n, p);
+    if (kind == 0) x = abc::binomial32(r, (int)n, (float)p);
     if (kind == 1) x = abc::binomial(r, n, p);
     if (kind == 2) x = abc::poisson32(r, lam);
     if (kind == 3) x = abc::poisson(r, (double)lam);
