@@ -67,6 +67,7 @@ struct abc_ctx {
   DBuf<uint32_t> d_id;
   DBuf<double> d_beta, d_age_dist;
   DBuf<float> d_beta32;  // capture efficiencies in FP32 for the production mode's capture
+  int64_t max_group_cells = INT64_MAX;  // cells of the largest (condition, age) group
   // simulation workspace
   DBuf<double> d_theta, d_stats;
   DBuf<int32_t> d_models;
@@ -330,6 +331,8 @@ int abc_set_cells(abc_ctx* c, int64_t n_cells, const int32_t* cell_cond, const i
   CK(cudaMemcpy(c->d_age_dist.p, age_dist, sizeof(double) * NG, cudaMemcpyHostToDevice));
   c->perm = perm;
   c->C = n_cells;
+  c->max_group_cells = 0;
+  for (int g = 0; g < NG; ++g) c->max_group_cells = std::max<int64_t>(c->max_group_cells, gs[g + 1] - gs[g]);
   c->cells_set = true;
   return ABC_OK;
 }
@@ -499,6 +502,7 @@ static int enqueue_simulate(abc_ctx* c, int model, const int32_t* d_models, cons
     st.captured = want_cells ? c->d_captured.p : nullptr;
     st.fp32 = fp64 ? 0 : 1;
     st.beta32 = c->d_beta32.p;
+    st.max_group_cells = c->max_group_cells;
     CK(launch_stats(st, c->stream));
     CK(prof_mark(c));
   }

@@ -22,6 +22,7 @@ struct StatsArgs {
   int2* captured;            // optional [P][C]
   int fp32 = 0;              // production mode: FP32 binomial capture (a different realisation)
   const float* beta32 = nullptr;  // [C] the capture efficiencies in FP32 (production mode)
+  int64_t max_group_cells = INT64_MAX;  // cells of the largest (condition, age) group
 };
 
 struct SetupArgs {

@@ -1,6 +1,8 @@
 // kernels_fp64.cu — prior draw, particle setup, FP64 (oracle-mode) SSA and the
 // fused capture + statistics kernel.  Built with -fmad=false: every FP64
 // result here is bit-identical to the FP64 CPU oracle.
+#include <type_traits>
+
 #include "kernels.h"
 #include "sampler32.cuh"
 
@@ -262,7 +264,10 @@ __device__ __forceinline__ __int128 shfl_xor_i128(__int128 v, int o) {
   return (__int128)(((unsigned __int128)(unsigned long long)hi << 64) | (unsigned __int128)lo);
 }
 
-template <bool CAP32>
+// NARROW: 64-bit sums of the squared counts (production mode: counts at most
+// 2^24, where FP32 increments stop, and at most 2^14 cells per group, so the
+// sums stay below 2^62); 128-bit otherwise.
+template <bool CAP32, bool NARROW>
 __global__ void __launch_bounds__(256) stats_kernel(StatsArgs A) {
   __shared__ double mom[kMaxAges * kMaxConds * 5];
   __shared__ double wts[kMaxAges * kMaxConds];
@@ -275,8 +280,9 @@ __global__ void __launch_bounds__(256) stats_kernel(StatsArgs A) {
     const uint32_t pg = (uint32_t)(A.p_offset + p);
     for (int g = warp; g < ng; g += (blockDim.x >> 5)) {
       const int g0 = A.gstart[g], g1 = A.gstart[g + 1];
+      using Sq = typename std::conditional<NARROW, long long, __int128>::type;
       long long su = 0, sl = 0;
-      __int128 suu = 0, sll = 0, sul = 0;
+      Sq suu = 0, sll = 0, sul = 0;
       for (int i = g0 + lane; i < g1; i += 32) {
         int2 c = cnt[i];
         Rng r;
@@ -293,30 +299,34 @@ __global__ void __launch_bounds__(256) stats_kernel(StatsArgs A) {
         if (A.captured) A.captured[p * A.n_cells + i] = make_int2((int)cu, (int)cl);
         su += cu;
         sl += cl;
-        suu += (__int128)(cu * cu);
-        sll += (__int128)(cl * cl);
-        sul += (__int128)(cu * cl);
+        suu += (Sq)(cu * cu);
+        sll += (Sq)(cl * cl);
+        sul += (Sq)(cu * cl);
       }
       for (int o = 16; o > 0; o >>= 1) {
         su += shfl_xor_ll(su, o);
         sl += shfl_xor_ll(sl, o);
-        suu += shfl_xor_i128(suu, o);
-        sll += shfl_xor_i128(sll, o);
-        sul += shfl_xor_i128(sul, o);
+        if (NARROW) {
+          suu += (Sq)shfl_xor_ll((long long)suu, o);
+          sll += (Sq)shfl_xor_ll((long long)sll, o);
+          sul += (Sq)shfl_xor_ll((long long)sul, o);
+        } else {
+          suu += (Sq)shfl_xor_i128((__int128)suu, o);
+          sll += (Sq)shfl_xor_i128((__int128)sll, o);
+          sul += (Sq)shfl_xor_i128((__int128)sul, o);
+        }
       }
-      if (lane == 0) {
-        long long n = g1 - g0;
-        double nd = (double)n;
-        double dn = nd * (double)(n - 1);
-        __int128 nvu = (__int128)n * suu - (__int128)su * su;
-        __int128 ncv = (__int128)n * sul - (__int128)su * sl;
-        __int128 nvl = (__int128)n * sll - (__int128)sl * sl;
-        double* m = mom + g * 5;
-        m[0] = (double)su / nd;
-        m[1] = (double)sl / nd;
-        m[2] = i128_to_double(nvu) / dn;
-        m[3] = i128_to_double(ncv) / dn;
-        m[4] = i128_to_double(nvl) / dn;
+      if (lane < 5) {  // lane j forms moment j: [E u, E l, Var u, Cov ul, Var l], one FP64 division each
+        const long long n = g1 - g0;
+        const double nd = (double)n;
+        const double dn = nd * (double)(n - 1);
+        __int128 x;
+        if (lane == 0) x = su;
+        else if (lane == 1) x = sl;
+        else if (lane == 2) x = (__int128)n * suu - (__int128)su * su;
+        else if (lane == 3) x = (__int128)n * sul - (__int128)su * sl;
+        else x = (__int128)n * sll - (__int128)sl * sl;
+        mom[g * 5 + lane] = i128_to_double(x) / (lane < 2 ? nd : dn);
       }
     }
     __syncthreads();
@@ -329,10 +339,12 @@ __global__ void __launch_bounds__(256) stats_kernel(StatsArgs A) {
 cudaError_t launch_stats(const StatsArgs& a, cudaStream_t s) {
   if (a.n_particles <= 0) return cudaSuccess;
   int blocks = (int)(a.n_particles < 1048576 ? a.n_particles : 1048576);
-  if (a.fp32)
-    stats_kernel<true><<<blocks, 256, 0, s>>>(a);
+  if (a.fp32 && a.max_group_cells <= 16384)
+    stats_kernel<true, true><<<blocks, 256, 0, s>>>(a);
+  else if (a.fp32)
+    stats_kernel<true, false><<<blocks, 256, 0, s>>>(a);
   else
-    stats_kernel<false><<<blocks, 256, 0, s>>>(a);
+    stats_kernel<false, false><<<blocks, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 

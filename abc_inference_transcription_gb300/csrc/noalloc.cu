@@ -249,6 +249,7 @@ extern "C" int abc_simulate_noalloc(const abc_config* cfg, int model, int64_t n_
   sta.captured = nullptr;
   sta.fp32 = fp64 ? 0 : 1;
   sta.beta32 = d_beta32;
+  sta.max_group_cells = *std::max_element(count.begin(), count.end());
   NA_CK(launch_stats(sta, stream));
 
   int hs = 0;
