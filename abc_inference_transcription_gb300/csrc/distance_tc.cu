@@ -411,7 +411,6 @@ __global__ void __launch_bounds__(kThreads, 1)
 // the whole gene row is resident, so any gene K-step is at hand.
 // ---------------------------------------------------------------------------
 constexpr int kResMaxStages = 4;
-constexpr int kResPrefetch = 2;  // particle tiles ahead whose rows are prefetched into L2
 constexpr uint32_t kResSmemMax = 227u * 1024u;  // dynamic shared memory of one CTA
 
 __host__ __device__ constexpr uint32_t res_smem(int n_chunks, int stages) {
@@ -489,11 +488,6 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int c = 0; c < NC; ++c) tma_load(b_base + (uint32_t)c * kBBytes, &tmB, bfull, c * kEl, n * BN);
         ++b_issued;
         for (int m = j; m < a.nM && ok; m += cpt) {
-          // the particle rows of the tile kResPrefetch steps ahead start their way from DRAM into L2
-          // now, so that the ring's loads (at most S chunks ahead of the MMAs) find them there
-          const int mp = m + kResPrefetch * cpt;
-          if (mp < a.nM)
-            for (int c = 0; c < NC; ++c) tma_prefetch_l2(&tmA, c * kEl, mp * BM);
           for (int c = 0; c < NC; ++c) {
             if (!mbar_wait(&empty[stage], phase ^ 1)) {
               atomicOr(a.err, kErrProducer);

@@ -43,41 +43,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
   return true;
 }
 
-// As mbar_wait, but each probe may suspend the thread (up to ns nanoseconds)
-// until the phase completes, so a long wait takes no issue slots from the
-// warps that share the scheduler.
-__device__ __forceinline__ bool mbar_try_sleep(uint64_t* b, uint32_t parity, uint32_t ns) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(su32(b)), "r"(parity), "r"(ns)
-      : "memory");
-  return ok != 0;
-}
-__device__ __forceinline__ bool mbar_wait_sleep(uint64_t* b, uint32_t parity) {
-  if (mbar_try_sleep(b, parity, 20000u)) return true;
-  const long long t0 = clock64();
-  while (!mbar_try_sleep(b, parity, 20000u))
-    if (clock64() - t0 > kWaitLimit) return false;
-  return true;
-}
-
 __device__ __forceinline__ void tma_load(uint32_t dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
   asm volatile(
       "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], "
       "[%2];" ::"r"(dst),
       "l"(reinterpret_cast<uint64_t>(map)), "r"(su32(bar)), "r"(x), "r"(y)
       : "memory");
-}
-
-// Bring one box of a tiled tensor into L2 (no shared-memory destination, no barrier).
-__device__ __forceinline__ void tma_prefetch_l2(const CUtensorMap* map, int x, int y) {
-  asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"(reinterpret_cast<uint64_t>(map)),
-               "r"(x), "r"(y)
-               : "memory");
 }
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
