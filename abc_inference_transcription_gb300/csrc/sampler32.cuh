@@ -1,9 +1,10 @@
 // sampler32.cuh — FP32 samplers of the production mode: Poisson (initial
 // states), binomial (capture) and the moment-matched initial count.  The
-// same methods as the FP64 samplers of common.cuh, with the per-draw
-// arithmetic in FP32; each algorithm's final exact log-density test, a small
-// fraction of the draws, stays in FP64.  Device code only; tested directly
-// against the exact distributions (tests/test_samplers32.py).
+// same methods as the FP64 samplers of common.cuh, with all arithmetic in
+// FP32, the final exact log-density tests included (each rewritten in log1p
+// form so that its terms stay of the order of the deviation, not of n).
+// Device code only; tested directly against the exact distributions
+// (tests/test_samplers32.py).
 #pragma once
 #include "common.cuh"
 #include "model.cuh"
