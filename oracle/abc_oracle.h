@@ -12,6 +12,13 @@
  *         bit-exact partner of the GPU FP64 mode
  *   (iii) distance + acceptance (scripts/compute_errors.jl:30-70,
  *         scripts/accepted_particles.jl:9-32)
+ *
+ * How each is pinned: (i) against the reference's golden outputs
+ * data/recovered_statistics (fixtures in tests/golden/); the Philox stream
+ * against the Random123 known-answer vectors; (ii) statistically against (i);
+ * (iii) parity unpinned -- the reference ships no error matrix, accepted list
+ * or raw data to recompute them from, so (iii) is checked only against an
+ * independent numpy restatement of the same formulas.
  */
 #ifndef ABC_ORACLE_H
 #define ABC_ORACLE_H

@@ -3,6 +3,12 @@
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() (as the
 checker) and bench.py's CPU-baseline / reference arm.  The product never
 imports this module.
+
+Pinning: the moment ODE against the reference's data/recovered_statistics
+(tests/golden/), Philox against the Random123 known-answer vectors, the FP64
+SSA statistically against the moment ODE; errors() and accept(): parity
+unpinned (no reference error matrix or accepted list exists), checked against
+an independent numpy restatement.
 """
 from __future__ import annotations
 
